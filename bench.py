@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""agent-steps/s of the chili mechanics/interaction step on GB300.
+
+One bench step = one complete run of the workload from its initial state: for the default
+workload (rods_2d) 100,000 bacterial rods x 6 vertices, 500 explicit-Euler steps in FP64.
+  value  device-resident throughput: the initial state is restored on the device (crg_snapshot)
+         and the 500 steps run from CUDA graphs; CUDA events on the library's stream bracket
+         the K timed steps; L2 is flushed (256 MiB write) between timed steps.
+  e2e    the same run through the public C ABI with host buffers: crg_upload from pinned
+         host memory, crg_step, crg_download to host, every bench step.
+  cpu_baseline  the oracle (a C++ restatement of chili, multi-threaded by subdomains like
+         chili) on the host cores on a bounded sample of the same workload.
+--impl reference times that CPU implementation alone, with all host threads.
+
+Multi-GPU: the path is replicated, not sharded (independent simulations); each rank runs
+the workload on its own GPU and rank 0 reports the sum of agent-steps over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "agent-steps/s on 1 GB300: FP64 plain vs mixed/batched; served p50/p99 latency"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="crg", choices=["crg", "reference"])
+    p.add_argument("--workload", default="rods_2d", choices=["rods_2d", "spheres_3d"])
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(name, n_sub):
+    from cellular_raza_gb300 import workloads as W
+
+    if name == "rods_2d":
+        return W.rods_2d(seed=2024, n_subdomains=n_sub)
+    return W.spheres_3d(seed=2024, n_subdomains=n_sub)
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def committed_traffic(kernel_key):
+    """Per-launch DRAM bytes of the force kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel_key)
+    except (OSError, ValueError):
+        return None
+
+
+# ----------------------------------------------------------------------------- CPU arms
+
+def cpu_run(w, n_threads, seconds, max_steps):
+    """Times the oracle on a bounded sample: steps chosen so the run takes ~`seconds`."""
+    import pyoracle
+
+    pyoracle.build()
+    m = w.model.replace(n_subdomains=n_threads)
+    probe = pyoracle.run(m, w.pos, w.vel, 1)["elapsed_s"]
+    steps = int(max(1, min(max_steps, seconds / max(probe, 1e-6))))
+    r = pyoracle.run(m, w.pos, w.vel, steps)
+    return {"value": w.n * steps / r["elapsed_s"], "unit": "agent-steps/s", "cores": n_threads,
+            "kind": "port",
+            "sample": f"{w.name}: {w.n} agents x {steps} of {w.n_steps} steps, "
+                      f"{n_threads} threads = {n_threads} chili subdomains "
+                      f"({r['elapsed_s']:.1f} s)"}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n_threads = os.cpu_count() or 1
+    w = make_workload(args.workload, n_threads)
+    import pyoracle
+
+    pyoracle.build()
+    m = w.model.replace(n_subdomains=n_threads)
+    probe = pyoracle.run(m, w.pos, w.vel, 1)["elapsed_s"]
+    # each bench step is a bounded sample of the workload sized to ~8 s
+    steps = int(max(1, min(w.n_steps, 8.0 / max(probe, 1e-6))))
+    for _ in range(args.warmup):
+        pyoracle.run(m, w.pos, w.vel, 1)
+    t_total = 0.0
+    for _ in range(args.steps):
+        t_total += pyoracle.run(m, w.pos, w.vel, steps)["elapsed_s"]
+    value = w.n * steps * args.steps / t_total
+    sample = (f"{w.name}: {w.n} agents x {steps} of {w.n_steps} steps per bench step, "
+              f"{n_threads} threads")
+    line = {
+        "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64)", "impl": "reference",
+        "config": {"workload": w.name, "agents": w.n, "sim_steps_per_bench_step": steps,
+                   "n_subdomains": n_threads},
+        "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": n_threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+
+def algorithmic_flops(w, stats):
+    """FP64 work one force launch must do once the FP32 prefilter has removed the
+    evaluations beyond the cutoff (sqrt, exp, division count one flop each).
+    spheres: 30 flop per interacting ordered pair (8 distance + 22 force) + 21 per agent
+    (update); rods: 45 flop per in-range vertex-segment evaluation (18 nearest point,
+    6 distance, 21 force) + 250 per rod (springs, curvature, update)."""
+    n_inter = float(stats["n_inter"].astype("float64").sum())
+    if w.model.kind == "rod":
+        return 45.0 * n_inter + 250.0 * w.n
+    return 30.0 * n_inter + 21.0 * w.n
+
+
+def crg_arm(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import numpy as np
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    from cellular_raza_gb300 import _native as N
+    from cellular_raza_gb300 import engine as E
+
+    n_cpu = os.cpu_count() or 1
+    w = make_workload(args.workload, n_cpu)
+    sim = E.Simulation.single(w.model, w.n)
+    sim.upload(w.pos, w.vel)
+    sim.snapshot()
+    stats = sim.neighbor_stats()
+    ext = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def run_once():
+        sim.snapshot(restore=True)
+        sim.step(w.n_steps)
+
+    for _ in range(max(args.warmup, 3)):
+        run_once()
+    torch.cuda.synchronize()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(ext)
+        for k in range(args.steps):
+            run_once()
+            if k + 1 < args.steps:
+                with torch.cuda.stream(ext):
+                    flush.zero_()
+        ev1.record(ext)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    t_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    agent_steps = w.n * w.n_steps * args.steps * world
+    value = agent_steps / (t_max / 1e3)
+
+    # e2e through the C ABI with host buffers (pinned)
+    nbytes = w.pos.size * 8
+    pin_pos = torch.from_numpy(w.pos.reshape(-1).copy()).pin_memory()
+    pin_vel = torch.from_numpy(w.vel.reshape(-1).copy()).pin_memory()
+    out_pos = torch.empty(w.pos.size, dtype=torch.float64).pin_memory()
+    out_vel = torch.empty(w.pos.size, dtype=torch.float64).pin_memory()
+    out_ids = torch.empty(w.n, dtype=torch.int64).pin_memory()
+    out_vox = torch.empty(w.n, dtype=torch.int32).pin_memory()
+    L = N.load()
+    dp = C.POINTER(C.c_double)
+
+    def e2e_once():
+        rc = L.crg_upload(sim._h, w.n, None, C.cast(pin_pos.data_ptr(), dp),
+                          C.cast(pin_vel.data_ptr(), dp), None)
+        N.check(rc, "crg_upload", sim._h)
+        sim.step(w.n_steps)
+        rc = L.crg_download(sim._h, C.cast(out_pos.data_ptr(), dp),
+                            C.cast(out_vel.data_ptr(), dp),
+                            C.cast(out_ids.data_ptr(), C.POINTER(C.c_uint64)),
+                            C.cast(out_vox.data_ptr(), C.POINTER(C.c_uint32)))
+        N.check(rc, "crg_download", sim._h)
+
+    for _ in range(max(args.warmup, 3)):
+        e2e_once()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for k in range(args.steps):
+        e2e_once()
+        if k + 1 < args.steps:
+            with torch.cuda.stream(ext):
+                flush.zero_()
+    e1.record(ext)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = agent_steps / (e2e_ms / 1e3)
+    h2d = 2 * nbytes
+    d2h = 2 * nbytes + 8 * w.n + 4 * w.n
+
+    # roofline of the dominant (force) kernel: per-launch device time with CUDA events on
+    # the library's stream, from a profiled pass over the same run
+    sim.set_option(N.OPT_PROFILE, 1)
+    sim.snapshot(restore=True)
+    prof_steps = min(w.n_steps, 100)
+    sim.step(prof_steps)
+    prof = sim.profile()
+    sim.set_option(N.OPT_PROFILE, 0)
+    force_ms = prof["force_ms"] / prof_steps
+    sort_ms = prof["sort_ms"] / prof_steps
+    flops = algorithmic_flops(w, stats)
+    peaks = measured_peaks()
+    fma = E.measure_fma_peaks()
+    fp64_peak = fma["fp64_tflops"]
+    achieved = flops / (force_ms * 1e-3) / 1e12
+    kernel_key = f"{args.workload}_force"
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak if fp64_peak else None,
+                "traffic": committed_traffic(kernel_key),
+                "peak_source": "measured DFMA microbenchmark (crg_measure_fma_peaks) on this GPU",
+                "kernel": "k_rods_step" if w.model.kind == "rod" else "k_spheres_step",
+                "force_ms_per_launch": force_ms, "sort_ms_per_step": sort_ms,
+                "algorithmic_flop_per_launch": flops}
+    # the sort kernels are HBM-bound: algorithmic bytes per step
+    nc = w.model.nc
+    sort_bytes = w.n * (2 * 2 * 8 * nc + 2 * 8 + 4 * 4 + 4 * nc + 8 * 3)
+    hbm = peaks.get("hbm_gbs")
+    roofline_sort = {"bound": "hbm", "achieved": sort_bytes / (sort_ms * 1e-3) / 1e9,
+                     "peak": hbm, "unit": "GB/s",
+                     "frac": (sort_bytes / (sort_ms * 1e-3) / 1e9 / hbm) if hbm else None,
+                     "bytes_per_step": sort_bytes}
+    gpu_launches = prof["kernels"] // prof_steps * w.n_steps * args.steps if prof_steps else None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_run(w, n_cpu, args.cpu_seconds, w.n_steps)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": w.name, "agents": w.n,
+                       "vertices_per_agent": w.model.n_vertices, "dim": w.model.dim,
+                       "sim_steps_per_bench_step": w.n_steps, "solver": "euler",
+                       "precision": "f64", "n_subdomains": n_cpu,
+                       "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "agent-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": roofline,
+            "roofline_sort": roofline_sort,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": gpu_launches,
+            "fma_peaks_tflops": fma,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        crg_arm(args)
+
+
+if __name__ == "__main__":
+    main()

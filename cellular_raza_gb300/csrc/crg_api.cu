@@ -1,0 +1,790 @@
+// crg_api.cu -- the C ABI (include/crg.h): handles, upload/step/download, graphs.
+//
+// A handle owns one "pack": one or more simulations of the same agent kind, dimension,
+// precision and solver order, stored back to back in component-major SoA buffers and
+// advanced by the same kernel launches.  One step is
+//   force+update kernel  (crg_spheres.cu / crg_rods.cu: forces, solver, boundary, next key,
+//                         histogram of next keys)
+//   sort                 (crg_sort.cu: scan, scatter, per-voxel order, gather)
+// and runs on the handle's stream; steps are captured into CUDA graphs in chunks.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "crg_internal.cuh"
+#include "crg_kernels.h"
+
+using crg::PackArgs;
+using crg::SimDev;
+using crg::SortArgs;
+
+struct crg_ctx {
+  int dim = 3, kind = CRG_KIND_SPHERE, nv = 1, nc = 3, precision = CRG_PREC_F64, order = 1;
+  int n_sims = 1;
+  std::vector<SimDev> sims_h;
+  std::vector<int64_t> caps;
+  std::vector<uint32_t> agent_off_h;  // [n_sims + 1]
+  int64_t cap = 0;
+  uint32_t n_agents = 0;
+  uint32_t n_vox = 0;
+  // device memory
+  SimDev *d_sims = nullptr;
+  uint32_t *d_agent_off = nullptr, *d_sim_of_voxel = nullptr;
+  double *pos = nullptr, *vel = nullptr, *npos = nullptr, *nvel = nullptr;
+  uint64_t *id = nullptr, *nid = nullptr;
+  uint32_t *key = nullptr, *nkey = nullptr;
+  float *off = nullptr;
+  double *hist = nullptr, *nhist = nullptr;
+  uint8_t *hmeta = nullptr, *nhmeta = nullptr;
+  uint32_t *count = nullptr, *start = nullptr, *bsum = nullptr;
+  uint64_t *tmp = nullptr;
+  int32_t *status = nullptr;
+  int64_t *step_ctr = nullptr;
+  double *dbg_force = nullptr;
+  double *staging = nullptr;
+  char *snap = nullptr;  // crg_snapshot buffer
+  uint32_t snap_agents = 0;
+  int64_t snap_steps = 0;
+  int32_t *h_status = nullptr;  // pinned
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int gexec_steps = 0;
+  int graph_chunk = 32;
+  int prefilter = 1;
+  int block = 0;
+  int profile = 0;
+  double prof_ms[3] = {0, 0, 0};
+  int32_t err_code = CRG_OK;
+  int64_t err_agent = -1, err_step = -1;
+  int64_t steps_done = 0;
+};
+
+namespace {
+
+#define CUDA_TRY(expr)                                  \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) {                            \
+      return e_ == cudaErrorMemoryAllocation ? CRG_ENOMEM : CRG_ECUDA; \
+    }                                                   \
+  } while (0)
+
+bool to_usize_h(double x, uint64_t &out) {
+  if (x > -1.0 && x < 18446744073709551616.0) {
+    out = (uint64_t)x;
+    return true;
+  }
+  return false;
+}
+
+// get_decomp_res (cellular_raza-building-blocks/src/domains/cartesian_cuboid_n.rs:19-59).
+bool decomp_res(uint64_t n_voxel, uint64_t n_regions, uint64_t &n_out, uint64_t &m_out,
+                uint64_t &avg_out) {
+  int64_t average_len = (int64_t)std::ceil((double)n_voxel / (double)n_regions);
+  int64_t n = (int64_t)n_regions, m = 0;
+  for (uint64_t it = 0; it < n_regions; ++it) {
+    int64_t r = (int64_t)n_voxel - average_len * n - (average_len - 1) * m;
+    if (r == 0) {
+      n_out = (uint64_t)n;
+      m_out = (uint64_t)m;
+      avg_out = (uint64_t)average_len;
+      return true;
+    } else if (r > 0) {
+      if (n == (int64_t)n_regions) {
+        average_len += 1;
+        n = (int64_t)n_regions;
+        m = 0;
+      }
+    } else {
+      n -= 1;
+      m += 1;
+    }
+  }
+  return false;
+}
+
+// Fills the geometry and parameters of one simulation descriptor.
+int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
+  std::memset(&S, 0, sizeof(S));
+  if (d.dim != 2 && d.dim != 3) return CRG_EINVAL;
+  S.dim = d.dim;
+  uint64_t total = 1;
+  for (int i = 0; i < 3; ++i) S.nvox[i] = 1;
+  for (int i = 0; i < d.dim; ++i) {
+    if (!(d.min[i] < d.max[i])) return CRG_EBOUNDARY;  // check_min_max (:149-162)
+    S.min[i] = d.min[i];
+    S.max[i] = d.max[i];
+    uint64_t nvox;
+    if (d.voxel_mode == 0) {
+      // from_boundaries_and_interaction_range (cartesian_cuboid_n.rs:183-222)
+      if (!(d.interaction_range > 0.0)) return CRG_EINVAL;
+      double n = std::floor((d.max[i] - d.min[i]) / d.interaction_range);
+      uint64_t mm;
+      if (!to_usize_h(n, mm)) return CRG_EBOUNDARY;
+      nvox = std::max<uint64_t>(mm, 1);
+      S.dx[i] = (d.max[i] - d.min[i]) / n;
+    } else {
+      // from_boundaries_and_n_voxels (cartesian_cuboid_n.rs:226-256)
+      if (d.n_voxels[i] <= 0) return CRG_EINVAL;
+      nvox = (uint64_t)d.n_voxels[i];
+      S.dx[i] = (d.max[i] - d.min[i]) / (double)nvox;
+    }
+    if (nvox > (1u << 30)) return CRG_ENOTSUP;
+    S.nvox[i] = (int32_t)nvox;
+    total *= nvox;
+    if (total > 0xffffffffull / 2) return CRG_ENOTSUP;
+  }
+  S.n_vox = (uint32_t)total;
+  if (d.n_subdomains < 1) return CRG_EINVAL;
+  uint64_t n, mm, avg;
+  if ((uint64_t)d.n_subdomains > total || !decomp_res(total, (uint64_t)d.n_subdomains, n, mm, avg))
+    return CRG_EDECOMPOSE;
+  S.sd_switch = (uint32_t)(n * avg);
+  S.sd_avg = (uint32_t)avg;
+  S.sd_div2 = (uint32_t)std::max<uint64_t>(avg - 1, 1);
+  S.sd_n = (uint32_t)n;
+  S.weight_mode = d.weight_mode;
+  S.mass = m.mass;
+  S.damping = m.damping;
+  S.spring_tension = m.spring_tension;
+  S.rigidity = m.rigidity;
+  S.spring_length = m.spring_length;
+  S.radius = m.radius;
+  S.stiffness = m.stiffness;
+  S.cutoff = m.cutoff;
+  S.strength = m.strength;
+  S.dt = m.dt;
+  S.order = m.solver_order;
+  S.radius_f = (float)m.radius;
+  S.stiffness_f = (float)m.stiffness;
+  S.cutoff_f = (float)m.cutoff;
+  S.strength_f = (float)m.strength;
+  double dxmax = 0.0;
+  for (int i = 0; i < d.dim; ++i) {
+    S.dxf[i] = (float)S.dx[i];
+    if (std::isfinite(S.dx[i])) dxmax = std::max(dxmax, S.dx[i]);
+  }
+  // FP32 offsets are trusted while |off| <= off_lim.  Every FP32 quantity entering the
+  // prefilter distance is then within a few ulps of off_lim (offset roundings, the corner
+  // shift, the differences), so its absolute error is bounded by 16 * off_lim * 2^-24 per
+  // axis.  The margin below is more than 100 times that bound.
+  double ext = (m.kind == CRG_KIND_ROD) ? 4.0 * (m.n_vertices - 1) * std::fabs(m.spring_length) : 0.0;
+  double off_lim = 4.0 * dxmax + ext + 1.0;
+  double err = 16.0 * off_lim * std::ldexp(1.0, -24) * std::sqrt((double)d.dim);
+  double margin = 128.0 * err + 1e-4 * std::fabs(m.cutoff) + 1e-6;
+  double thr = std::fabs(m.cutoff) + margin;
+  S.off_lim = (float)off_lim;
+  S.filt_thr2 = (float)(thr * thr);
+  if (!std::isfinite(S.filt_thr2)) S.filt_thr2 = __builtin_inff();
+  return CRG_OK;
+}
+
+int32_t check_model(const crg_model &m) {
+  if (m.kind != CRG_KIND_SPHERE && m.kind != CRG_KIND_ROD) return CRG_EINVAL;
+  if (m.kind == CRG_KIND_SPHERE && m.n_vertices != 1) return CRG_EINVAL;
+  if (m.kind == CRG_KIND_ROD && (m.n_vertices < 2 || m.n_vertices > crg::kMaxVertices))
+    return CRG_ENOTSUP;
+  if (m.solver_order < 1 || m.solver_order > 3) return CRG_EINVAL;
+  if (m.precision != CRG_PREC_F64 && m.precision != CRG_PREC_MIXED) return CRG_EINVAL;
+  if (m.kind == CRG_KIND_ROD && m.precision != CRG_PREC_F64) return CRG_ENOTSUP;
+  if (m.diffusion != 0.0) return CRG_ENOTSUP;  // stochastic mechanics is not on this path
+  if (!(m.dt > 0.0)) return CRG_EINVAL;
+  return CRG_OK;
+}
+
+template <class T>
+int32_t dalloc(T **p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return e == cudaErrorMemoryAllocation ? CRG_ENOMEM : CRG_ECUDA;
+  }
+  return CRG_OK;
+}
+
+void free_all(crg_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
+                  c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
+                  c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
+                  c->step_ctr, c->dbg_force, c->staging, c->snap};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+int32_t allocate(crg_ctx *c) {
+  const int64_t cap = c->cap;
+  const int nc = c->nc;
+  int32_t r;
+#define A(ptr, n) \
+  if ((r = dalloc(&c->ptr, (size_t)(n))) != CRG_OK) return r
+  A(d_sims, c->n_sims);
+  A(d_agent_off, c->n_sims + 1);
+  A(pos, cap * nc);
+  A(vel, cap * nc);
+  A(npos, cap * nc);
+  A(nvel, cap * nc);
+  A(id, cap);
+  A(nid, cap);
+  A(key, cap);
+  A(nkey, cap);
+  A(off, cap * nc);
+  A(tmp, cap);
+  A(count, (size_t)c->n_vox + 1);
+  A(start, (size_t)c->n_vox + 1);
+  A(bsum, (size_t)c->n_vox / 4096 + 2);
+  A(status, 4);
+  A(step_ctr, 1);
+  A(staging, cap * nc);
+  if (c->order > 1) {
+    A(hist, cap * nc * 2);
+    A(nhist, cap * nc * 2);
+    A(hmeta, cap);
+    A(nhmeta, cap);
+  }
+  if (c->n_sims > 1) A(d_sim_of_voxel, c->n_vox);
+#undef A
+  CUDA_TRY(cudaMallocHost((void **)&c->h_status, 4 * sizeof(int32_t)));
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 4, c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->step_ctr, 0, sizeof(int64_t), c->stream));
+  if (c->n_sims > 1) {
+    std::vector<uint32_t> sov(c->n_vox);
+    for (int s = 0; s < c->n_sims; ++s)
+      for (uint32_t v = 0; v < c->sims_h[s].n_vox; ++v) sov[c->sims_h[s].voxel_off + v] = s;
+    CUDA_TRY(cudaMemcpy(c->d_sim_of_voxel, sov.data(), sizeof(uint32_t) * c->n_vox,
+                        cudaMemcpyHostToDevice));
+  }
+  return CRG_OK;
+}
+
+int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *models,
+                    const int64_t *capacities, crg_ctx **out) {
+  if (!out || n_sims < 1 || !domains || !models || !capacities) return CRG_EINVAL;
+  *out = nullptr;
+  crg_ctx *c = new (std::nothrow) crg_ctx();
+  if (!c) return CRG_ENOMEM;
+  const crg_model &m0 = models[0];
+  c->dim = domains[0].dim;
+  c->kind = m0.kind;
+  c->nv = m0.kind == CRG_KIND_ROD ? m0.n_vertices : 1;
+  c->nc = c->nv * c->dim;
+  c->precision = m0.precision;
+  c->order = m0.solver_order;
+  c->n_sims = n_sims;
+  c->sims_h.resize(n_sims);
+  c->caps.assign(capacities, capacities + n_sims);
+  uint64_t vox = 0;
+  int64_t cap = 0;
+  for (int s = 0; s < n_sims; ++s) {
+    const crg_model &m = models[s];
+    int32_t r = check_model(m);
+    if (r == CRG_OK && (m.kind != m0.kind || m.n_vertices != m0.n_vertices ||
+                        m.precision != m0.precision || m.solver_order != m0.solver_order ||
+                        domains[s].dim != c->dim))
+      r = CRG_EINVAL;
+    if (r == CRG_OK && capacities[s] < 0) r = CRG_EINVAL;
+    if (r == CRG_OK) r = fill_sim(domains[s], m, c->sims_h[s]);
+    if (r != CRG_OK) {
+      delete c;
+      return r;
+    }
+    c->sims_h[s].voxel_off = (uint32_t)vox;
+    vox += c->sims_h[s].n_vox;
+    cap += capacities[s];
+    if (vox > 0x7fffffffull || cap > 0x7fffffffll) {
+      delete c;
+      return CRG_ENOTSUP;
+    }
+  }
+  c->n_vox = (uint32_t)vox;
+  c->cap = std::max<int64_t>(cap, 1);
+  c->agent_off_h.assign(n_sims + 1, 0);
+  int32_t r = allocate(c);
+  if (r != CRG_OK) {
+    free_all(c);
+    delete c;
+    return r;
+  }
+  *out = c;
+  return CRG_OK;
+}
+
+PackArgs pack_args(crg_ctx *c) {
+  PackArgs P;
+  std::memset(&P, 0, sizeof(P));
+  P.sims = c->d_sims;
+  P.sim_agent_off = c->d_agent_off;
+  P.n_sims = c->n_sims;
+  P.cap = c->cap;
+  P.n_agents = c->n_agents;
+  P.n_vox = c->n_vox;
+  P.pos = c->pos;
+  P.vel = c->vel;
+  P.id = c->id;
+  P.key = c->key;
+  P.off = c->off;
+  P.hist = c->hist;
+  P.hmeta = c->hmeta;
+  P.start = c->start;
+  P.npos = c->npos;
+  P.nvel = c->nvel;
+  P.nid = c->nid;
+  P.nkey = c->nkey;
+  P.nhist = c->nhist;
+  P.nhmeta = c->nhmeta;
+  P.count = c->count;
+  P.status = c->status;
+  P.step_ctr = c->step_ctr;
+  P.dbg_force = c->dbg_force;
+  P.prefilter = c->prefilter;
+  return P;
+}
+
+SortArgs sort_args(crg_ctx *c, int initial) {
+  SortArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.sims = c->d_sims;
+  A.sim_agent_off = c->d_agent_off;
+  A.sim_of_voxel = c->d_sim_of_voxel;
+  A.n_sims = c->n_sims;
+  A.nc = c->nc;
+  A.initial = initial;
+  A.cap = c->cap;
+  A.n_agents = c->n_agents;
+  A.n_vox = c->n_vox;
+  A.pos = c->pos;
+  A.vel = c->vel;
+  A.id = c->id;
+  A.key = c->key;
+  A.off = c->off;
+  A.hist = c->hist;
+  A.hmeta = c->hmeta;
+  A.npos = c->npos;
+  A.nvel = c->nvel;
+  A.nid = c->nid;
+  A.nkey = c->nkey;
+  A.nhist = c->nhist;
+  A.nhmeta = c->nhmeta;
+  A.count = c->count;
+  A.start = c->start;
+  A.tmp = c->tmp;
+  A.status = c->status;
+  A.step_ctr = initial ? nullptr : c->step_ctr;
+  return A;
+}
+
+void launch_force(crg_ctx *c) {
+  PackArgs P = pack_args(c);
+  if (c->kind == CRG_KIND_SPHERE)
+    crg::launch_spheres_step(c->dim, c->precision, P, c->block, c->stream);
+  else
+    crg::launch_rods_step(c->dim, c->nv, c->precision, P, c->block, c->stream);
+}
+
+void launch_one_step(crg_ctx *c) {
+  launch_force(c);
+  crg::launch_sort(sort_args(c, 0), c->bsum, c->stream);
+}
+
+int32_t read_status(crg_ctx *c) {
+  CUDA_TRY(cudaMemcpyAsync(c->h_status, c->status, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if (c->h_status[0] != CRG_OK) {
+    c->err_code = c->h_status[0];
+    c->err_agent = (int64_t)(((uint64_t)(uint32_t)c->h_status[2] << 32) | (uint32_t)c->h_status[1]);
+    c->err_step = c->h_status[3];
+    return c->err_code;
+  }
+  return CRG_OK;
+}
+
+int32_t ensure_graph(crg_ctx *c, int steps) {
+  if (c->gexec && c->gexec_steps == steps) return CRG_OK;
+  if (c->gexec) {
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+  }
+  cudaGraph_t g;
+  CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < steps; ++k) launch_one_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess) return CRG_ECUDA;
+  e = cudaGraphInstantiate(&c->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    c->gexec = nullptr;
+    return CRG_ECUDA;
+  }
+  c->gexec_steps = steps;
+  return CRG_OK;
+}
+
+void invalidate_graph(crg_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->gexec_steps = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *crg_strerror(int32_t code) {
+  switch (code) {
+    case CRG_OK: return "ok";
+    case CRG_ECALC: return "calculation error (CalcError)";
+    case CRG_EBOUNDARY: return "agent outside the domain (BoundaryError)";
+    case CRG_EINDEX: return "agent outside every voxel (IndexError)";
+    case CRG_EDECOMPOSE: return "cannot decompose the domain (DecomposeError)";
+    case CRG_EINVAL: return "invalid argument";
+    case CRG_ENOMEM: return "out of device memory";
+    case CRG_ECUDA: return "CUDA runtime error";
+    case CRG_ETIMEDOUT: return "device wait timed out";
+    case CRG_ENOTSUP: return "not supported";
+    default: return "unknown status";
+  }
+}
+
+int32_t crg_create(const crg_domain *domain, const crg_model *model, int64_t capacity,
+                   crg_ctx **out) {
+  if (!domain || !model) return CRG_EINVAL;
+  return create_impl(1, domain, model, &capacity, out);
+}
+
+int32_t crg_create_batch(int32_t n_sims, const crg_domain *domains, const crg_model *models,
+                         const int64_t *capacities, crg_ctx **out) {
+  return create_impl(n_sims, domains, models, capacities, out);
+}
+
+int32_t crg_destroy(crg_ctx *c) {
+  if (!c) return CRG_EINVAL;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_all(c);
+  delete c;
+  return CRG_OK;
+}
+
+int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *pos,
+                   const double *vel, const uint64_t *ids) {
+  if (!c || n < 0 || (n > 0 && (!pos || !vel))) return CRG_EINVAL;
+  std::vector<int64_t> cnt(c->n_sims);
+  if (c->n_sims == 1) {
+    cnt[0] = counts ? counts[0] : n;
+  } else {
+    if (!counts) return CRG_EINVAL;
+    cnt.assign(counts, counts + c->n_sims);
+  }
+  int64_t tot = 0;
+  for (int s = 0; s < c->n_sims; ++s) {
+    if (cnt[s] < 0 || cnt[s] > c->caps[s]) return CRG_EINVAL;
+    tot += cnt[s];
+  }
+  if (tot != n) return CRG_EINVAL;
+  c->n_agents = (uint32_t)n;
+  c->agent_off_h.assign(c->n_sims + 1, 0);
+  for (int s = 0; s < c->n_sims; ++s) {
+    c->agent_off_h[s + 1] = c->agent_off_h[s] + (uint32_t)cnt[s];
+    c->sims_h[s].agent_off = c->agent_off_h[s];
+    c->sims_h[s].n_agents = (uint32_t)cnt[s];
+  }
+  invalidate_graph(c);
+  c->err_code = CRG_OK;
+  c->err_agent = c->err_step = -1;
+  c->steps_done = 0;
+  cudaStream_t st = c->stream;
+  CUDA_TRY(cudaMemcpyAsync(c->d_sims, c->sims_h.data(), sizeof(SimDev) * c->n_sims,
+                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c->d_agent_off, c->agent_off_h.data(),
+                           sizeof(uint32_t) * (c->n_sims + 1), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 4, st));
+  CUDA_TRY(cudaMemsetAsync(c->step_ctr, 0, sizeof(int64_t), st));
+  CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), st));
+  const size_t bytes = sizeof(double) * (size_t)n * c->nc;
+  if (n > 0) {
+    CUDA_TRY(cudaMemcpyAsync(c->staging, pos, bytes, cudaMemcpyHostToDevice, st));
+    crg::launch_transpose_in(c->staging, c->npos, (uint32_t)n, c->nc, c->cap, st);
+    CUDA_TRY(cudaMemcpyAsync(c->staging, vel, bytes, cudaMemcpyHostToDevice, st));
+    crg::launch_transpose_in(c->staging, c->nvel, (uint32_t)n, c->nc, c->cap, st);
+    if (ids) {
+      CUDA_TRY(cudaMemcpyAsync(c->nid, ids, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
+    } else {
+      std::vector<uint64_t> iota(n);
+      int64_t k = 0;
+      for (int s = 0; s < c->n_sims; ++s)
+        for (int64_t j = 0; j < cnt[s]; ++j) iota[k++] = (uint64_t)j;
+      CUDA_TRY(cudaMemcpyAsync(c->nid, iota.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+    }
+  }
+  if (c->order > 1) {
+    CUDA_TRY(cudaMemsetAsync(c->nhmeta, 0, (size_t)c->cap, st));
+    CUDA_TRY(cudaMemsetAsync(c->nhist, 0, sizeof(double) * (size_t)c->cap * c->nc * 2, st));
+  }
+  SortArgs A = sort_args(c, 1);
+  crg::launch_init_keys(A, c->nv, st);
+  crg::launch_sort(A, c->bsum, st);
+  CUDA_TRY(cudaGetLastError());
+  int32_t r = read_status(c);
+  if (r != CRG_OK) {
+    c->err_step = 0;
+    return r;
+  }
+  return CRG_OK;
+}
+
+int32_t crg_step(crg_ctx *c, int64_t n_steps) {
+  if (!c || n_steps < 0) return CRG_EINVAL;
+  if (c->err_code != CRG_OK) return c->err_code;
+  if (n_steps == 0 || c->n_agents == 0) {
+    c->steps_done += n_steps;
+    return CRG_OK;
+  }
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  if (c->profile) {
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    c->prof_ms[0] = c->prof_ms[1] = 0.0;
+    c->prof_ms[2] = 0.0;
+  }
+  int64_t left = n_steps;
+  const int chunk = c->graph_chunk;
+  while (left > 0) {
+    if (c->profile) {
+      const int k = (int)std::min<int64_t>(left, 64);
+      for (int s = 0; s < k; ++s) {
+        cudaEventRecord(ev[0], c->stream);
+        launch_force(c);
+        cudaEventRecord(ev[1], c->stream);
+        crg::launch_sort(sort_args(c, 0), c->bsum, c->stream);
+        cudaEventRecord(ev[2], c->stream);
+        cudaEventSynchronize(ev[2]);
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        c->prof_ms[0] += a;
+        c->prof_ms[1] += b;
+        c->prof_ms[2] += 1 + crg::sort_kernel_count();
+      }
+      left -= k;
+    } else if (chunk > 0 && left >= chunk) {
+      int32_t r = ensure_graph(c, chunk);
+      if (r != CRG_OK) return r;
+      const int64_t reps = std::min<int64_t>(left / chunk, std::max(1, 256 / chunk));
+      for (int64_t k = 0; k < reps; ++k) CUDA_TRY(cudaGraphLaunch(c->gexec, c->stream));
+      left -= reps * chunk;
+    } else {
+      const int k = (int)std::min<int64_t>(left, 256);
+      for (int s = 0; s < k; ++s) launch_one_step(c);
+      left -= k;
+    }
+    CUDA_TRY(cudaGetLastError());
+    int32_t r = read_status(c);
+    if (r != CRG_OK) break;
+  }
+  if (c->profile)
+    for (auto &e : ev) cudaEventDestroy(e);
+  c->steps_done += n_steps - std::max<int64_t>(left, 0);
+  return c->err_code;
+}
+
+int32_t crg_download(crg_ctx *c, double *pos, double *vel, uint64_t *ids, uint32_t *voxel) {
+  if (!c) return CRG_EINVAL;
+  const uint32_t n = c->n_agents;
+  if (n == 0) return CRG_OK;
+  cudaStream_t st = c->stream;
+  const size_t bytes = sizeof(double) * (size_t)n * c->nc;
+  if (pos) {
+    crg::launch_transpose_out(c->pos, c->staging, n, c->nc, c->cap, st);
+    CUDA_TRY(cudaMemcpyAsync(pos, c->staging, bytes, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (vel) {
+    crg::launch_transpose_out(c->vel, c->staging, n, c->nc, c->cap, st);
+    CUDA_TRY(cudaMemcpyAsync(vel, c->staging, bytes, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (ids) CUDA_TRY(cudaMemcpyAsync(ids, c->id, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, st));
+  if (voxel) {
+    CUDA_TRY(cudaMemcpyAsync(voxel, c->key, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (int s = 0; s < c->n_sims; ++s)
+      for (uint32_t i = c->agent_off_h[s]; i < c->agent_off_h[s + 1]; ++i)
+        voxel[i] -= c->sims_h[s].voxel_off;
+  }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CRG_OK;
+}
+
+int32_t crg_snapshot(crg_ctx *c, int32_t op) {
+  if (!c || (op != CRG_SNAPSHOT_SAVE && op != CRG_SNAPSHOT_RESTORE)) return CRG_EINVAL;
+  const size_t cap = (size_t)c->cap, nc = (size_t)c->nc;
+  struct Part {
+    void *p;
+    size_t bytes;
+  };
+  std::vector<Part> parts = {
+      {c->pos, sizeof(double) * cap * nc}, {c->vel, sizeof(double) * cap * nc},
+      {c->id, sizeof(uint64_t) * cap},     {c->key, sizeof(uint32_t) * cap},
+      {c->off, sizeof(float) * cap * nc},  {c->start, sizeof(uint32_t) * ((size_t)c->n_vox + 1)},
+      {c->step_ctr, sizeof(int64_t)}};
+  if (c->order > 1) {
+    parts.push_back({c->hist, sizeof(double) * cap * nc * 2});
+    parts.push_back({c->hmeta, cap});
+  }
+  size_t total = 0;
+  for (auto &p : parts) total += (p.bytes + 255) & ~size_t(255);
+  if (op == CRG_SNAPSHOT_SAVE && !c->snap) {
+    int32_t r = dalloc(&c->snap, total);
+    if (r != CRG_OK) return r;
+  }
+  if (!c->snap) return CRG_EINVAL;
+  size_t off = 0;
+  for (auto &p : parts) {
+    char *s = c->snap + off;
+    if (op == CRG_SNAPSHOT_SAVE)
+      CUDA_TRY(cudaMemcpyAsync(s, p.p, p.bytes, cudaMemcpyDeviceToDevice, c->stream));
+    else
+      CUDA_TRY(cudaMemcpyAsync(p.p, s, p.bytes, cudaMemcpyDeviceToDevice, c->stream));
+    off += (p.bytes + 255) & ~size_t(255);
+  }
+  if (op == CRG_SNAPSHOT_SAVE) {
+    c->snap_agents = c->n_agents;
+    c->snap_steps = c->steps_done;
+  } else {
+    if (c->snap_agents != c->n_agents) return CRG_EINVAL;
+    c->steps_done = c->snap_steps;
+    c->err_code = CRG_OK;
+    c->err_agent = c->err_step = -1;
+    CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 4, c->stream));
+  }
+  return CRG_OK;
+}
+
+int32_t crg_get_stream(crg_ctx *c, void **stream) {
+  if (!c || !stream) return CRG_EINVAL;
+  *stream = (void *)c->stream;
+  return CRG_OK;
+}
+
+int32_t crg_agent_count(crg_ctx *c, int64_t *n) {
+  if (!c || !n) return CRG_EINVAL;
+  *n = c->n_agents;
+  return CRG_OK;
+}
+
+int32_t crg_last_error(crg_ctx *c, int64_t *agent, int64_t *step) {
+  if (!c) return CRG_EINVAL;
+  if (agent) *agent = c->err_agent;
+  if (step) *step = c->err_step;
+  return c->err_code;
+}
+
+int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
+  if (!c) return CRG_EINVAL;
+  switch (option) {
+    case CRG_OPT_PREFILTER: c->prefilter = value ? 1 : 0; break;
+    case CRG_OPT_GRAPH_CHUNK:
+      if (value < 0 || value > 4096) return CRG_EINVAL;
+      c->graph_chunk = (int)value;
+      break;
+    case CRG_OPT_BLOCK:
+      if (value < 0 || value > 1024) return CRG_EINVAL;
+      c->block = (int)value;
+      break;
+    case CRG_OPT_PROFILE: c->profile = value ? 1 : 0; break;
+    case CRG_OPT_DEBUG_FORCES:
+      if (value && !c->dbg_force) {
+        int32_t r = dalloc(&c->dbg_force, (size_t)c->cap * c->nc);
+        if (r != CRG_OK) return r;
+        CUDA_TRY(cudaMemset(c->dbg_force, 0, sizeof(double) * (size_t)c->cap * c->nc));
+      } else if (!value && c->dbg_force) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->dbg_force);
+        c->dbg_force = nullptr;
+      }
+      break;
+    default: return CRG_EINVAL;
+  }
+  invalidate_graph(c);
+  return CRG_OK;
+}
+
+int32_t crg_profile(crg_ctx *c, double *out3) {
+  if (!c || !out3) return CRG_EINVAL;
+  for (int k = 0; k < 3; ++k) out3[k] = c->prof_ms[k];
+  return CRG_OK;
+}
+
+int32_t crg_debug_forces(crg_ctx *c, double *force, uint64_t *ids) {
+  if (!c || !c->dbg_force) return CRG_EINVAL;
+  const uint32_t n = c->n_agents;
+  cudaStream_t st = c->stream;
+  if (force) {
+    crg::launch_transpose_out(c->dbg_force, c->staging, n, c->nc, c->cap, st);
+    CUDA_TRY(cudaMemcpyAsync(force, c->staging, sizeof(double) * (size_t)n * c->nc,
+                             cudaMemcpyDeviceToHost, st));
+  }
+  if (ids) CUDA_TRY(cudaMemcpyAsync(ids, c->nid, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CRG_OK;
+}
+
+int32_t crg_debug_neighbor_stats(crg_ctx *c, uint32_t *n_cand, uint32_t *n_inter,
+                                 uint64_t *cand_hash, uint64_t *ids) {
+  if (!c) return CRG_EINVAL;
+  const uint32_t n = c->n_agents;
+  if (n == 0) return CRG_OK;
+  uint32_t *d_nc = nullptr, *d_ni = nullptr;
+  uint64_t *d_h = nullptr;
+  int32_t r;
+  if ((r = dalloc(&d_nc, n)) || (r = dalloc(&d_ni, n)) || (r = dalloc(&d_h, n))) {
+    cudaFree(d_nc);
+    cudaFree(d_ni);
+    cudaFree(d_h);
+    return r;
+  }
+  crg::launch_neighbor_stats(c->dim, c->kind == CRG_KIND_ROD ? c->nv : 1, pack_args(c), d_nc,
+                             d_ni, d_h, c->stream);
+  cudaStream_t st = c->stream;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && n_cand) e = cudaMemcpyAsync(n_cand, d_nc, 4ull * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && n_inter) e = cudaMemcpyAsync(n_inter, d_ni, 4ull * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && cand_hash) e = cudaMemcpyAsync(cand_hash, d_h, 8ull * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && ids) e = cudaMemcpyAsync(ids, c->id, 8ull * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_nc);
+  cudaFree(d_ni);
+  cudaFree(d_h);
+  return e == cudaSuccess ? CRG_OK : CRG_ECUDA;
+}
+
+int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
+  if (!fp64_tflops || !fp32_tflops) return CRG_EINVAL;
+  return crg::measure_fma_peaks(fp64_tflops, fp32_tflops);
+}
+
+}  // extern "C"
+
+namespace crg {
+void launch_sphere_stats(int dim, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,
+                         uint64_t *hash, cudaStream_t st);
+void launch_rod_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,
+                      uint64_t *hash, cudaStream_t st);
+
+void launch_neighbor_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand,
+                           uint32_t *n_inter, uint64_t *hash, cudaStream_t st) {
+  if (nv == 1)
+    launch_sphere_stats(dim, P, n_cand, n_inter, hash, st);
+  else
+    launch_rod_stats(dim, nv, P, n_cand, n_inter, hash, st);
+}
+}  // namespace crg

@@ -1,0 +1,173 @@
+// crg_internal.cuh -- device-side descriptors and helpers shared by the crg kernels.
+//
+// Layout in HBM (one "pack" = one or more independent simulations of the same agent kind,
+// dimension and precision, concatenated):
+//   * agents are kept physically sorted by global voxel index (the cell list); every
+//     per-agent array is component-major SoA: x[c * cap + i] for component c of agent i,
+//     where a component is (vertex, axis) for rods and the axis for spheres;
+//   * voxels of simulation s occupy the global index range [voxel_off, voxel_off + n_vox);
+//     the agents of s occupy [agent_off, agent_off + n_agents) because the sort is global;
+//   * start[v] .. start[v+1] is the agent range of global voxel v after each re-sort.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/crg.h"
+
+namespace crg {
+
+constexpr int kMaxVertices = 8;
+
+// Per-simulation descriptor (device copy).  Geometry follows CartesianCuboid
+// (cellular_raza-building-blocks/src/domains/cartesian_cuboid_n.rs:65-72).
+struct SimDev {
+  int32_t dim;
+  int32_t nvox[3];
+  double min[3], max[3], dx[3];
+  float dxf[3];
+  uint32_t voxel_off, n_vox;
+  uint32_t agent_off, n_agents;
+  // Subdomain chunking of get_decomp_res/create_subdomains (cartesian_cuboid_n.rs:19-59,
+  // 493-584): voxel i belongs to i/avg if i < switcher, else (i-switcher)/div2 + n.
+  uint32_t sd_switch, sd_avg, sd_div2, sd_n;
+  int32_t weight_mode;  // CRG_WEIGHTS_CHILI or CRG_WEIGHTS_PHYSICAL
+  // Mechanics / interaction parameters.
+  double mass, damping;
+  double spring_tension, rigidity, spring_length;
+  double radius, stiffness, cutoff, strength;
+  double dt;
+  float radius_f, stiffness_f, cutoff_f, strength_f;
+  float filt_thr2;  // squared FP32 prefilter threshold (cutoff + conservative margin)^2
+  float off_lim;    // |FP32 offset| bound the prefilter margin was derived for
+  int32_t order;    // 1 Euler, 2 AB2, 3 AB3
+};
+
+// Arguments shared by the per-step kernels of a pack.
+struct PackArgs {
+  const SimDev *sims;
+  const uint32_t *sim_agent_off;  // [n_sims + 1] prefix of agent counts
+  int32_t n_sims;
+  int64_t cap;      // component stride
+  uint32_t n_agents;
+  uint32_t n_vox;   // total voxels of the pack
+  // current (sorted) state
+  const double *pos;
+  const double *vel;
+  const uint64_t *id;
+  const uint32_t *key;
+  const float *off;  // FP32 offsets from the voxel corner (prefilter / mixed precision)
+  const double *hist;     // AB history [2 slots][2 (dx,dv)][nc][cap] or null
+  const uint8_t *hmeta;   // ring buffer (first | size << 4) or null
+  const uint32_t *start;  // [n_vox + 1]
+  // next (updated, unsorted) state
+  double *npos;
+  double *nvel;
+  uint64_t *nid;    // ids in the pre-step order (copied by the force kernel)
+  uint32_t *nkey;
+  double *nhist;
+  uint8_t *nhmeta;
+  uint32_t *count;  // histogram of nkey (atomic)
+  // status word: [0] code, [1] agent id lo, [2] agent id hi, [3] step
+  int32_t *status;
+  const int64_t *step_ctr;
+  double *dbg_force;  // optional [nc][cap]: interaction force of this step
+  int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
+};
+
+// ---- IEEE FP64 helpers that are never contracted into fused multiply-adds ----------
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// num::ToPrimitive::to_usize for f64: truncation toward zero on the open interval
+// (-1, 2^64); everything else (NaN included) has no value.
+__device__ __forceinline__ bool to_usize(double x, uint64_t &out) {
+  if (x > -1.0 && x < 18446744073709551616.0) {
+    out = (x < 1.0) ? 0ull : (uint64_t)x;
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ uint32_t subdomain_of(const SimDev &S, uint32_t v) {
+  return v < S.sd_switch ? v / S.sd_avg : (v - S.sd_switch) / S.sd_div2 + S.sd_n;
+}
+
+// CartesianSubDomain::get_index_of (cartesian_cuboid_n.rs:469-490) + plain-index lookup.
+// Returns 0 ok, 1 conversion failure, 2 index outside the voxel grid.
+template <int D>
+__device__ __forceinline__ int voxel_of(const SimDev &S, const double *p, uint32_t &plain) {
+  uint64_t idx[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    double n_vox = ddiv(dsub(p[i], S.min[i]), S.dx[i]);
+    if (!to_usize(n_vox, idx[i])) return 1;
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+    if (idx[i] >= (uint64_t)S.nvox[i]) return 2;
+  uint64_t q = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) q = q * (uint64_t)S.nvox[i] + idx[i];
+  plain = (uint32_t)q;
+  return 0;
+}
+
+template <int D>
+__device__ __forceinline__ void unravel(const SimDev &S, uint32_t v, int *idx) {
+#pragma unroll
+  for (int i = D - 1; i >= 0; --i) {
+    idx[i] = (int)(v % (uint32_t)S.nvox[i]);
+    v /= (uint32_t)S.nvox[i];
+  }
+}
+
+// Corner of voxel idx in FP64: min + idx * dx (used only for the FP32 offsets).
+__device__ __forceinline__ double voxel_corner(const SimDev &S, int axis, int idx) {
+  return S.min[axis] + (double)idx * S.dx[axis];
+}
+
+__device__ __forceinline__ uint32_t sim_of_agent(const PackArgs &P, uint32_t i) {
+  int lo = 0, hi = P.n_sims;  // invariant: off[lo] <= i < off[hi]
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(&P.sim_agent_off[mid]) <= i)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return (uint32_t)lo;
+}
+
+__device__ __forceinline__ void set_status(int32_t *status, int32_t code, uint64_t agent,
+                                           int64_t step) {
+  if (atomicCAS(&status[0], 0, code) == 0) {
+    status[1] = (int32_t)(agent & 0xffffffffu);
+    status[2] = (int32_t)(agent >> 32);
+    status[3] = (int32_t)step;
+  }
+}
+
+// calculate_morse_interaction (cellular_raza-building-blocks/src/cell_building_blocks/
+// interaction.rs:151-182) in FP64, returning the own-perspective force already scaled by
+// one half (chili adds f.xa(1/2), update_mechanics.rs:98,194-199).  Each operation is
+// separately rounded in the reference's order.  Returns false for a zero force
+// (dist > cutoff or dist == 0).
+template <int D>
+__device__ __forceinline__ bool morse_half_f64(const double *z, const SimDev &S,
+                                               double ext_radius, double *h) {
+  double n2 = dmul(z[0], z[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
+  double dist = __dsqrt_rn(n2);
+  if (dist > S.cutoff || dist == 0.0) return false;
+  double r = dadd(S.radius, ext_radius);
+  double e = exp(dmul(-S.stiffness, dsub(dist, r)));
+  double force = dmul(dmul(dmul(dmul(-2.0, S.strength), S.stiffness), e), dsub(1.0, e));
+#pragma unroll
+  for (int c = 0; c < D; ++c) h[c] = dmul(dmul(ddiv(z[c], dist), force), 0.5);
+  return true;
+}
+
+}  // namespace crg

@@ -1,0 +1,61 @@
+// crg_kernels.h -- host-side launch wrappers shared between the crg translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace crg {
+
+struct SimDev;
+struct PackArgs;
+
+// Arguments of the cell-list kernels (crg_sort.cu).
+struct SortArgs {
+  const SimDev *sims;
+  const uint32_t *sim_agent_off;  // [n_sims + 1]
+  const uint32_t *sim_of_voxel;   // [n_vox] (batch handles only)
+  int32_t n_sims;
+  int32_t nc;      // components per agent (n_vertices * dim)
+  int32_t initial; // 1 for the insertion sort after crg_upload (every agent class 0)
+  int64_t cap;
+  uint32_t n_agents;
+  uint32_t n_vox;
+  // sorted state (written by the gather)
+  double *pos, *vel;
+  uint64_t *id;
+  uint32_t *key;
+  float *off;
+  double *hist;
+  uint8_t *hmeta;
+  // updated state in the previous order (read by the gather)
+  const double *npos, *nvel;
+  const uint64_t *nid;
+  uint32_t *nkey;
+  const double *nhist;
+  const uint8_t *nhmeta;
+  // scratch
+  uint32_t *count;  // [n_vox]
+  uint32_t *start;  // [n_vox + 1]
+  uint64_t *tmp;    // [cap]
+  int32_t *status;
+  int64_t *step_ctr;
+};
+
+void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st);
+int sort_kernel_count();
+void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st);
+void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
+                         cudaStream_t st);
+void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
+                          cudaStream_t st);
+
+// Force + integrator + boundary + next voxel key (+ histogram) for one step.
+void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st);
+void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
+                      cudaStream_t st);
+// Diagnostics over the current cell list.
+void launch_neighbor_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand,
+                           uint32_t *n_inter, uint64_t *hash, cudaStream_t st);
+
+int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
+
+}  // namespace crg

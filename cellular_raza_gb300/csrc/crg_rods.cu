@@ -1,0 +1,523 @@
+// crg_rods.cu -- one chili step for RodMechanics + RodInteraction<MorsePotential> rods.
+//
+// One thread per rod in cell-list order.  For every candidate rod b in the 3^D
+// neighbourhood of rod a's voxel (keyed by centroid, bacterial_rods.rs:550-554) it builds
+// the two matrices RodInteraction::calculate_force_between produces
+// (bacterial_rods.rs:292-336):
+//   own_a(b): a's vertices against b's segments, force on a's vertices (a.calc(a, b).0)
+//   ext_a(b): b's vertices against a's segments, force distributed on a's vertices
+//             with weights (1 - t, t)                                   (b.calc(b, a).1)
+// and adds them scaled by one half in chili's order:
+//   same voxel, b before a in the voxel: ext then own   (update_mechanics.rs:193-199,
+//   same voxel, b after a:                own then ext    a is the first or second cell)
+//   neighbour voxel, same subdomain:      own only        (:205-220; the ext half is dropped)
+//   neighbour voxel, other subdomain:     own then ext    (steps 2 and 3, :285-382)
+// Vertex/segment evaluations whose FP32 distance exceeds the cutoff plus margin are zero
+// in FP64 as well and are skipped; the rest are evaluated in FP64 in the reference's
+// operation order.  RodMechanics::calculate_increment (bacterial_rods.rs:157-213), the
+// solver, apply_boundary (:489-534) and the centroid voxel key follow.
+#include "crg_internal.cuh"
+#include "crg_kernels.h"
+
+namespace crg {
+
+namespace {
+
+// nearest_point_from_point_to_line (interaction.rs:497-509): returns q and t.
+template <int D>
+__device__ __forceinline__ void nearest_point_f64(const double *p, const double *l0,
+                                                  const double *l1, double *q, double &t) {
+  double ab[D], ap[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    ab[c] = dsub(l1[c], l0[c]);
+    ap[c] = dsub(p[c], l0[c]);
+  }
+  double dot = dmul(ab[0], ap[0]);
+  double nsq = dmul(ab[0], ab[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) {
+    dot = dadd(dot, dmul(ab[c], ap[c]));
+    nsq = dadd(nsq, dmul(ab[c], ab[c]));
+  }
+  t = ddiv(dot, nsq);
+  if (t < 0.0) t = 0.0;
+  if (t > 1.0) t = 1.0;
+  const double omt = dsub(1.0, t);
+#pragma unroll
+  for (int c = 0; c < D; ++c) q[c] = dadd(dmul(l0[c], omt), dmul(l1[c], t));
+}
+
+// Full (unhalved) Morse force on `own` from the point `ext` (interaction.rs:151-182).
+template <int D>
+__device__ __forceinline__ bool morse_full_f64(const double *own, const double *ext,
+                                               const SimDev &S, double *f) {
+  double z[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) z[c] = dsub(own[c], ext[c]);
+  double n2 = dmul(z[0], z[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
+  const double dist = __dsqrt_rn(n2);
+  if (dist > S.cutoff || dist == 0.0) return false;
+  const double r = dadd(S.radius, S.radius);
+  const double e = exp(dmul(-S.stiffness, dsub(dist, r)));
+  const double force = dmul(dmul(dmul(dmul(-2.0, S.strength), S.stiffness), e), dsub(1.0, e));
+#pragma unroll
+  for (int c = 0; c < D; ++c) f[c] = dmul(ddiv(z[c], dist), force);
+  return true;
+}
+
+// Squared FP32 distance from p to the segment (l0, l1) (prefilter only).
+template <int D>
+__device__ __forceinline__ float seg_dist2_f32(const float *p, const float *l0,
+                                               const float *l1) {
+  float ab[D], ap[D];
+  float dot = 0.f, nsq = 0.f;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    ab[c] = l1[c] - l0[c];
+    ap[c] = p[c] - l0[c];
+    dot = fmaf(ab[c], ap[c], dot);
+    nsq = fmaf(ab[c], ab[c], nsq);
+  }
+  float t = (nsq > 0.f) ? __fdividef(dot, nsq) : 0.f;
+  t = fminf(fmaxf(t, 0.f), 1.f);
+  float d2 = 0.f;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const float w = fmaf(-t, ab[c], ap[c]);
+    d2 = fmaf(w, w, d2);
+  }
+  return d2;
+}
+
+// One half of the pair interaction.  is_ext = false: own_a(b) (a's vertices X against
+// b's segments Y, force on X's rows).  is_ext = true: ext_a(b) (b's vertices against a's
+// segments, -f distributed on a's rows j, j+1 with weights 1-t, t).  Per-thread operands
+// live in shared memory ([component][thread]) so the loops can run over vertices without
+// spilling; the accumulated matrix is left in sT.  Returns whether any term was non-zero.
+template <int D, int NV, int B>
+__device__ __forceinline__ bool rod_pass(bool is_ext, const double *posb, int64_t cap,
+                                         const SimDev &S, float thr2, const double (*sPa)[B],
+                                         double (*sT)[B], const float (*sOa)[B],
+                                         const float (*sOb)[B], int tid) {
+  constexpr int NC = NV * D;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) sT[k][tid] = 0.0;
+  bool any = false;
+#pragma unroll 1
+  for (int vx = 0; vx < NV; ++vx) {
+#pragma unroll 1
+    for (int sy = 0; sy + 1 < NV; ++sy) {
+      float p32[D], l0f[D], l1f[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        p32[c] = is_ext ? sOb[vx * D + c][tid] : sOa[vx * D + c][tid];
+        l0f[c] = is_ext ? sOa[sy * D + c][tid] : sOb[sy * D + c][tid];
+        l1f[c] = is_ext ? sOa[(sy + 1) * D + c][tid] : sOb[(sy + 1) * D + c][tid];
+      }
+      if (seg_dist2_f32<D>(p32, l0f, l1f) > thr2) continue;
+      double p[D], l0[D], l1[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        if (is_ext) {
+          p[c] = posb[(vx * D + c) * cap];
+          l0[c] = sPa[sy * D + c][tid];
+          l1[c] = sPa[(sy + 1) * D + c][tid];
+        } else {
+          p[c] = sPa[vx * D + c][tid];
+          l0[c] = posb[(sy * D + c) * cap];
+          l1[c] = posb[((sy + 1) * D + c) * cap];
+        }
+      }
+      double q[D], t, f[D];
+      nearest_point_f64<D>(p, l0, l1, q, t);
+      if (!morse_full_f64<D>(p, q, S, f)) continue;
+      any = true;
+      if (!is_ext) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) sT[vx * D + c][tid] = dadd(sT[vx * D + c][tid], f[c]);
+      } else {
+        const double omt = dsub(1.0, t);
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          const double fe = -f[c];
+          sT[sy * D + c][tid] = dadd(sT[sy * D + c][tid], dmul(fe, omt));
+          sT[(sy + 1) * D + c][tid] = dadd(sT[(sy + 1) * D + c][tid], dmul(fe, t));
+        }
+      }
+    }
+  }
+  return any;
+}
+
+template <int NC, int B>
+__device__ __forceinline__ void add_half(double *acc, const double (*sT)[B], int tid) {
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], dmul(sT[k][tid], 0.5));
+}
+
+template <int D>
+__device__ __forceinline__ double norm_f64(const double *v) {
+  double n2 = dmul(v[0], v[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(v[c], v[c]));
+  return __dsqrt_rn(n2);
+}
+
+template <int D, int NV, int B>
+__global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
+  constexpr int NC = NV * D;
+  __shared__ double sPa[NC][B];
+  __shared__ double sT[NC][B];
+  __shared__ float sOa[NC][B];
+  __shared__ float sOb[NC][B];
+  const int tid = threadIdx.x;
+  const uint32_t i = blockIdx.x * B + tid;
+  if (i >= P.n_agents) return;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  const int64_t cap = P.cap;
+  const uint32_t key = P.key[i];
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  double pa[NC];
+  float oa[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    pa[k] = P.pos[k * cap + i];
+    oa[k] = P.off[k * cap + i];
+    sPa[k][tid] = pa[k];
+    sOa[k][tid] = oa[k];
+  }
+  float amin[D], amax[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    amin[c] = oa[c];
+    amax[c] = oa[c];
+  }
+#pragma unroll
+  for (int k = D; k < NC; ++k) {
+    amin[k % D] = fminf(amin[k % D], oa[k]);
+    amax[k % D] = fmaxf(amax[k % D], oa[k]);
+  }
+  const bool a_nan = !(amin[0] == amin[0]) || !(amax[D - 1] == amax[D - 1]);
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+  double acc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool same = (w == v);
+        const bool twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
+                           subdomain_of(S, w) != sub_v;
+        // b's offsets in a's voxel frame: off_b + (corner_b - corner_a) = off_b + (j-idx) dx
+        float kd[D];
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        const uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        for (uint32_t b = b0; b < b1; ++b) {
+          if (b == i) continue;
+          float ob[NC];
+          float bmin[D], bmax[D];
+#pragma unroll
+          for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            bmin[c] = ob[c];
+            bmax[c] = ob[c];
+          }
+#pragma unroll
+          for (int k = D; k < NC; ++k) {
+            bmin[k % D] = fminf(bmin[k % D], ob[k]);
+            bmax[k % D] = fmaxf(bmax[k % D], ob[k]);
+          }
+          // Bounding boxes farther apart than the threshold on one axis: all 2 x NV x (NV-1)
+          // evaluations are beyond the cutoff.  (fminf/fmaxf drop NaNs, so a NaN anywhere
+          // disables the box test.)
+          bool far = false;
+          bool b_nan = false;
+#pragma unroll
+          for (int k = 0; k < NC; ++k) b_nan |= !(ob[k] == ob[k]);
+          if (!a_nan && !b_nan) {
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+              far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+          }
+          if (far) continue;
+#pragma unroll
+          for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
+          const double *posb = P.pos + b;
+          const bool ext_first = same && (b < i);
+#pragma unroll 1
+          for (int pass = 0; pass < 2; ++pass) {
+            const bool is_ext = (pass == 0) == ext_first;
+            if (is_ext && !twice) continue;
+            if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
+              add_half<NC, B>(acc, sT, tid);
+          }
+        }
+      }
+  if (P.dbg_force) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) P.dbg_force[k * cap + i] = acc[k];
+  }
+
+  // RodMechanics::calculate_increment (bacterial_rods.rs:157-213).
+  double va[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) va[k] = P.vel[k * cap + i];
+  double tf[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) tf[k] = acc[k];
+  double dist[NV - 1][D];
+#pragma unroll
+  for (int s = 0; s + 1 < NV; ++s)
+#pragma unroll
+    for (int c = 0; c < D; ++c) dist[s][c] = dsub(pa[s * D + c], pa[(s + 1) * D + c]);
+  // springs
+#pragma unroll
+  for (int s = 0; s + 1 < NV; ++s) {
+    const double nrm = norm_f64<D>(dist[s]);
+    if (nrm != 0.0) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const double dir = ddiv(dist[s][c], nrm);
+        const double fi = dmul(dmul(-dir, S.spring_tension), dsub(nrm, S.spring_length));
+        tf[s * D + c] = dadd(tf[s * D + c], dmul(fi, 0.5));
+        tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], dmul(-fi, 0.5));
+      }
+    }
+  }
+  // curvature: Matrix::angle = acos(clamp(dot / (|a| |b|), -1, 1)), 0 for zero length
+#pragma unroll
+  for (int s = 0; s + 2 < NV; ++s) {
+    const double *c1 = dist[s];
+    const double *c2 = dist[s + 1];
+    double prod = dmul(c1[0], c2[0]);
+#pragma unroll
+    for (int c = 1; c < D; ++c) prod = dadd(prod, dmul(c1[c], c2[c]));
+    const double n1 = norm_f64<D>(c1), n2 = norm_f64<D>(c2);
+    double angle = 0.0;
+    if (!(n1 == 0.0 || n2 == 0.0)) {
+      double cang = ddiv(prod, dmul(n1, n2));
+      if (cang < -1.0) cang = -1.0;
+      if (cang > 1.0) cang = 1.0;
+      angle = acos(cang);
+    }
+    double fd[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) fd[c] = dsub(c1[c], c2[c]);
+    const double fdn = norm_f64<D>(fd);
+    const double tn = tan(dmul(0.5, angle));
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const double fdir = (fdn != 0.0) ? ddiv(fd[c], fdn) : fd[c];
+      const double f = dmul(dmul(dmul(fdir, 2.0), S.rigidity), tn);
+      tf[s * D + c] = dadd(tf[s * D + c], dmul(-f, 0.5));
+      tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], f);
+      tf[(s + 2) * D + c] = dadd(tf[(s + 2) * D + c], dmul(-f, 0.5));
+    }
+  }
+  // damping
+#pragma unroll
+  for (int k = 0; k < NC; ++k) tf[k] = dsub(tf[k], dmul(va[k], S.damping));
+
+  // solver (dx = v, dv = total force)
+  double np[NC], nvl[NC];
+  const double dt = S.dt;
+  if (S.order == 1) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      np[k] = dadd(dadd(dmul(va[k], dt), pa[k]), 0.0);
+      nvl[k] = dadd(dadd(dmul(tf[k], dt), va[k]), 0.0);
+    }
+  } else {
+    const bool ab3 = (S.order == 3) && P.hmeta[i];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      if (ab3) {
+        const double f0 = 23.0 / 12.0, f1 = -16.0 / 12.0, f2 = 5.0 / 12.0;
+        const double px = P.hist[k * cap + i], pv = P.hist[(NC + k) * cap + i];
+        np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dadd(dmul(px, f1), dmul(va[k], f2))), dt),
+                          pa[k]), 0.0);
+        nvl[k] = dadd(dadd(dmul(dadd(dmul(tf[k], f0), dadd(dmul(pv, f1), dmul(tf[k], f2))), dt),
+                           va[k]), 0.0);
+      } else {
+        const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
+        np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dmul(va[k], f1)), dt), pa[k]), 0.0);
+        nvl[k] = dadd(dadd(dmul(dadd(dmul(tf[k], f0), dmul(tf[k], f1)), dt), va[k]), 0.0);
+      }
+      P.nhist[k * cap + i] = va[k];
+      P.nhist[(NC + k) * cap + i] = tf[k];
+    }
+    P.nhmeta[i] = 1;
+  }
+
+  // CartesianSubDomainRods::apply_boundary (bacterial_rods.rs:489-534).
+  bool inside = true;
+#pragma unroll
+  for (int s = 0; s < NV; ++s)
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      double &p = np[s * D + c];
+      double &u = nvl[s * D + c];
+      if (p < S.min[c]) {
+        p = dsub(dmul(S.min[c], 2.0), p);
+        u = fabs(u);
+      }
+      if (p > S.max[c]) {
+        p = dsub(dmul(S.max[c], 2.0), p);
+        u = -fabs(u);
+      }
+    }
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+    if (np[k] < S.min[k % D] || np[k] > S.max[k % D]) inside = false;
+  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1);
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    P.npos[k * cap + i] = np[k];
+    P.nvel[k * cap + i] = nvl[k];
+  }
+  // Next key from the centroid row_sum / nrows (bacterial_rods.rs:550-554).
+  double cen[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) s = dadd(s, np[q * D + c]);
+    cen[c] = ddiv(s, (double)NV);
+  }
+  uint32_t plain;
+  uint32_t nk = key;
+  if (voxel_of<D>(S, cen, plain) == 0) nk = S.voxel_off + plain;
+  P.nkey[i] = nk;
+  P.nid[i] = P.id[i];
+  atomicAdd(&P.count[nk], 1u);
+}
+
+// Candidate rods of the current cell list, a hash of their ids and the number of in-range
+// vertex/segment evaluations of a.calc(a, b) (own perspective, FP64, no prefilter).
+template <int D, int NV>
+__global__ void k_rod_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_inter,
+                            uint64_t *hash) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n_agents) return;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  const uint32_t v = P.key[i] - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  uint32_t nc = 0, ni = 0;
+  uint64_t h = 0;
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        for (uint32_t b = P.start[S.voxel_off + w]; b < P.start[S.voxel_off + w + 1]; ++b) {
+          if (b == i) continue;
+          ++nc;
+          uint64_t x = P.id[b] + 0x9e3779b97f4a7c15ull;
+          x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+          x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+          h += x ^ (x >> 31);
+          for (int vi = 0; vi < NV; ++vi)
+            for (int sj = 0; sj + 1 < NV; ++sj) {
+              double p[D], l0[D], l1[D], q[D], t, f[D];
+              for (int c = 0; c < D; ++c) {
+                p[c] = P.pos[(vi * D + c) * P.cap + i];
+                l0[c] = P.pos[(sj * D + c) * P.cap + b];
+                l1[c] = P.pos[((sj + 1) * D + c) * P.cap + b];
+              }
+              nearest_point_f64<D>(p, l0, l1, q, t);
+              if (morse_full_f64<D>(p, q, S, f)) ++ni;
+            }
+        }
+      }
+  n_cand[i] = nc;
+  n_inter[i] = ni;
+  hash[i] = h;
+}
+
+template <int D, int NV>
+void launch_t(const PackArgs &P, int block, cudaStream_t st) {
+  (void)block;
+  constexpr int B = 64;
+  const unsigned grid = (P.n_agents + B - 1) / B;
+  k_rods_step<D, NV, B><<<grid, B, 0, st>>>(P);
+}
+
+template <int D>
+void launch_d(int nv, const PackArgs &P, int block, cudaStream_t st) {
+  switch (nv) {
+    case 2: launch_t<D, 2>(P, block, st); break;
+    case 3: launch_t<D, 3>(P, block, st); break;
+    case 4: launch_t<D, 4>(P, block, st); break;
+    case 5: launch_t<D, 5>(P, block, st); break;
+    case 6: launch_t<D, 6>(P, block, st); break;
+    case 7: launch_t<D, 7>(P, block, st); break;
+    case 8: launch_t<D, 8>(P, block, st); break;
+    default: break;
+  }
+}
+
+}  // namespace
+
+void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
+                      cudaStream_t st) {
+  (void)precision;  // rods run the FP64 path
+  if (!P.n_agents) return;
+  if (block <= 0 || block > 128) block = 64;
+  if (dim == 3)
+    launch_d<3>(nv, P, block, st);
+  else
+    launch_d<2>(nv, P, block, st);
+}
+
+template <int D>
+void launch_stats_d(int nv, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,
+                    uint64_t *hash, cudaStream_t st) {
+  const unsigned grid = (P.n_agents + 127) / 128;
+  switch (nv) {
+    case 2: k_rod_stats<D, 2><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    case 3: k_rod_stats<D, 3><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    case 4: k_rod_stats<D, 4><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    case 5: k_rod_stats<D, 5><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    case 6: k_rod_stats<D, 6><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    case 7: k_rod_stats<D, 7><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    case 8: k_rod_stats<D, 8><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
+    default: break;
+  }
+}
+
+void launch_rod_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,
+                      uint64_t *hash, cudaStream_t st) {
+  if (!P.n_agents) return;
+  if (dim == 3)
+    launch_stats_d<3>(nv, P, n_cand, n_inter, hash, st);
+  else
+    launch_stats_d<2>(nv, P, n_cand, n_inter, hash, st);
+}
+
+}  // namespace crg

@@ -1,0 +1,282 @@
+// crg_sort.cu -- device cell list: voxel keys, counting sort and state gather.
+//
+// Replaces chili's per-voxel Vec storage and its re-sort
+// (cellular_raza-core/src/backend/chili/update_mechanics.rs:418-513) with one global
+// counting sort per step.  The order inside a voxel reproduces chili's exactly:
+//   class 0: agents that stayed (drain+partition keeps their order, :431-455),
+//   class 1: movers from a voxel of the same subdomain, pushed in source order (:459-466),
+//   class 2: movers from another subdomain, received and sorted by source voxel (:496-498),
+// and inside each class by the previous cell-list position, which is the previous
+// (voxel, position-in-voxel) order.  Slots are taken with atomics and then each voxel's
+// segment is sorted by (class, previous position), so the result is deterministic.
+#include "crg_internal.cuh"
+#include "crg_kernels.h"
+
+namespace crg {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive prefix and
+// writes the block total to *total.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total) {
+  __shared__ uint32_t warp_tot[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  uint32_t incl = warp_incl_scan(x);
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t t = (lane < nwarps) ? warp_tot[lane] : 0u;
+    uint32_t ti = warp_incl_scan(t);
+    if (lane < nwarps) warp_tot[lane] = ti - t;
+    if (lane == 31) warp_tot[31] = ti;  // total (nwarps <= 32)
+  }
+  __syncthreads();
+  uint32_t res = warp_tot[warp] + incl - x;
+  *total = warp_tot[31];
+  __syncthreads();
+  return res;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__restrict__ count,
+                                                              uint32_t n, uint32_t *bsum) {
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k)
+    if (base + k < n) s += count[base + k];
+  uint32_t tot;
+  block_excl_scan(s, &tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+// Single block: exclusive scan of the block sums in place; grand total -> start[n].
+__global__ void __launch_bounds__(kScanThreads) k_scan_blocks(uint32_t *bsum, uint32_t nb,
+                                                              uint32_t *start, uint32_t n) {
+  uint32_t carry = 0;
+  for (uint32_t b0 = 0; b0 < nb; b0 += kScanThreads) {
+    uint32_t j = b0 + threadIdx.x;
+    uint32_t x = (j < nb) ? bsum[j] : 0u;
+    uint32_t tot;
+    uint32_t ex = block_excl_scan(x, &tot);
+    if (j < nb) bsum[j] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) start[n] = carry;
+}
+
+// Final pass: start[j] = exclusive prefix; count[j] = 0 (reused as the scatter cursor).
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(uint32_t *__restrict__ count,
+                                                             uint32_t n,
+                                                             const uint32_t *__restrict__ bsum,
+                                                             uint32_t *__restrict__ start) {
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < n) ? count[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t tot;
+  uint32_t ex = block_excl_scan(s, &tot) + bsum[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) {
+      start[base + k] = ex;
+      count[base + k] = 0u;
+    }
+    ex += v[k];
+  }
+}
+
+// Slot assignment.  Sort key = class << 32 | previous position.
+__global__ void k_scatter(const SortArgs A) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n_agents) return;
+  const uint32_t k = A.nkey[i];
+  uint32_t cls = 0;
+  if (!A.initial) {
+    const uint32_t old = A.key[i];
+    if (k != old) {
+      const uint32_t s = (A.n_sims == 1) ? 0u : A.sim_of_voxel ? A.sim_of_voxel[k] : 0u;
+      const SimDev &S = A.sims[s];
+      cls = (subdomain_of(S, k - S.voxel_off) == subdomain_of(S, old - S.voxel_off)) ? 1u : 2u;
+    }
+  }
+  const uint32_t slot = A.start[k] + atomicAdd(&A.count[k], 1u);
+  A.tmp[slot] = ((uint64_t)cls << 32) | (uint64_t)i;
+}
+
+// One thread per voxel: order the voxel's segment and reset its histogram counter.
+__global__ void k_segsort(const SortArgs A) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= A.n_vox) return;
+  const uint32_t s0 = A.start[v], s1 = A.start[v + 1];
+  A.count[v] = 0u;
+  if (s1 - s0 < 2) return;
+  uint64_t *t = A.tmp;
+  for (uint32_t a = s0 + 1; a < s1; ++a) {
+    uint64_t x = t[a];
+    uint32_t b = a;
+    while (b > s0 && t[b - 1] > x) {
+      t[b] = t[b - 1];
+      --b;
+    }
+    t[b] = x;
+  }
+}
+
+// One thread per slot: move the updated state into cell-list order and refresh the FP32
+// offsets from the voxel corner.
+__global__ void k_gather(const SortArgs A) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0 && A.step_ctr) *A.step_ctr += 1;
+  if (s >= A.n_agents) return;
+  const uint32_t src = (uint32_t)(A.tmp[s] & 0xffffffffull);
+  const uint32_t k = A.nkey[src];
+  A.key[s] = k;
+  A.id[s] = A.nid[src];
+  const int64_t cap = A.cap;
+  const uint32_t sim = (A.n_sims == 1) ? 0u : A.sim_of_voxel[k];
+  const SimDev &S = A.sims[sim];
+  int idx[3] = {0, 0, 0};
+  {
+    uint32_t v = k - S.voxel_off;
+    for (int i = S.dim - 1; i >= 0; --i) {
+      idx[i] = (int)(v % (uint32_t)S.nvox[i]);
+      v /= (uint32_t)S.nvox[i];
+    }
+  }
+  const int nc = A.nc;
+  const int dim = S.dim;
+  for (int c = 0; c < nc; ++c) {
+    const double p = A.npos[c * cap + src];
+    A.pos[c * cap + s] = p;
+    A.vel[c * cap + s] = A.nvel[c * cap + src];
+    const int axis = c % dim;
+    const double corner = voxel_corner(S, axis, idx[axis]);
+    float o = (float)(p - corner);
+    // Offsets far outside the voxel (an agent kept in its old voxel because its new index
+    // fell outside the grid) would weaken the prefilter's error bound: mark them NaN so
+    // every comparison involving them falls through to the exact FP64 path.
+    if (!(fabsf(o) <= S.off_lim)) o = __int_as_float(0x7fc00000);
+    A.off[c * cap + s] = o;
+  }
+  if (A.hist) {
+    for (int c = 0; c < 2 * nc; ++c) A.hist[c * cap + s] = A.nhist[c * cap + src];
+    A.hmeta[s] = A.nhmeta[src];
+  }
+}
+
+// Initial voxel keys from the caller's agents (input order), as Domain::decompose does it
+// with CartesianCuboid::get_voxel_index_of_raw (cartesian_cuboid_n.rs:320-337): a key
+// point with pos[i] <= min[i] is a BoundaryError; an index outside the grid is an
+// IndexError ("could not find voxel index", concepts-derive/src/domain.rs:367-373).
+// Rods use the centroid row_sum / nrows (bacterial_rods.rs:368-372).
+__global__ void k_init_keys(const SortArgs A, int nv) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n_agents) return;
+  uint32_t sim = 0;
+  if (A.n_sims > 1) {
+    int lo = 0, hi = A.n_sims;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (A.sim_agent_off[mid] <= i) lo = mid; else hi = mid;
+    }
+    sim = (uint32_t)lo;
+  }
+  const SimDev &S = A.sims[sim];
+  const int dim = S.dim;
+  const int64_t cap = A.cap;
+  double kp[3];
+  for (int a = 0; a < dim; ++a) {
+    double s = 0.0;
+    if (nv == 1) {
+      s = A.npos[a * cap + i];
+    } else {
+      for (int v = 0; v < nv; ++v) s = dadd(s, A.npos[(v * dim + a) * cap + i]);
+      s = ddiv(s, (double)nv);
+    }
+    kp[a] = s;
+  }
+  int bad = 0;
+  for (int a = 0; a < dim; ++a)
+    if (S.min[a] >= kp[a]) bad = 1;
+  uint32_t plain = 0;
+  if (!bad) {
+    int r = (dim == 3) ? voxel_of<3>(S, kp, plain) : voxel_of<2>(S, kp, plain);
+    if (r == 1) bad = 1;
+    if (r == 2) bad = 2;
+  }
+  if (bad) {
+    set_status(A.status, bad == 1 ? CRG_EBOUNDARY : CRG_EINDEX, A.nid[i], 0);
+    plain = 0;
+  }
+  const uint32_t k = S.voxel_off + plain;
+  A.nkey[i] = k;
+  atomicAdd(&A.count[k], 1u);
+}
+
+// Agent-major host layout [n][nc] -> component-major device layout [nc][cap].
+__global__ void k_transpose_in(const double *__restrict__ src, double *__restrict__ dst,
+                               uint32_t n, int nc, int64_t cap) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int c = 0; c < nc; ++c) dst[c * cap + i] = src[(int64_t)i * nc + c];
+}
+
+__global__ void k_transpose_out(const double *__restrict__ src, double *__restrict__ dst,
+                                uint32_t n, int nc, int64_t cap) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int c = 0; c < nc; ++c) dst[(int64_t)i * nc + c] = src[c * cap + i];
+}
+
+}  // namespace
+
+static inline unsigned grid_for(uint64_t n, unsigned block) {
+  return (unsigned)((n + block - 1) / block);
+}
+
+void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
+  const uint32_t nb = (A.n_vox + kScanTile - 1) / kScanTile;
+  k_scan_reduce<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum);
+  k_scan_blocks<<<1, kScanThreads, 0, st>>>(bsum, nb, A.start, A.n_vox);
+  k_scan_final<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum, A.start);
+  if (A.n_agents) k_scatter<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
+  k_segsort<<<grid_for(A.n_vox, 256), 256, 0, st>>>(A);
+  if (A.n_agents) k_gather<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
+}
+
+int sort_kernel_count() { return 6; }
+
+void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st) {
+  if (A.n_agents) k_init_keys<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A, nv);
+}
+
+void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
+                         cudaStream_t st) {
+  if (n) k_transpose_in<<<grid_for(n, 256), 256, 0, st>>>(src, dst, n, nc, cap);
+}
+
+void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
+                          cudaStream_t st) {
+  if (n) k_transpose_out<<<grid_for(n, 256), 256, 0, st>>>(src, dst, n, nc, cap);
+}
+
+}  // namespace crg

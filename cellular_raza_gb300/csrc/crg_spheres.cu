@@ -1,0 +1,285 @@
+// crg_spheres.cu -- one chili step for NewtonDamped + MorsePotential spheres.
+//
+// One thread per agent in cell-list order gathers the forces from the 3^D neighbour
+// voxels (cellular_raza-building-blocks/src/domains/cartesian_cuboid_n.rs:641-662), then
+// applies the solver, the reflecting boundary and computes its next voxel key.
+//
+// Summation order.  With one subdomain chili adds, for agent a, the own-perspective
+// half-forces F_a(b)/2 voxel by voxel in ascending plain index and, inside a voxel, in the
+// voxel's Vec order; a partner in the same voxel contributes its half twice in a row
+// (update_mechanics.rs:178-203), a partner in a neighbour voxel once (:205-220, the
+// other half is dropped).  A partner in a voxel of another subdomain contributes twice
+// (steps 2 and 3, :285-382).  The loop below visits partners in exactly that order and
+// adds the same separately rounded half-forces, so with one subdomain it repeats chili's
+// sums; with several it adds the same terms in a different order.
+//
+// Candidate prefilter.  A pair whose FP32 distance (from FP32 offsets to the voxel corner,
+// error far below the margin folded into filt_thr2) exceeds the cutoff plus margin has an
+// FP64 distance above the cutoff, hence a zero force, and is skipped; everything else is
+// evaluated in FP64.  Skipping a zero changes no sum.
+#include "crg_internal.cuh"
+#include "crg_kernels.h"
+
+namespace crg {
+
+namespace {
+
+template <int D>
+struct Neigh {
+  int lo[D], hi[D];
+};
+
+// Kahan-compensated FP32 accumulation (mixed precision).
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+  float y = x - c;
+  float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+template <int D, int PREC>
+__global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n_agents) return;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  const int64_t cap = P.cap;
+  const uint32_t key = P.key[i];
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  double pa[D], va[D];
+  float oa[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    pa[c] = P.pos[c * cap + i];
+    va[c] = P.vel[c * cap + i];
+    oa[c] = P.off[c * cap + i];
+  }
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  double acc[D];
+  float fs[D], fcmp[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    acc[c] = 0.0;
+    fs[c] = 0.0f;
+    fcmp[c] = 0.0f;
+  }
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
+                           subdomain_of(S, w) != sub_v;
+        // corner(a) - corner(b) = -(j - idx) * dx
+        float kd[D];
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        const uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        for (uint32_t b = b0; b < b1; ++b) {
+          if (b == i) continue;
+          float zf[D];
+          float d2 = 0.0f;
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
+            d2 = fmaf(zf[c], zf[c], d2);
+          }
+          if (d2 > thr2) continue;  // NaN falls through to the exact path
+          if (PREC == CRG_PREC_F64) {
+            double z[D], h[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
+            if (morse_half_f64<D>(z, S, S.radius, h)) {
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                acc[c] = dadd(acc[c], h[c]);
+                if (twice) acc[c] = dadd(acc[c], h[c]);
+              }
+            }
+          } else {
+            // FP32 Morse on the FP32 displacement (offsets are accurate to ~1e-6 dx).
+            const float dist = sqrtf(d2);
+            if (!(dist > S.cutoff_f || dist == 0.0f)) {
+              const float r = S.radius_f + S.radius_f;
+              const float e = expf(-S.stiffness_f * (dist - r));
+              const float force = -2.0f * S.strength_f * S.stiffness_f * e * (1.0f - e);
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const float h = (zf[c] / dist) * force * 0.5f;
+                kahan_add(fs[c], fcmp[c], h);
+                if (twice) kahan_add(fs[c], fcmp[c], h);
+              }
+            } else if (dist != dist) {
+              // NaN positions propagate like the FP64 path would.
+#pragma unroll
+              for (int c = 0; c < D; ++c) kahan_add(fs[c], fcmp[c], dist);
+            }
+          }
+        }
+      }
+  if (PREC != CRG_PREC_F64) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = (double)fs[c] - (double)fcmp[c];
+  }
+  if (P.dbg_force) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) P.dbg_force[c * cap + i] = acc[c];
+  }
+
+  // NewtonDamped::calculate_increment (mechanics.rs:166-173): dx = v, dv = F/m - lambda v.
+  double dxv[D], dvv[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    dxv[c] = va[c];
+    dvv[c] = dsub(ddiv(acc[c], S.mass), dmul(S.damping, va[c]));
+  }
+  // Solvers (chili/solvers.rs:23-55, 156-347).  The random contribution is zero
+  // (mechanics.rs:158-164), so the final `.xapy(1, dx_rand * dt)` adds +0.
+  double np[D], nvl[D];
+  const double dt = S.dt;
+  uint8_t meta = 0;
+  if (S.order == 1) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      np[c] = dadd(dadd(dmul(dxv[c], dt), pa[c]), 0.0);
+      nvl[c] = dadd(dadd(dmul(dvv[c], dt), va[c]), 0.0);
+    }
+  } else {
+    // The history is pushed before it is read (solvers.rs:178-185), so the newest stored
+    // increment is the current one: AB2 uses [dx, dx]; AB3 uses [dx, dx] on its first step
+    // and [dx, previous, dx] afterwards.
+    const uint8_t have_prev = P.hmeta[i];
+    const bool ab3 = (S.order == 3) && have_prev;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      if (ab3) {
+        const double f0 = 23.0 / 12.0, f1 = -16.0 / 12.0, f2 = 5.0 / 12.0;
+        const double px = P.hist[c * cap + i], pv = P.hist[(D + c) * cap + i];
+        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dadd(dmul(px, f1), dmul(dxv[c], f2))), dt),
+                          pa[c]), 0.0);
+        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dadd(dmul(pv, f1), dmul(dvv[c], f2))), dt),
+                           va[c]), 0.0);
+      } else {
+        const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
+        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dmul(dxv[c], f1)), dt), pa[c]), 0.0);
+        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dmul(dvv[c], f1)), dt), va[c]), 0.0);
+      }
+      P.nhist[c * cap + i] = dxv[c];
+      P.nhist[(D + c) * cap + i] = dvv[c];
+    }
+    meta = 1;
+    P.nhmeta[i] = meta;
+  }
+
+  // CartesianSubDomain::apply_boundary (cartesian_cuboid_n.rs:594-631).
+  bool inside = true;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    if (np[c] < S.min[c]) {
+      np[c] = dsub(dmul(2.0, S.min[c]), np[c]);
+      nvl[c] = fabs(nvl[c]);
+    }
+    if (np[c] > S.max[c]) {
+      np[c] = dsub(dmul(2.0, S.max[c]), np[c]);
+      nvl[c] = -fabs(nvl[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c)
+    if (np[c] < S.min[c] || np[c] > S.max[c]) inside = false;
+  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1);
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    P.npos[c * cap + i] = np[c];
+    P.nvel[c * cap + i] = nvl[c];
+  }
+  // sort_cells_in_voxels_step_1 (update_mechanics.rs:427-456): a failed or out-of-grid
+  // index leaves the agent in its voxel.
+  uint32_t plain;
+  uint32_t nk = key;
+  if (voxel_of<D>(S, np, plain) == 0) nk = S.voxel_off + plain;
+  P.nkey[i] = nk;
+  P.nid[i] = P.id[i];
+  atomicAdd(&P.count[nk], 1u);
+}
+
+template <int D>
+__global__ void k_sphere_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_inter,
+                               uint64_t *hash) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n_agents) return;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  const int64_t cap = P.cap;
+  const uint32_t v = P.key[i] - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  uint32_t nc = 0, ni = 0;
+  uint64_t h = 0;
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        for (uint32_t b = P.start[S.voxel_off + w]; b < P.start[S.voxel_off + w + 1]; ++b) {
+          if (b == i) continue;
+          ++nc;
+          uint64_t x = P.id[b] + 0x9e3779b97f4a7c15ull;
+          x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+          x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+          h += x ^ (x >> 31);
+          double z[D], hf[D];
+          for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + i], P.pos[c * cap + b]);
+          if (morse_half_f64<D>(z, S, S.radius, hf)) ++ni;
+        }
+      }
+  n_cand[i] = nc;
+  n_inter[i] = ni;
+  hash[i] = h;
+}
+
+}  // namespace
+
+void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st) {
+  if (!P.n_agents) return;
+  if (block <= 0 || block > 256) block = 128;
+  const unsigned grid = (P.n_agents + block - 1) / block;
+  if (dim == 3) {
+    if (precision == CRG_PREC_F64)
+      k_spheres_step<3, CRG_PREC_F64><<<grid, block, 0, st>>>(P);
+    else
+      k_spheres_step<3, CRG_PREC_MIXED><<<grid, block, 0, st>>>(P);
+  } else {
+    if (precision == CRG_PREC_F64)
+      k_spheres_step<2, CRG_PREC_F64><<<grid, block, 0, st>>>(P);
+    else
+      k_spheres_step<2, CRG_PREC_MIXED><<<grid, block, 0, st>>>(P);
+  }
+}
+
+void launch_sphere_stats(int dim, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,
+                         uint64_t *hash, cudaStream_t st) {
+  if (!P.n_agents) return;
+  const unsigned grid = (P.n_agents + 127) / 128;
+  if (dim == 3)
+    k_sphere_stats<3><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash);
+  else
+    k_sphere_stats<2><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash);
+}
+
+}  // namespace crg

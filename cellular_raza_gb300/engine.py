@@ -1,0 +1,211 @@
+"""Python handle over the C ABI: one simulation or a batch of simulations on the GPU.
+
+This is a thin owner of a ``crg_ctx*``; every call goes through libcrg.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+from .workloads import Model
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def to_c(model: Model):
+    d = N.CrgDomain()
+    d.dim = model.dim
+    if model.n_voxels is None:
+        d.voxel_mode = 0
+        d.interaction_range = float(model.interaction_range)
+    else:
+        d.voxel_mode = 1
+        for i, n in enumerate(model.n_voxels):
+            d.n_voxels[i] = int(n)
+    for i in range(model.dim):
+        d.min[i] = float(model.domain_min[i])
+        d.max[i] = float(model.domain_max[i])
+    d.n_subdomains = int(model.n_subdomains)
+    d.weight_mode = int(model.weight_mode)
+    m = N.CrgModel()
+    m.kind = N.KIND_ROD if model.kind == "rod" else N.KIND_SPHERE
+    m.n_vertices = int(model.n_vertices)
+    m.solver_order = int(model.solver_order)
+    m.precision = N.PREC_MIXED if model.precision == "mixed" else N.PREC_F64
+    for f in ("mass", "damping", "spring_tension", "rigidity", "spring_length", "diffusion",
+              "radius", "stiffness", "cutoff", "strength", "dt"):
+        setattr(m, f, float(getattr(model, f)))
+    return d, m
+
+
+class Simulation:
+    """A crg handle holding one or more simulations advanced by the same launches."""
+
+    def __init__(self, models: Sequence[Model], capacities: Sequence[int]):
+        self._L = N.load()
+        self.models = list(models)
+        self.nc = self.models[0].nc
+        self.dim = self.models[0].dim
+        self.nv = self.models[0].n_vertices
+        n = len(self.models)
+        doms = (N.CrgDomain * n)()
+        mods = (N.CrgModel * n)()
+        for s, mdl in enumerate(self.models):
+            doms[s], mods[s] = to_c(mdl)
+        caps = (C.c_int64 * n)(*[int(c) for c in capacities])
+        h = C.c_void_p()
+        if n == 1:
+            rc = self._L.crg_create(C.byref(doms[0]), C.byref(mods[0]), caps[0], C.byref(h))
+        else:
+            rc = self._L.crg_create_batch(n, doms, mods, caps, C.byref(h))
+        N.check(rc, "crg_create")
+        self._h = h
+        self.counts: List[int] = [0] * n
+
+    @classmethod
+    def single(cls, model: Model, capacity: int) -> "Simulation":
+        return cls([model], [capacity])
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.crg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ------------------------------------------------------------------ data movement
+    def upload(self, pos: np.ndarray, vel: np.ndarray, counts: Optional[Sequence[int]] = None,
+               ids: Optional[np.ndarray] = None):
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        vel = np.ascontiguousarray(vel, dtype=np.float64)
+        n = pos.shape[0]
+        if pos.size != n * self.nc or vel.shape != pos.shape:
+            raise ValueError("pos/vel must have shape [n][n_vertices][dim]")
+        cnt = None
+        if len(self.models) > 1:
+            if counts is None:
+                raise ValueError("a batch upload needs per-simulation counts")
+            cnt = (C.c_int64 * len(self.models))(*[int(c) for c in counts])
+            self.counts = [int(c) for c in counts]
+        else:
+            self.counts = [n]
+        idp = None
+        if ids is not None:
+            ids = np.ascontiguousarray(ids, dtype=np.uint64)
+            idp = ids.ctypes.data_as(C.POINTER(C.c_uint64))
+        rc = self._L.crg_upload(self._h, n, cnt, _dp(pos), _dp(vel), idp)
+        N.check(rc, "crg_upload", self._h)
+
+    def step(self, n_steps: int = 1):
+        rc = self._L.crg_step(self._h, int(n_steps))
+        N.check(rc, "crg_step", self._h)
+
+    @property
+    def n_agents(self) -> int:
+        n = C.c_int64()
+        self._L.crg_agent_count(self._h, C.byref(n))
+        return n.value
+
+    def download(self, order: str = "list") -> Dict[str, np.ndarray]:
+        """Current state.  order="list": cell-list order; "id": per simulation sorted by id
+        (ids 0..n-1 when upload was given no ids)."""
+        n = self.n_agents
+        shape = (n, self.nv, self.dim)
+        pos = np.empty(shape)
+        vel = np.empty(shape)
+        ids = np.empty(n, np.uint64)
+        vox = np.empty(n, np.uint32)
+        rc = self._L.crg_download(self._h, _dp(pos), _dp(vel),
+                                  ids.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                  vox.ctypes.data_as(C.POINTER(C.c_uint32)))
+        N.check(rc, "crg_download", self._h)
+        out = {"pos": pos, "vel": vel, "ids": ids, "voxel": vox}
+        if order == "id":
+            out = self._by_id(out)
+        return out
+
+    def _by_id(self, out):
+        # simulations occupy consecutive ranges of the cell list
+        res = {k: np.empty_like(v) for k, v in out.items()}
+        off = 0
+        for c in self.counts:
+            sl = slice(off, off + c)
+            perm = np.argsort(out["ids"][sl], kind="stable")
+            for k, v in out.items():
+                res[k][sl] = v[sl][perm]
+            off += c
+        return res
+
+    # ------------------------------------------------------------------ options / diagnostics
+    def set_option(self, opt: int, value: int):
+        N.check(self._L.crg_set_option(self._h, int(opt), int(value)), "crg_set_option")
+
+    def debug_forces(self) -> Dict[str, np.ndarray]:
+        n = self.n_agents
+        f = np.empty((n, self.nv, self.dim))
+        ids = np.empty(n, np.uint64)
+        rc = self._L.crg_debug_forces(self._h, _dp(f), ids.ctypes.data_as(C.POINTER(C.c_uint64)))
+        N.check(rc, "crg_debug_forces")
+        return {"force": f, "ids": ids}
+
+    def neighbor_stats(self) -> Dict[str, np.ndarray]:
+        n = self.n_agents
+        nc = np.empty(n, np.uint32)
+        ni = np.empty(n, np.uint32)
+        h = np.empty(n, np.uint64)
+        ids = np.empty(n, np.uint64)
+        u32 = C.POINTER(C.c_uint32)
+        u64 = C.POINTER(C.c_uint64)
+        rc = self._L.crg_debug_neighbor_stats(self._h, nc.ctypes.data_as(u32),
+                                              ni.ctypes.data_as(u32), h.ctypes.data_as(u64),
+                                              ids.ctypes.data_as(u64))
+        N.check(rc, "crg_debug_neighbor_stats")
+        return {"n_cand": nc, "n_inter": ni, "cand_hash": h, "ids": ids}
+
+    def snapshot(self, restore: bool = False):
+        N.check(self._L.crg_snapshot(self._h, 1 if restore else 0), "crg_snapshot")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        N.check(self._L.crg_get_stream(self._h, C.byref(s)), "crg_get_stream")
+        return s.value or 0
+
+    def profile(self):
+        out = (C.c_double * 3)()
+        N.check(self._L.crg_profile(self._h, out), "crg_profile")
+        return {"force_ms": out[0], "sort_ms": out[1], "kernels": int(out[2])}
+
+
+def measure_fma_peaks():
+    """Measured FP64 / FP32 FMA throughput (TFLOP/s) of the current GPU."""
+    L = N.load()
+    a, b = C.c_double(), C.c_double()
+    N.check(L.crg_measure_fma_peaks(C.byref(a), C.byref(b)), "crg_measure_fma_peaks")
+    return {"fp64_tflops": a.value, "fp32_tflops": b.value}
+
+
+def run(workload, n_steps: Optional[int] = None, **opts) -> Dict[str, np.ndarray]:
+    """Upload a workload, run it and return the final state ordered by id."""
+    steps = workload.n_steps if n_steps is None else n_steps
+    with Simulation.single(workload.model, workload.n) as sim:
+        for k, v in opts.items():
+            sim.set_option(k, v)
+        sim.upload(workload.pos, workload.vel)
+        sim.step(steps)
+        return sim.download(order="id")

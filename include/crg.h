@@ -1,0 +1,177 @@
+/*
+ * crg.h -- C ABI of the GB300 mechanics/interaction backend for cellular_raza's chili loop.
+ *
+ * One handle runs one or more independent simulations ("a pack") on the current CUDA
+ * device.  A step is the chili Mechanics+Interaction step:
+ *   update_mechanics_interaction_step_1/2/3   (cellular_raza-core/src/backend/chili/
+ *                                              update_mechanics.rs:153-382)
+ *   local_mechanics_update                    (update_mechanics.rs:530-559)
+ *   apply_boundary                            (update_mechanics.rs:387-406)
+ *   sort_cells_in_voxels_step_1/2             (update_mechanics.rs:418-513)
+ * with NewtonDamped{2,3}D + MorsePotential spheres or RodMechanics + RodInteraction<Morse>
+ * rods on a CartesianCuboid with reflecting walls.
+ *
+ * Conventions: every call returns a status (CRG_OK = 0, else one of CRG_E*); the caller
+ * owns every host array and no pointer is retained past a call; the library owns device
+ * memory for the lifetime of the handle.  A handle is single-threaded; different handles
+ * may be used from different threads.  Nothing here aborts or traps.
+ *
+ * Host arrays of positions/velocities are agent-major: [n][n_vertices][dim] doubles
+ * (n_vertices = 1 for spheres), matching RodMechanics::pos rows
+ * (cellular_raza-building-blocks/src/cell_building_blocks/bacterial_rods.rs:82-107) and
+ * NewtonDamped::pos (mechanics.rs:14-80).
+ */
+#ifndef CRG_H
+#define CRG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The first five mirror chili's SimulationError variants
+ * (cellular_raza-core/src/backend/chili/errors.rs:73-122). */
+#define CRG_OK 0
+#define CRG_ECALC 1       /* CalcError */
+#define CRG_EBOUNDARY 2   /* BoundaryError (agent left the domain after reflection) */
+#define CRG_EINDEX 3      /* IndexError (agent outside every voxel at insertion) */
+#define CRG_EDECOMPOSE 4  /* DecomposeError (n_subdomains cannot split the voxels) */
+#define CRG_EINVAL 5      /* invalid argument */
+#define CRG_ENOMEM 6      /* device allocation failed / admission budget exceeded */
+#define CRG_ECUDA 7       /* CUDA runtime error */
+#define CRG_ETIMEDOUT 8   /* bounded device-side wait expired */
+#define CRG_ENOTSUP 9     /* feature outside what this build supports */
+
+#define CRG_KIND_SPHERE 0 /* NewtonDamped{2,3}D + MorsePotential */
+#define CRG_KIND_ROD 1    /* RodMechanics<f64,D> + RodInteraction<MorsePotential> */
+
+#define CRG_PREC_F64 0    /* every operation in FP64, in the reference's order */
+#define CRG_PREC_MIXED 1  /* FP32 pair forces with Kahan sums; FP64 state and update */
+
+#define CRG_WEIGHTS_CHILI 0    /* chili's subdomain-dependent pair weights (default) */
+#define CRG_WEIGHTS_PHYSICAL 1 /* every pair with weight 1 (not reference behaviour) */
+
+/* CartesianCuboid (cellular_raza-building-blocks/src/domains/cartesian_cuboid_n.rs:65-72)
+ * plus chili's Settings::n_threads (cellular_raza-core/src/backend/chili/setup.rs:17-27),
+ * which sets the number of subdomains and with it chili's pair weights. */
+typedef struct crg_domain {
+  int32_t dim;        /* 2 or 3 */
+  int32_t voxel_mode; /* 0: from_boundaries_and_interaction_range (:183-222)
+                         1: from_boundaries_and_n_voxels (:226-256) */
+  double min[3];
+  double max[3];
+  double interaction_range; /* voxel_mode 0 */
+  int64_t n_voxels[3];      /* voxel_mode 1 */
+  int32_t n_subdomains;     /* chili n_threads (>= 1) */
+  int32_t weight_mode;      /* CRG_WEIGHTS_* */
+} crg_domain;
+
+/* Agent model: Mechanics + Interaction parameters shared by every agent of a simulation.
+ *   spheres: NewtonDamped (mass, damping) + MorsePotential (radius, stiffness = potential_
+ *            stiffness, cutoff, strength)  (mechanics.rs:14-204, interaction.rs:184-299)
+ *   rods:    RodMechanics (spring_tension, rigidity, spring_length, damping, diffusion)
+ *            + RodInteraction(MorsePotential)  (bacterial_rods.rs:82-337)
+ * solver_order is run_simulation!'s mechanics_solver_order (1 Euler, 2 AB2, 3 AB3;
+ * cellular_raza-core-proc-macro/src/kwargs.rs:219-230). */
+typedef struct crg_model {
+  int32_t kind;         /* CRG_KIND_* */
+  int32_t n_vertices;   /* rods: vertices per rod (2..8); spheres: 1 */
+  int32_t solver_order; /* 1, 2 or 3 */
+  int32_t precision;    /* CRG_PREC_* */
+  double mass, damping;
+  double spring_tension, rigidity, spring_length, diffusion;
+  double radius, stiffness, cutoff, strength;
+  double dt;
+} crg_model;
+
+typedef struct crg_ctx crg_ctx;
+
+/* Creates a handle for one simulation with room for `capacity` agents.
+ * Replaces construct_simulation_runner (chili/datastructures.rs:51-217). */
+int32_t crg_create(const crg_domain *domain, const crg_model *model, int64_t capacity,
+                   crg_ctx **out);
+
+/* Creates a handle for `n_sims` independent simulations stepped by the same launches
+ * (batched form).  All models share kind, n_vertices, dim, precision and solver_order;
+ * parameters, domains and agent counts may differ.  capacities[s] bounds sim s. */
+int32_t crg_create_batch(int32_t n_sims, const crg_domain *domains, const crg_model *models,
+                         const int64_t *capacities, crg_ctx **out);
+
+/* Copies agents in from host memory and sorts them into voxels.  `ids` may be NULL
+ * (then agent k gets id k, like CellIdentifier::Initial(k)).  For a batch handle,
+ * counts[s] agents of sim s follow each other in the arrays (pass n = sum(counts));
+ * for a single handle pass counts = NULL.  Replaces Domain::decompose +
+ * insert_initial_cells (concepts-derive/src/domain.rs:292-400,
+ * chili/datastructures.rs:278-299): an agent with pos <= min on some axis is
+ * CRG_EBOUNDARY, one outside every voxel CRG_EINDEX. */
+int32_t crg_upload(crg_ctx *ctx, int64_t n, const int64_t *counts, const double *pos,
+                   const double *vel, const uint64_t *ids);
+
+/* Advances every simulation of the handle by n_steps chili steps (the macro-generated
+ * loop body, cellular_raza-core-proc-macro/src/run_sim.rs:380-403).  Stops at the first
+ * device-reported error and returns it; crg_last_error gives the agent and step. */
+int32_t crg_step(crg_ctx *ctx, int64_t n_steps);
+
+/* Copies the current agents out in cell-list order (sorted by voxel).  Any pointer may be
+ * NULL.  voxel receives the voxel plain index (per simulation). */
+int32_t crg_download(crg_ctx *ctx, double *pos, double *vel, uint64_t *ids, uint32_t *voxel);
+
+/* Number of agents currently held (total over simulations of a batch). */
+int32_t crg_agent_count(crg_ctx *ctx, int64_t *n);
+
+/* First error seen on the device: code, agent id and 1-based step (or -1). */
+int32_t crg_last_error(crg_ctx *ctx, int64_t *agent, int64_t *step);
+
+/* Device-side checkpoint of the whole handle state (cell list, velocities, solver history,
+ * step counter): CRG_SNAPSHOT_SAVE copies it into a second device buffer (allocated on the
+ * first save), CRG_SNAPSHOT_RESTORE copies it back.  chili has no checkpoint (planned,
+ * cellular_raza-core/src/lib.rs:14-22); its save points (chili/datastructures.rs:349-396)
+ * persist the same state. */
+#define CRG_SNAPSHOT_SAVE 0
+#define CRG_SNAPSHOT_RESTORE 1
+int32_t crg_snapshot(crg_ctx *ctx, int32_t op);
+
+/* The CUDA stream (cudaStream_t) every launch of the handle is issued on, for callers that
+ * order their own work or events against it. */
+int32_t crg_get_stream(crg_ctx *ctx, void **stream);
+
+/* Destroys the handle and frees its device memory. */
+int32_t crg_destroy(crg_ctx *ctx);
+
+/* Human-readable name of a status code (static string). */
+const char *crg_strerror(int32_t code);
+
+/* ---- options and diagnostics ------------------------------------------------------- */
+#define CRG_OPT_PREFILTER 1  /* 1 (default): FP32 candidate prefilter on; 0: off */
+#define CRG_OPT_GRAPH_CHUNK 2 /* steps per captured CUDA graph (0 disables graphs) */
+#define CRG_OPT_BLOCK 3       /* threads per block of the force kernel (autotuner) */
+int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
+
+/* Interaction force accumulated during the most recent step, [n][nv][dim] in the order
+ * of the ids array (same layout as crg_download's ids).  Capture must have been enabled
+ * with crg_set_option(ctx, CRG_OPT_DEBUG_FORCES, 1) before that step. */
+#define CRG_OPT_DEBUG_FORCES 5
+int32_t crg_debug_forces(crg_ctx *ctx, double *force, uint64_t *ids);
+
+/* Neighbour statistics of the CURRENT cell list (what the next step will visit): per agent
+ * the number of candidate partners in its 3^D voxel neighbourhood, the number with
+ * 0 < d <= cutoff (spheres), and a sum of splitmix64(id) over the candidates; in the order
+ * of ids. */
+int32_t crg_debug_neighbor_stats(crg_ctx *ctx, uint32_t *n_cand, uint32_t *n_inter,
+                                 uint64_t *cand_hash, uint64_t *ids);
+
+/* Device time of the kernels of the last crg_step call, split by phase (ms):
+ * [0] force+update, [1] sort; [2] number of kernels launched.  Requires
+ * CRG_OPT_PROFILE = 1 (events disable graph capture). */
+#define CRG_OPT_PROFILE 4
+int32_t crg_profile(crg_ctx *ctx, double *out3);
+
+/* Measures the FP64 and FP32 fused-multiply-add throughput of the current device with a
+ * dependent-chain microbenchmark (TFLOP/s, 2 flops per FMA). */
+int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRG_H */
