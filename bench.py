@@ -54,11 +54,23 @@ def dist_env():
     return rank, world, local
 
 
-def make_workload(name, n_sub):
+# chili's n_threads for every arm: the number of subdomains fixes chili's pair weights, so
+# both arms and the parity tests run the same physics whatever the host's core count.
+N_SUBDOMAINS = 16
+# The rods workload is unstable under the reference's own RodMechanics: crushed rods fold
+# to angles where the tan(angle/2) curvature force diverges and the run ends with a
+# BoundaryError near step 450 (the oracle and the GPU stop at the same rod and step).
+# The timed run therefore covers the first 400 of the 500 configured steps.
+RODS_TIMED_STEPS = 400
+
+
+def make_workload(name, n_sub=N_SUBDOMAINS):
     from cellular_raza_gb300 import workloads as W
 
     if name == "rods_2d":
-        return W.rods_2d(seed=2024, n_subdomains=n_sub)
+        w = W.rods_2d(seed=2024, n_subdomains=n_sub)
+        w.n_steps = RODS_TIMED_STEPS
+        return w
     return W.spheres_3d(seed=2024, n_subdomains=n_sub)
 
 
@@ -157,8 +169,8 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    n_threads = os.cpu_count() or 1
-    w = make_workload(args.workload, n_threads)
+    n_threads = N_SUBDOMAINS  # chili runs one OS thread per subdomain
+    w = make_workload(args.workload)
     import pyoracle
 
     pyoracle.build()
@@ -218,8 +230,8 @@ def crg_arm(args):
     from cellular_raza_gb300 import _native as N
     from cellular_raza_gb300 import engine as E
 
-    n_cpu = os.cpu_count() or 1
-    w = make_workload(args.workload, n_cpu)
+    n_cpu = N_SUBDOMAINS
+    w = make_workload(args.workload)
     sim = E.Simulation.single(w.model, w.n)
     sim.upload(w.pos, w.vel)
     sim.snapshot()

@@ -395,10 +395,18 @@ void launch_one_step(crg_ctx *c) {
   crg::launch_sort(sort_args(c, 0), c->bsum, c->stream);
 }
 
+// Waits for the handle's stream and reads the device status word.  A CUDA failure is
+// recorded as the handle's error (so every later call reports it too).
 int32_t read_status(crg_ctx *c) {
-  CUDA_TRY(cudaMemcpyAsync(c->h_status, c->status, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                           c->stream));
-  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  cudaError_t e = cudaMemcpyAsync(c->h_status, c->status, 4 * sizeof(int32_t),
+                                  cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    c->err_code = (e == cudaErrorMemoryAllocation) ? CRG_ENOMEM : CRG_ECUDA;
+    c->err_agent = -1;
+    c->err_step = c->steps_done;
+    return c->err_code;
+  }
   if (c->h_status[0] != CRG_OK) {
     c->err_code = c->h_status[0];
     c->err_agent = (int64_t)(((uint64_t)(uint32_t)c->h_status[2] << 32) | (uint32_t)c->h_status[1]);
@@ -451,6 +459,7 @@ const char *crg_strerror(int32_t code) {
     case CRG_ECUDA: return "CUDA runtime error";
     case CRG_ETIMEDOUT: return "device wait timed out";
     case CRG_ENOTSUP: return "not supported";
+    case CRG_EINTERNAL: return "device-side invariant check failed";
     default: return "unknown status";
   }
 }
@@ -586,7 +595,11 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
       for (int s = 0; s < k; ++s) launch_one_step(c);
       left -= k;
     }
-    CUDA_TRY(cudaGetLastError());
+    if (cudaGetLastError() != cudaSuccess) {
+      c->err_code = CRG_ECUDA;
+      c->err_step = c->steps_done;
+      break;
+    }
     int32_t r = read_status(c);
     if (r != CRG_OK) break;
   }

@@ -149,6 +149,27 @@ __device__ __forceinline__ void set_status(int32_t *status, int32_t code, uint64
   }
 }
 
+// Invariant checks of the cell list.  A violation records CRG_EINTERNAL with the index and
+// the check site (in the step slot of the status word); the caller skips the access.
+enum CheckSite : int32_t {
+  kSiteForceKey = 1,    // key of an agent outside the pack's voxels
+  kSiteForceRange = 2,  // voxel agent range outside [0, n_agents]
+  kSiteNextKey = 3,     // next key outside the pack's voxels
+  kSiteScatterKey = 4,
+  kSiteScatterSlot = 5,
+  kSiteSegRange = 6,
+  kSiteGatherSrc = 7,
+  kSiteGatherKey = 8,
+};
+
+__device__ __forceinline__ void invariant_failed(int32_t *status, int32_t site, uint64_t index) {
+  if (atomicCAS(&status[0], 0, CRG_EINTERNAL) == 0) {
+    status[1] = (int32_t)(index & 0xffffffffu);
+    status[2] = (int32_t)(index >> 32);
+    status[3] = site;
+  }
+}
+
 // calculate_morse_interaction (cellular_raza-building-blocks/src/cell_building_blocks/
 // interaction.rs:151-182) in FP64, returning the own-perspective force already scaled by
 // one half (chili adds f.xa(1/2), update_mechanics.rs:98,194-199).  Each operation is

@@ -179,7 +179,11 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
   const SimDev &S = P.sims[sim];
   const int64_t cap = P.cap;
-  const uint32_t key = P.key[i];
+  uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
   const uint32_t v = key - S.voxel_off;
   int idx[D];
   unravel<D>(S, v, idx);
@@ -203,7 +207,9 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
     amin[k % D] = fminf(amin[k % D], oa[k]);
     amax[k % D] = fmaxf(amax[k % D], oa[k]);
   }
-  const bool a_nan = !(amin[0] == amin[0]) || !(amax[D - 1] == amax[D - 1]);
+  bool a_nan = false;  // fminf/fmaxf drop NaNs, so test every offset
+#pragma unroll
+  for (int k = 0; k < NC; ++k) a_nan |= !(oa[k] == oa[k]);
   const uint32_t sub_v = subdomain_of(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
@@ -229,7 +235,11 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
         kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
         kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
         if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        const uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        if (b0 > b1 || b1 > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b1 = b0;
+        }
         for (uint32_t b = b0; b < b1; ++b) {
           if (b == i) continue;
           float ob[NC];
@@ -406,6 +416,10 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   uint32_t plain;
   uint32_t nk = key;
   if (voxel_of<D>(S, cen, plain) == 0) nk = S.voxel_off + plain;
+  if (nk - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteNextKey, i);
+    nk = key;
+  }
   P.nkey[i] = nk;
   P.nid[i] = P.id[i];
   atomicAdd(&P.count[nk], 1u);

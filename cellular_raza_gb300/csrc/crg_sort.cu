@@ -34,6 +34,7 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
 // writes the block total to *total.
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total) {
   __shared__ uint32_t warp_tot[32];
+  __shared__ uint32_t block_tot;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = (blockDim.x + 31) >> 5;
   uint32_t incl = warp_incl_scan(x);
@@ -42,12 +43,12 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total)
   if (warp == 0) {
     uint32_t t = (lane < nwarps) ? warp_tot[lane] : 0u;
     uint32_t ti = warp_incl_scan(t);
-    if (lane < nwarps) warp_tot[lane] = ti - t;
-    if (lane == 31) warp_tot[31] = ti;  // total (nwarps <= 32)
+    if (lane < nwarps) warp_tot[lane] = ti - t;  // exclusive prefix of each warp
+    if (lane == 31) block_tot = ti;              // total (nwarps <= 32)
   }
   __syncthreads();
   uint32_t res = warp_tot[warp] + incl - x;
-  *total = warp_tot[31];
+  *total = block_tot;
   __syncthreads();
   return res;
 }
@@ -118,7 +119,15 @@ __global__ void k_scatter(const SortArgs A) {
       cls = (subdomain_of(S, k - S.voxel_off) == subdomain_of(S, old - S.voxel_off)) ? 1u : 2u;
     }
   }
+  if (k >= A.n_vox) {
+    invariant_failed(A.status, kSiteScatterKey, i);
+    return;
+  }
   const uint32_t slot = A.start[k] + atomicAdd(&A.count[k], 1u);
+  if (slot >= A.n_agents) {
+    invariant_failed(A.status, kSiteScatterSlot, i);
+    return;
+  }
   A.tmp[slot] = ((uint64_t)cls << 32) | (uint64_t)i;
 }
 
@@ -128,6 +137,10 @@ __global__ void k_segsort(const SortArgs A) {
   if (v >= A.n_vox) return;
   const uint32_t s0 = A.start[v], s1 = A.start[v + 1];
   A.count[v] = 0u;
+  if (s0 > s1 || s1 > A.n_agents) {
+    invariant_failed(A.status, kSiteSegRange, v);
+    return;
+  }
   if (s1 - s0 < 2) return;
   uint64_t *t = A.tmp;
   for (uint32_t a = s0 + 1; a < s1; ++a) {
@@ -147,8 +160,16 @@ __global__ void k_gather(const SortArgs A) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && A.step_ctr) *A.step_ctr += 1;
   if (s >= A.n_agents) return;
-  const uint32_t src = (uint32_t)(A.tmp[s] & 0xffffffffull);
-  const uint32_t k = A.nkey[src];
+  uint32_t src = (uint32_t)(A.tmp[s] & 0xffffffffull);
+  if (src >= A.n_agents) {
+    invariant_failed(A.status, kSiteGatherSrc, s);
+    src = s;
+  }
+  uint32_t k = A.nkey[src];
+  if (k >= A.n_vox) {
+    invariant_failed(A.status, kSiteGatherKey, s);
+    k = 0;
+  }
   A.key[s] = k;
   A.id[s] = A.nid[src];
   const int64_t cap = A.cap;

@@ -44,7 +44,11 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
   const SimDev &S = P.sims[sim];
   const int64_t cap = P.cap;
-  const uint32_t key = P.key[i];
+  uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
   const uint32_t v = key - S.voxel_off;
   int idx[D];
   unravel<D>(S, v, idx);
@@ -84,7 +88,11 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
         kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
         kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
         if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        const uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        if (b0 > b1 || b1 > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b1 = b0;
+        }
         for (uint32_t b = b0; b < b1; ++b) {
           if (b == i) continue;
           float zf[D];
@@ -208,6 +216,10 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
   uint32_t plain;
   uint32_t nk = key;
   if (voxel_of<D>(S, np, plain) == 0) nk = S.voxel_off + plain;
+  if (nk - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteNextKey, i);
+    nk = key;
+  }
   P.nkey[i] = nk;
   P.nid[i] = P.id[i];
   atomicAdd(&P.count[nk], 1u);

@@ -200,12 +200,14 @@ def measure_fma_peaks():
     return {"fp64_tflops": a.value, "fp32_tflops": b.value}
 
 
-def run(workload, n_steps: Optional[int] = None, **opts) -> Dict[str, np.ndarray]:
-    """Upload a workload, run it and return the final state ordered by id."""
+def run(workload, n_steps: Optional[int] = None, options: Optional[Dict[int, int]] = None,
+        order: str = "id") -> Dict[str, np.ndarray]:
+    """Upload a workload, run it and return the final state (ordered by id by default).
+    ``options`` maps CRG_OPT_* values to settings."""
     steps = workload.n_steps if n_steps is None else n_steps
     with Simulation.single(workload.model, workload.n) as sim:
-        for k, v in opts.items():
+        for k, v in (options or {}).items():
             sim.set_option(k, v)
         sim.upload(workload.pos, workload.vel)
         sim.step(steps)
-        return sim.download(order="id")
+        return sim.download(order=order)

@@ -42,6 +42,8 @@ extern "C" {
 #define CRG_ECUDA 7       /* CUDA runtime error */
 #define CRG_ETIMEDOUT 8   /* bounded device-side wait expired */
 #define CRG_ENOTSUP 9     /* feature outside what this build supports */
+#define CRG_EINTERNAL 10  /* a device-side invariant check failed; the access was skipped
+                             (crg_last_error: agent = index, step = check site) */
 
 #define CRG_KIND_SPHERE 0 /* NewtonDamped{2,3}D + MorsePotential */
 #define CRG_KIND_ROD 1    /* RodMechanics<f64,D> + RodInteraction<MorsePotential> */

@@ -902,9 +902,11 @@ struct Sim {
   }
 
   void export_state(double *pos, double *vel, or_debug *dbg) {
+    size_t k = 0;
     for (Box &b : boxes)
       for (Voxel &v : b.voxels)
         for (Entry &e : v.cells) {
+          if (dbg && dbg->order_out) dbg->order_out[k++] = e.c.id;
           std::memcpy(pos + e.c.id * NC, e.c.pos, sizeof(e.c.pos));
           std::memcpy(vel + e.c.id * NC, e.c.vel, sizeof(e.c.vel));
           if (dbg && dbg->voxel_out) dbg->voxel_out[e.c.id] = (uint32_t)v.plain;

@@ -60,6 +60,8 @@ typedef struct or_debug {
   uint32_t *n_cand;      /* [n]: candidate partners scanned in the last step */
   uint32_t *n_inter;     /* [n]: partners with 0 < d <= cutoff (spheres) */
   uint64_t *cand_hash;   /* [n]: sum of mix(id) over candidate partners */
+  uint64_t *order_out;   /* [n]: agent ids in chili's storage order (voxels ascending,
+                            each voxel's Vec order) after the last step */
   int64_t error_agent;   /* filled on error: agent id, else -1 */
   int64_t error_step;    /* filled on error: 1-based step, else -1 */
 } or_debug;

@@ -60,6 +60,7 @@ class OrDebug(C.Structure):
         ("n_cand", C.POINTER(C.c_uint32)),
         ("n_inter", C.POINTER(C.c_uint32)),
         ("cand_hash", C.POINTER(C.c_uint64)),
+        ("order_out", C.POINTER(C.c_uint64)),
         ("error_agent", C.c_int64),
         ("error_step", C.c_int64),
     ]
@@ -161,6 +162,8 @@ def run(model, pos, vel, n_steps, debug=False):
         out["n_cand"] = np.zeros(n, np.uint32)
         out["n_inter"] = np.zeros(n, np.uint32)
         out["cand_hash"] = np.zeros(n, np.uint64)
+        out["order"] = np.zeros(n, np.uint64)
+        dbg.order_out = out["order"].ctypes.data_as(C.POINTER(C.c_uint64))
         dbg.force_last = _dp(out["force"])
         dbg.voxel_out = out["voxel"].ctypes.data_as(C.POINTER(C.c_uint32))
         dbg.n_cand = out["n_cand"].ctypes.data_as(C.POINTER(C.c_uint32))

@@ -37,8 +37,11 @@ def gpu_one_step(gpu, w):
     stats = sim.neighbor_stats()
     sim.step(1)
     f = sim.debug_forces()
+    lst = sim.download(order="list")
     st1 = sim.download(order="id")
     sim.close()
+    st1["list_ids"] = lst["ids"]
+    st1["list_voxel"] = lst["voxel"]
     return st0, stats, by_id(f["force"], f["ids"]), st1
 
 
@@ -49,6 +52,10 @@ def check_one_step(gpu, oracle, w):
     # insertion and re-sort keys: bit-exact
     assert np.array_equal(st0["voxel"], init_vox)
     assert np.array_equal(st1["voxel"], ref["voxel"])
+    # cell list: sorted by voxel, and inside each voxel chili's Vec order (stayers, then
+    # movers of the same subdomain, then movers of other subdomains, each by source order)
+    assert np.all(np.diff(st1["list_voxel"].astype(np.int64)) >= 0)
+    assert np.array_equal(st1["list_ids"], ref["order"])
     # neighbour sets visited in the step: bit-exact
     ids = stats["ids"].astype(np.int64)
     assert np.array_equal(by_id(stats["n_cand"], ids), ref["n_cand"])
@@ -98,11 +105,11 @@ def test_prefilter_is_exact(gpu):
     and without it are bitwise identical."""
     w = W.spheres_3d(seed=14, n_subdomains=2)
     a = E.run(w, 100)
-    b = E.run(w, 100, **{N.OPT_PREFILTER: 0})
+    b = E.run(w, 100, options={N.OPT_PREFILTER: 0})
     assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
     r = W.rods_2d(seed=14, n=4000)
     a = E.run(r, 20)
-    b = E.run(r, 20, **{N.OPT_PREFILTER: 0})
+    b = E.run(r, 20, options={N.OPT_PREFILTER: 0})
     assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
 
 
@@ -180,3 +187,21 @@ def test_insertion_errors(gpu):
         with pytest.raises(N.CrgError) as e:
             sim.upload(pos, w.vel)
         assert e.value.code == N.CRG_EINDEX
+
+
+def test_large_grids_many_scan_tiles(gpu, oracle):
+    """Voxel grids spanning many 4,096-voxel scan tiles (the cell-list scan is tiled)."""
+    w = W.spheres_3d(seed=51, n=40_000)  # 28^3 = 21,952 voxels
+    ref, st1 = check_one_step(gpu, oracle, w)
+    r = W.rods_2d(seed=52, n=30_000, n_subdomains=7)  # 136^2 = 18,496 voxels
+    check_one_step(gpu, oracle, r)
+
+
+def test_cell_list_order_over_many_steps(gpu, oracle):
+    """After many steps with agents crossing voxels and subdomains, the GPU cell list holds
+    exactly chili's per-voxel order."""
+    for n_sub in (1, 6):
+        w = W.spheres_3d(seed=53, n=6000, n_subdomains=n_sub)
+        ref = oracle.run(w.model, w.pos, w.vel, 60, debug=True)
+        got = E.run(w, 60, order="list")
+        assert np.array_equal(got["ids"], ref["order"])
