@@ -22,8 +22,10 @@ EXPORTED = [
     "crg_create", "crg_create_batch", "crg_upload", "crg_step", "crg_download",
     "crg_agent_count", "crg_last_error", "crg_destroy", "crg_strerror", "crg_set_option",
     "crg_debug_forces", "crg_debug_neighbor_stats", "crg_profile", "crg_measure_fma_peaks",
-    "crg_snapshot", "crg_get_stream",
+    "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc",
 ]
+NOALLOC_MAX_POINTS = 1 << 20
+NOALLOC_MAX_VOXELS = 1 << 20
 
 
 class CrgDomain(C.Structure):
@@ -111,6 +113,7 @@ def load(build_if_missing: bool = True):
     L.crg_measure_fma_peaks.argtypes = [dp, dp]
     L.crg_snapshot.argtypes = [vp, C.c_int32]
     L.crg_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.crg_cell_list_noalloc.argtypes = [C.POINTER(CrgDomain), C.c_int64, vp, vp, vp, vp, vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if name != "crg_strerror":

@@ -301,3 +301,169 @@ void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, in
 }
 
 }  // namespace crg
+
+// ---------------------------------------------------------------------------------------
+// crg_cell_list_noalloc: the cell list of caller-owned device points without allocating.
+//
+// The scratch the counting sort needs (voxel histogram, scan block sums, slot keys, status
+// word) lives in one fixed device array compiled into the library.  Host code cannot use
+// the array's name as a device address (in host code the name refers to a host-side
+// shadow), so the device address is looked up once per device with cudaGetSymbolAddress
+// and handed to the kernels.
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr uint32_t kNaMaxPoints = CRG_NOALLOC_MAX_POINTS;
+constexpr uint32_t kNaMaxVoxels = CRG_NOALLOC_MAX_VOXELS;
+constexpr size_t kNaAlign = 256;
+constexpr size_t na_round(size_t b) { return (b + kNaAlign - 1) / kNaAlign * kNaAlign; }
+constexpr size_t kNaCountOff = 0;
+constexpr size_t kNaCountBytes = na_round(sizeof(uint32_t) * ((size_t)kNaMaxVoxels + 1));
+constexpr size_t kNaBsumOff = kNaCountOff + kNaCountBytes;
+constexpr size_t kNaBsumBytes = na_round(sizeof(uint32_t) * ((size_t)kNaMaxVoxels / 4096 + 2));
+constexpr size_t kNaTmpOff = kNaBsumOff + kNaBsumBytes;
+constexpr size_t kNaTmpBytes = na_round(sizeof(uint64_t) * (size_t)kNaMaxPoints);
+constexpr size_t kNaStatusOff = kNaTmpOff + kNaTmpBytes;
+constexpr size_t kNaBytes = kNaStatusOff + na_round(sizeof(int32_t) * 4);  // 12,584,704 B
+
+// Shared by every call on a device; keeps the previous call's contents.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[kNaMaxDevices] = {};
+
+// Voxel index of every point with crg_upload's insertion rules; histogram into count.
+template <int D>
+__global__ void k_noalloc_keys(const crg::SimDev S, uint32_t n, const double *__restrict__ pos,
+                               uint32_t *__restrict__ voxel, uint32_t *count, int32_t *status) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double p[D];
+  int bad = 0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    p[a] = pos[(size_t)a * n + i];
+    if (S.min[a] >= p[a]) bad = 1;
+  }
+  uint32_t plain = 0;
+  if (!bad) {
+    const int r = crg::voxel_of<D>(S, p, plain);
+    if (r == 1) bad = 1;
+    if (r == 2) bad = 2;
+  }
+  if (bad) {
+    if (atomicCAS(&status[0], 0, bad == 1 ? CRG_EBOUNDARY : CRG_EINDEX) == 0) status[1] = (int32_t)i;
+    plain = 0;
+  }
+  voxel[i] = plain;
+  atomicAdd(&count[plain], 1u);
+}
+
+__global__ void k_noalloc_order(const uint64_t *__restrict__ tmp, uint32_t n,
+                                uint32_t *__restrict__ order) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) order[s] = (uint32_t)(tmp[s] & 0xffffffffull);
+}
+
+}  // namespace
+
+extern "C" int32_t crg_cell_list_noalloc(const crg_domain *d, int64_t n, const double *pos_dev,
+                                         uint32_t *voxel_out, uint32_t *order_out,
+                                         uint32_t *start_out, void *stream) {
+  if (!d || n < 0 || n > (int64_t)kNaMaxPoints || !start_out) return CRG_EINVAL;
+  if (n > 0 && (!pos_dev || !voxel_out || !order_out)) return CRG_EINVAL;
+  if (d->dim != 2 && d->dim != 3) return CRG_EINVAL;
+  // Grid of CartesianCuboid::from_boundaries_and_interaction_range / _and_n_voxels
+  // (cellular_raza-building-blocks/src/domains/cartesian_cuboid_n.rs:183-256).
+  crg::SimDev S;
+  memset(&S, 0, sizeof(S));
+  S.dim = d->dim;
+  S.nvox[0] = S.nvox[1] = S.nvox[2] = 1;
+  uint64_t total = 1;
+  for (int a = 0; a < d->dim; ++a) {
+    if (!(d->min[a] < d->max[a])) return CRG_EBOUNDARY;
+    S.min[a] = d->min[a];
+    S.max[a] = d->max[a];
+    uint64_t nv;
+    if (d->voxel_mode == 0) {
+      if (!(d->interaction_range > 0.0)) return CRG_EINVAL;
+      const double f = floor((d->max[a] - d->min[a]) / d->interaction_range);
+      if (!(f > -1.0 && f < 18446744073709551616.0)) return CRG_EBOUNDARY;
+      nv = (uint64_t)f < 1 ? 1 : (uint64_t)f;
+      S.dx[a] = (d->max[a] - d->min[a]) / f;
+    } else {
+      if (d->n_voxels[a] <= 0) return CRG_EINVAL;
+      nv = (uint64_t)d->n_voxels[a];
+      S.dx[a] = (d->max[a] - d->min[a]) / (double)nv;
+    }
+    if (nv > kNaMaxVoxels) return CRG_EINVAL;
+    total *= nv;
+    if (total > kNaMaxVoxels) return CRG_EINVAL;
+    S.nvox[a] = (int32_t)nv;
+  }
+  S.n_vox = (uint32_t)total;
+
+  // One-time set-up per device: the device address of the scratch array.
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return CRG_ECUDA;
+  void *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return CRG_ECUDA;
+      g_noalloc_ptr[dev] = p;
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  unsigned char *b = static_cast<unsigned char *>(base);
+  uint32_t *count = reinterpret_cast<uint32_t *>(b + kNaCountOff);
+  uint32_t *bsum = reinterpret_cast<uint32_t *>(b + kNaBsumOff);
+  uint64_t *tmp = reinterpret_cast<uint64_t *>(b + kNaTmpOff);
+  int32_t *status = reinterpret_cast<int32_t *>(b + kNaStatusOff);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint32_t un = (uint32_t)n, nvox = S.n_vox;
+
+  // The histogram and the status word must start at zero; the slot keys are fully
+  // rewritten by the scatter.
+  if (cudaMemsetAsync(count, 0, sizeof(uint32_t) * ((size_t)nvox + 1), st) != cudaSuccess ||
+      cudaMemsetAsync(status, 0, sizeof(int32_t) * 4, st) != cudaSuccess)
+    return CRG_ECUDA;
+  if (un) {
+    const unsigned grid = (un + 255) / 256;
+    if (S.dim == 3)
+      k_noalloc_keys<3><<<grid, 256, 0, st>>>(S, un, pos_dev, voxel_out, count, status);
+    else
+      k_noalloc_keys<2><<<grid, 256, 0, st>>>(S, un, pos_dev, voxel_out, count, status);
+  }
+  crg::SortArgs A;
+  memset(&A, 0, sizeof(A));
+  A.n_sims = 1;
+  A.nc = S.dim;
+  A.initial = 1;
+  A.cap = (int64_t)n;
+  A.n_agents = un;
+  A.n_vox = nvox;
+  A.nkey = voxel_out;
+  A.count = count;
+  A.start = start_out;
+  A.tmp = tmp;
+  A.status = status;
+  const uint32_t nb = (nvox + crg::kScanTile - 1) / crg::kScanTile;
+  crg::k_scan_reduce<<<nb, crg::kScanThreads, 0, st>>>(count, nvox, bsum);
+  crg::k_scan_blocks<<<1, crg::kScanThreads, 0, st>>>(bsum, nb, start_out, nvox);
+  crg::k_scan_final<<<nb, crg::kScanThreads, 0, st>>>(count, nvox, bsum, start_out);
+  if (un) crg::k_scatter<<<(un + 255) / 256, 256, 0, st>>>(A);
+  crg::k_segsort<<<(nvox + 255) / 256, 256, 0, st>>>(A);
+  if (un) k_noalloc_order<<<(un + 255) / 256, 256, 0, st>>>(tmp, un, order_out);
+  if (cudaGetLastError() != cudaSuccess) return CRG_ECUDA;
+  int32_t h_status[4] = {0, 0, 0, 0};
+  if (cudaMemcpyAsync(h_status, status, sizeof(h_status), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return CRG_ECUDA;
+  return h_status[0];
+}

@@ -173,6 +173,40 @@ int32_t crg_profile(crg_ctx *ctx, double *out3);
  * dependent-chain microbenchmark (TFLOP/s, 2 flops per FMA). */
 int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
 
+/* ---- cell list without device allocation -------------------------------------------
+ * No counterpart in the reference: chili keeps its cells in per-voxel Vecs and never
+ * builds a device cell list.
+ *
+ * Builds the voxel index and the cell list of n points that already live in device
+ * memory, using only the caller's buffers and a scratch area compiled into this library
+ * (a fixed device array of about 12.6 MB, present on every GPU that loads the library
+ * until the process exits).  It calls no cudaMalloc/cudaFree and no allocating library
+ * routine.  It is meant for callers that cannot allocate device memory at this point:
+ * a host whose device memory is owned by its own arena or pool (a Rust caller managing
+ * memory through its own allocator), a serving loop whose HBM budget is fully committed to
+ * admitted jobs, or a latency-critical loop that must not pay for cudaMalloc/cudaFree,
+ * which can synchronise the whole device.
+ *
+ *   pos_dev    device, component-major [dim][n] doubles (point i, axis a at a * n + i)
+ *   voxel_out  device [n]: voxel plain index of point i, with the insertion rules of
+ *              crg_upload (pos <= min on some axis: CRG_EBOUNDARY; outside every voxel:
+ *              CRG_EINDEX; the first offending point index is not reported)
+ *   order_out  device [n]: the point index held by each slot of the cell list (voxels
+ *              ascending, input order inside a voxel) -- the order crg_upload produces
+ *   start_out  device [n_voxels + 1]: first slot of every voxel, start_out[n_voxels] = n
+ *   stream     cudaStream_t to run on (NULL: the default stream); the call waits for it
+ *
+ * Limits: n <= CRG_NOALLOC_MAX_POINTS and n_voxels <= CRG_NOALLOC_MAX_VOXELS, otherwise
+ * CRG_EINVAL before anything runs.  All calls share the scratch array: calls that overlap
+ * on the GPU (different streams or threads at the same time) race and must be serialised
+ * by the caller.  The first call on a device looks up the scratch address on that device
+ * (cudaGetSymbolAddress); make that first call before any stream capture. */
+#define CRG_NOALLOC_MAX_POINTS (1 << 20)
+#define CRG_NOALLOC_MAX_VOXELS (1 << 20)
+int32_t crg_cell_list_noalloc(const crg_domain *domain, int64_t n, const double *pos_dev,
+                              uint32_t *voxel_out, uint32_t *order_out, uint32_t *start_out,
+                              void *stream);
+
 #ifdef __cplusplus
 }
 #endif

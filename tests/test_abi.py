@@ -26,6 +26,23 @@ def test_library_builds_and_exports_every_symbol():
         assert hasattr(lib, name), name
 
 
+def test_noalloc_limits_are_checked_before_any_device_work():
+    """crg_cell_list_noalloc rejects sizes beyond its fixed scratch on the host, before any
+    CUDA call (so this runs without a GPU)."""
+    from cellular_raza_gb300 import engine, workloads
+
+    lib = _native.load()
+    dom, _ = engine.to_c(workloads.spheres(10, 100.0, seed=1).model)
+    null = ctypes.c_void_p(0)
+    rc = lib.crg_cell_list_noalloc(ctypes.byref(dom), _native.NOALLOC_MAX_POINTS + 1, null, null,
+                                   null, null, None)
+    assert rc == _native.CRG_EINVAL
+    dom, _ = engine.to_c(workloads.spheres(10, 2000.0, seed=1).model)  # 133^3 voxels
+    rc = lib.crg_cell_list_noalloc(ctypes.byref(dom), 0, null, null, null, ctypes.c_void_p(8),
+                                   None)
+    assert rc == _native.CRG_EINVAL
+
+
 def test_status_strings_without_gpu():
     lib = _native.load()
     assert lib.crg_strerror(_native.CRG_EBOUNDARY).decode().startswith("agent outside")
