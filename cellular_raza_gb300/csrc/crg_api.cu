@@ -55,6 +55,7 @@ struct crg_ctx {
   int gexec_steps = 0;
   int graph_chunk = 32;
   int prefilter = 1;
+  int variant = 0;
   int block = 0;
   int profile = 0;
   double prof_ms[3] = {0, 0, 0};
@@ -309,6 +310,8 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
   c->cap = std::max<int64_t>(cap, 1);
   c->agent_off_h.assign(n_sims + 1, 0);
   int32_t r = allocate(c);
+  if (r == CRG_OK && c->kind == CRG_KIND_ROD && crg::prepare_rods(c->dim, c->nv) != 0)
+    r = CRG_ECUDA;
   if (r != CRG_OK) {
     free_all(c);
     delete c;
@@ -346,6 +349,7 @@ PackArgs pack_args(crg_ctx *c) {
   P.step_ctr = c->step_ctr;
   P.dbg_force = c->dbg_force;
   P.prefilter = c->prefilter;
+  P.variant = c->variant;
   return P;
 }
 
@@ -714,6 +718,10 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
       c->block = (int)value;
       break;
     case CRG_OPT_PROFILE: c->profile = value ? 1 : 0; break;
+    case CRG_OPT_KERNEL_VARIANT:
+      if (value < 0 || value > 2) return CRG_EINVAL;
+      c->variant = (int)value;
+      break;
     case CRG_OPT_DEBUG_FORCES:
       if (value && !c->dbg_force) {
         int32_t r = dalloc(&c->dbg_force, (size_t)c->cap * c->nc);

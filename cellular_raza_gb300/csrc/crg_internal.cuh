@@ -72,6 +72,7 @@ struct PackArgs {
   const int64_t *step_ctr;
   double *dbg_force;  // optional [nc][cap]: interaction force of this step
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
+  int32_t variant;    // force kernel: 0 warp-packed (default), 1 thread per agent
 };
 
 // ---- IEEE FP64 helpers that are never contracted into fused multiply-adds ----------

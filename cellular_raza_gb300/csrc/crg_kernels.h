@@ -52,6 +52,7 @@ void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, in
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st);
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
                       cudaStream_t st);
+int prepare_rods(int dim, int nv);  // 0 on success
 // Diagnostics over the current cell list.
 void launch_neighbor_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand,
                            uint32_t *n_inter, uint64_t *hash, cudaStream_t st);

@@ -166,128 +166,17 @@ __device__ __forceinline__ double norm_f64(const double *v) {
   return __dsqrt_rn(n2);
 }
 
-template <int D, int NV, int B>
-__global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
+// RodMechanics::calculate_increment (bacterial_rods.rs:157-213), the solver, apply_boundary
+// (:489-534) and the next voxel key from the centroid, for rod i with interaction force acc.
+template <int D, int NV>
+__device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, uint32_t i,
+                                           uint32_t key, const double *pa, const double *acc) {
   constexpr int NC = NV * D;
-  __shared__ double sPa[NC][B];
-  __shared__ double sT[NC][B];
-  __shared__ float sOa[NC][B];
-  __shared__ float sOb[NC][B];
-  const int tid = threadIdx.x;
-  const uint32_t i = blockIdx.x * B + tid;
-  if (i >= P.n_agents) return;
-  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
-  const SimDev &S = P.sims[sim];
   const int64_t cap = P.cap;
-  uint32_t key = P.key[i];
-  if (key - S.voxel_off >= S.n_vox) {
-    invariant_failed(P.status, kSiteForceKey, i);
-    key = S.voxel_off;
-  }
-  const uint32_t v = key - S.voxel_off;
-  int idx[D];
-  unravel<D>(S, v, idx);
-  double pa[NC];
-  float oa[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    pa[k] = P.pos[k * cap + i];
-    oa[k] = P.off[k * cap + i];
-    sPa[k][tid] = pa[k];
-    sOa[k][tid] = oa[k];
-  }
-  float amin[D], amax[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    amin[c] = oa[c];
-    amax[c] = oa[c];
-  }
-#pragma unroll
-  for (int k = D; k < NC; ++k) {
-    amin[k % D] = fminf(amin[k % D], oa[k]);
-    amax[k % D] = fmaxf(amax[k % D], oa[k]);
-  }
-  bool a_nan = false;  // fminf/fmaxf drop NaNs, so test every offset
-#pragma unroll
-  for (int k = 0; k < NC; ++k) a_nan |= !(oa[k] == oa[k]);
-  const uint32_t sub_v = subdomain_of(S, v);
-  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
-  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
-  double acc[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
-  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
-    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
-  }
-  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
-    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
-      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
-        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
-                                    : (uint32_t)j0 * S.nvox[1] + j1;
-        const bool same = (w == v);
-        const bool twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
-                           subdomain_of(S, w) != sub_v;
-        // b's offsets in a's voxel frame: off_b + (corner_b - corner_a) = off_b + (j-idx) dx
-        float kd[D];
-        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
-        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
-        if (b0 > b1 || b1 > P.n_agents) {
-          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-          b1 = b0;
-        }
-        for (uint32_t b = b0; b < b1; ++b) {
-          if (b == i) continue;
-          float ob[NC];
-          float bmin[D], bmax[D];
-#pragma unroll
-          for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            bmin[c] = ob[c];
-            bmax[c] = ob[c];
-          }
-#pragma unroll
-          for (int k = D; k < NC; ++k) {
-            bmin[k % D] = fminf(bmin[k % D], ob[k]);
-            bmax[k % D] = fmaxf(bmax[k % D], ob[k]);
-          }
-          // Bounding boxes farther apart than the threshold on one axis: all 2 x NV x (NV-1)
-          // evaluations are beyond the cutoff.  (fminf/fmaxf drop NaNs, so a NaN anywhere
-          // disables the box test.)
-          bool far = false;
-          bool b_nan = false;
-#pragma unroll
-          for (int k = 0; k < NC; ++k) b_nan |= !(ob[k] == ob[k]);
-          if (!a_nan && !b_nan) {
-#pragma unroll
-            for (int c = 0; c < D; ++c)
-              far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
-          }
-          if (far) continue;
-#pragma unroll
-          for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
-          const double *posb = P.pos + b;
-          const bool ext_first = same && (b < i);
-#pragma unroll 1
-          for (int pass = 0; pass < 2; ++pass) {
-            const bool is_ext = (pass == 0) == ext_first;
-            if (is_ext && !twice) continue;
-            if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
-              add_half<NC, B>(acc, sT, tid);
-          }
-        }
-      }
   if (P.dbg_force) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) P.dbg_force[k * cap + i] = acc[k];
   }
-
-  // RodMechanics::calculate_increment (bacterial_rods.rs:157-213).
   double va[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) va[k] = P.vel[k * cap + i];
@@ -425,6 +314,726 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   atomicAdd(&P.count[nk], 1u);
 }
 
+template <int D, int NV, int B>
+__global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
+  constexpr int NC = NV * D;
+  __shared__ double sPa[NC][B];
+  __shared__ double sT[NC][B];
+  __shared__ float sOa[NC][B];
+  __shared__ float sOb[NC][B];
+  const int tid = threadIdx.x;
+  const uint32_t i = blockIdx.x * B + tid;
+  if (i >= P.n_agents) return;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  const int64_t cap = P.cap;
+  uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  double pa[NC];
+  float oa[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    pa[k] = P.pos[k * cap + i];
+    oa[k] = P.off[k * cap + i];
+    sPa[k][tid] = pa[k];
+    sOa[k][tid] = oa[k];
+  }
+  float amin[D], amax[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    amin[c] = oa[c];
+    amax[c] = oa[c];
+  }
+#pragma unroll
+  for (int k = D; k < NC; ++k) {
+    amin[k % D] = fminf(amin[k % D], oa[k]);
+    amax[k % D] = fmaxf(amax[k % D], oa[k]);
+  }
+  bool a_nan = false;  // fminf/fmaxf drop NaNs, so test every offset
+#pragma unroll
+  for (int k = 0; k < NC; ++k) a_nan |= !(oa[k] == oa[k]);
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+  double acc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool same = (w == v);
+        const bool twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
+                           subdomain_of(S, w) != sub_v;
+        // b's offsets in a's voxel frame: off_b + (corner_b - corner_a) = off_b + (j-idx) dx
+        float kd[D];
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        if (b0 > b1 || b1 > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b1 = b0;
+        }
+        for (uint32_t b = b0; b < b1; ++b) {
+          if (b == i) continue;
+          float ob[NC];
+          float bmin[D], bmax[D];
+#pragma unroll
+          for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            bmin[c] = ob[c];
+            bmax[c] = ob[c];
+          }
+#pragma unroll
+          for (int k = D; k < NC; ++k) {
+            bmin[k % D] = fminf(bmin[k % D], ob[k]);
+            bmax[k % D] = fmaxf(bmax[k % D], ob[k]);
+          }
+          // Bounding boxes farther apart than the threshold on one axis: all 2 x NV x (NV-1)
+          // evaluations are beyond the cutoff.  (fminf/fmaxf drop NaNs, so a NaN anywhere
+          // disables the box test.)
+          bool far = false;
+          bool b_nan = false;
+#pragma unroll
+          for (int k = 0; k < NC; ++k) b_nan |= !(ob[k] == ob[k]);
+          if (!a_nan && !b_nan) {
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+              far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+          }
+          if (far) continue;
+#pragma unroll
+          for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
+          const double *posb = P.pos + b;
+          const bool ext_first = same && (b < i);
+#pragma unroll 1
+          for (int pass = 0; pass < 2; ++pass) {
+            const bool is_ext = (pass == 0) == ext_first;
+            if (is_ext && !twice) continue;
+            if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
+              add_half<NC, B>(acc, sT, tid);
+          }
+        }
+      }
+  rod_update<D, NV>(P, S, i, key, pa, acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// Warp-packed variant.  The thread-per-rod kernel above leaves most FP64 lanes idle: each
+// thread evaluates a different number of vertex/segment pairs that survive the FP32
+// prefilter.  Here lane l of a warp owns rod a_l and enumerates its surviving evaluations
+// (its "items") in exactly the order k_rods_step visits them, K at a time, into a per-lane
+// slot list in shared memory.  The whole warp then evaluates every queued item in FP64 with
+// all lanes busy, and finally each lane folds its own results into its pass accumulator M
+// and the rod force in order.  Items that end a pass carry a flush flag (acc += M / 2,
+// M = 0); a pass whose last item went out in an earlier round gets a marker item.  The
+// arithmetic per item and the summation order are those of k_rods_step, so both kernels
+// produce identical bits.
+// ---------------------------------------------------------------------------------------
+constexpr uint32_t kItFlush = 1u;    // fold M into acc after this item
+constexpr uint32_t kItMarker = 2u;   // no evaluation: flush only
+constexpr uint32_t kItExt = 4u;      // ext_a(b) item (b's vertex against a's segment)
+constexpr uint32_t kItZero = 8u;     // evaluated: force is zero (beyond cutoff or at zero distance)
+
+__device__ __forceinline__ uint64_t pack_item(uint32_t b, uint32_t flags, int vx, int sy) {
+  return ((uint64_t)b << 32) | ((uint64_t)(sy & 15) << 8) | ((uint64_t)(vx & 15) << 4) | flags;
+}
+
+template <int D, int NV, int W, int K>
+__global__ void __launch_bounds__(W * 32) k_rods_packed(const PackArgs P) {
+  constexpr int NC = NV * D, NE = NV - 1, NS = NV * NE;
+  __shared__ uint64_t sItem[W][K][32];
+  __shared__ double sRes[W][K][2 * D][32];
+  __shared__ double sM[W][NC][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t warp_base = (blockIdx.x * W + wid) * 32;
+  const uint32_t i = warp_base + lane;
+  const bool valid = i < P.n_agents;
+  const int64_t cap = P.cap;
+  const uint32_t ii = valid ? i : 0u;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
+  const SimDev &S = P.sims[sim];
+  uint32_t key = P.key[ii];
+  if (key - S.voxel_off >= S.n_vox) {
+    if (valid) invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  float amin[D], amax[D];
+  bool a_nan = false;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const float o = P.off[k * cap + ii];
+    a_nan |= !(o == o);
+    if (k < D) {
+      amin[k] = o;
+      amax[k] = o;
+    } else {
+      amin[k % D] = fminf(amin[k % D], o);
+      amax[k % D] = fmaxf(amax[k % D], o);
+    }
+  }
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+#pragma unroll
+  for (int k = 0; k < NC; ++k) sM[wid][k][lane] = 0.0;
+  double acc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+
+  // neighbourhood box (ascending plain index = j0 outer, last axis inner)
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+    nb[c] = hi - lo[c] + 1;
+  }
+  const int n_box = nb[0] * nb[1] * nb[2];
+  // enumeration cursor
+  bool done = !valid;
+  int stage = 0;  // 0: next voxel, 1: next candidate, 2: inside a pass
+  int o_box = 0;
+  uint32_t b_next = 0, b_end = 0, cur_b = 0;
+  bool same = false, twice = false, ext_first = false, pending_flush = false;
+  int pass = 0, vs = 0, pass_items = 0;
+  float kd[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) kd[c] = 0.f;
+
+  while (__any_sync(0xffffffffu, !done || pending_flush)) {
+    // ---- 1. enumerate up to K items -------------------------------------------------
+    int cnt = 0;
+    int pass_items_round = 0;
+    if (pending_flush) {
+      sItem[wid][cnt++][lane] = pack_item(0, kItMarker, 0, 0);
+      pending_flush = false;
+    }
+    while (!done && cnt < K) {
+      if (stage == 0) {
+        if (o_box >= n_box) {
+          done = true;
+          break;
+        }
+        const int j2 = lo[2] + o_box % nb[2];
+        const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
+        const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
+        ++o_box;
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        same = (w == v);
+        twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        b_next = P.start[S.voxel_off + w];
+        b_end = P.start[S.voxel_off + w + 1];
+        if (b_next > b_end || b_end > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b_end = b_next;
+        }
+        stage = 1;
+        continue;
+      }
+      if (stage == 1) {
+        if (b_next >= b_end) {
+          stage = 0;
+          continue;
+        }
+        const uint32_t b = b_next++;
+        if (b == i) continue;
+        float bmin[D], bmax[D];
+        bool b_nan = false;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+          const float o = P.off[k * cap + b] + kd[k % D];
+          b_nan |= !(o == o);
+          if (k < D) {
+            bmin[k] = o;
+            bmax[k] = o;
+          } else {
+            bmin[k % D] = fminf(bmin[k % D], o);
+            bmax[k % D] = fmaxf(bmax[k % D], o);
+          }
+        }
+        bool far = false;
+        if (!a_nan && !b_nan) {
+#pragma unroll
+          for (int c = 0; c < D; ++c)
+            far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+        }
+        if (far) continue;
+        cur_b = b;
+        ext_first = same && (b < i);
+        pass = 0;
+        vs = 0;
+        pass_items = 0;
+        pass_items_round = 0;
+        stage = 2;
+        continue;
+      }
+      // stage 2: scan the (vertex, segment) pairs of the current pass
+      const bool is_ext = (pass == 0) == ext_first;
+      if (is_ext && !twice) vs = NS;
+      while (vs < NS && cnt < K) {
+        const int vx = vs / NE, sy = vs - (vs / NE) * NE;
+        ++vs;
+        const uint32_t pr = is_ext ? cur_b : i;  // owner of the point
+        const uint32_t sr = is_ext ? i : cur_b;  // owner of the segment
+        const float pk = is_ext ? 1.f : 0.f;     // which side carries the corner shift
+        float p32[D], l0[D], l1[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          p32[c] = P.off[(vx * D + c) * cap + pr] + pk * kd[c];
+          l0[c] = P.off[(sy * D + c) * cap + sr] + (1.f - pk) * kd[c];
+          l1[c] = P.off[((sy + 1) * D + c) * cap + sr] + (1.f - pk) * kd[c];
+        }
+        if (seg_dist2_f32<D>(p32, l0, l1) > thr2) continue;
+        sItem[wid][cnt++][lane] = pack_item(cur_b, is_ext ? kItExt : 0u, vx, sy);
+        ++pass_items;
+        ++pass_items_round;
+      }
+      if (vs >= NS) {
+        if (pass_items > 0) {
+          if (pass_items_round > 0)
+            sItem[wid][cnt - 1][lane] |= kItFlush;
+          else if (cnt < K)
+            sItem[wid][cnt++][lane] = pack_item(0, kItMarker, 0, 0);
+          else
+            pending_flush = true;
+        }
+        ++pass;
+        vs = 0;
+        pass_items = 0;
+        pass_items_round = 0;
+        if (pass == 2) stage = 1;
+        if (pending_flush) break;
+      }
+    }
+    __syncwarp();
+
+    // ---- 2. evaluate every queued item with the whole warp ---------------------------
+    int incl = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
+    }
+    const int excl = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int base = 0; base < total; base += 32) {
+      const int j = base + lane;
+      // owner lane: the largest l with excl_l <= j
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+        if (cand < 32 && e <= j) l = cand;
+      }
+      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);  // parameters of the owner
+      if (j < total) {
+        const SimDev &So = P.sims[sim_l];
+        const int k = j - ex_l;
+        const uint64_t it = sItem[wid][k][l];
+        const uint32_t fl = (uint32_t)it & 15u;
+        if (!(fl & kItMarker)) {
+          const uint32_t b = (uint32_t)(it >> 32);
+          const uint32_t a = warp_base + l;
+          const int vx = (int)((it >> 4) & 15), sy = (int)((it >> 8) & 15);
+          const bool is_ext = fl & kItExt;
+          const uint32_t pr = is_ext ? b : a, sr = is_ext ? a : b;
+          double p[D], l0[D], l1[D], q[D], t, f[D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            p[c] = P.pos[(vx * D + c) * cap + pr];
+            l0[c] = P.pos[(sy * D + c) * cap + sr];
+            l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
+          }
+          nearest_point_f64<D>(p, l0, l1, q, t);
+          if (morse_full_f64<D>(p, q, So, f)) {
+            if (!is_ext) {
+#pragma unroll
+              for (int c = 0; c < D; ++c) sRes[wid][k][c][l] = f[c];
+            } else {
+              const double omt = dsub(1.0, t);
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const double fe = -f[c];
+                sRes[wid][k][c][l] = dmul(fe, omt);
+                sRes[wid][k][D + c][l] = dmul(fe, t);
+              }
+            }
+          } else {
+            sItem[wid][k][l] = it | kItZero;
+          }
+        }
+      }
+    }
+    __syncwarp();
+
+    // ---- 3. each lane folds its results in order ------------------------------------
+    for (int k = 0; k < cnt; ++k) {
+      const uint64_t it = sItem[wid][k][lane];
+      const uint32_t fl = (uint32_t)it & 15u;
+      if (!(fl & (kItMarker | kItZero))) {
+        const int vx = (int)((it >> 4) & 15), sy = (int)((it >> 8) & 15);
+        if (!(fl & kItExt)) {
+#pragma unroll
+          for (int c = 0; c < D; ++c)
+            sM[wid][vx * D + c][lane] = dadd(sM[wid][vx * D + c][lane], sRes[wid][k][c][lane]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            sM[wid][sy * D + c][lane] = dadd(sM[wid][sy * D + c][lane], sRes[wid][k][c][lane]);
+            sM[wid][(sy + 1) * D + c][lane] =
+                dadd(sM[wid][(sy + 1) * D + c][lane], sRes[wid][k][D + c][lane]);
+          }
+        }
+      }
+      if (fl & (kItFlush | kItMarker)) {
+#pragma unroll
+        for (int q = 0; q < NC; ++q) {
+          acc[q] = dadd(acc[q], dmul(sM[wid][q][lane], 0.5));
+          sM[wid][q][lane] = 0.0;
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (!valid) return;
+  double pa[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
+  rod_update<D, NV>(P, S, i, key, pa, acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass-synchronous variant (default).  Each round every lane of the warp handles exactly one
+// pass -- own_a(b) or ext_a(b) for its next candidate rod b -- so the scan of the
+// NV x (NV-1) vertex/segment pairs is a uniform loop that records the FP32 survivors in a
+// bitmask; the warp then evaluates all survivors of all lanes in FP64 with every lane busy
+// (results to shared memory), and each lane folds its results into the pass matrix M in
+// (vertex, segment) order with compile-time indices and adds M / 2 to the rod force.
+// Same items, same per-item arithmetic, same order as k_rods_step: identical bits.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int nth_set_bit64(uint64_t m, int n) {  // n-th set bit (0-based)
+  const uint32_t lo = (uint32_t)m;
+  const int clo = __popc(lo);
+  if (n < clo) return (int)__fns(lo, 0, n + 1);
+  return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - clo + 1);
+}
+
+template <int D, int NV>
+__global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
+  constexpr int NC = NV * D, NE = NV - 1, NP = NV * NE, R = D + 1;
+  extern __shared__ double sRes[];  // [NP][R][32]: f (and t for ext items), then sRow
+  double *sRow = sRes + NP * R * 32;  // [NV][D][32]: folded rows of the pass matrix
+  const int lane = threadIdx.x;
+  const uint32_t warp_base = blockIdx.x * 32;
+  const uint32_t i = warp_base + lane;
+  const bool valid = i < P.n_agents;
+  const int64_t cap = P.cap;
+  const uint32_t ii = valid ? i : 0u;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
+  const SimDev &S = P.sims[sim];
+  uint32_t key = P.key[ii];
+  if (key - S.voxel_off >= S.n_vox) {
+    if (valid) invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  float oa[NC];
+  float amin[D], amax[D];
+  bool a_nan = false;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    oa[k] = P.off[k * cap + ii];
+    a_nan |= !(oa[k] == oa[k]);
+    if (k < D) {
+      amin[k] = oa[k];
+      amax[k] = oa[k];
+    } else {
+      amin[k % D] = fminf(amin[k % D], oa[k]);
+      amax[k % D] = fmaxf(amax[k % D], oa[k]);
+    }
+  }
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+  double acc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+    nb[c] = hi - lo[c] + 1;
+  }
+  const int n_box = nb[0] * nb[1] * nb[2];
+  // cursor
+  bool done = !valid;
+  int o_box = 0;
+  uint32_t b_next = 0, b_end = 0, cur_b = 0;
+  bool same = false, twice = false, ext_first = false;
+  int n_pass = 0, pass = 0;  // passes of the current candidate / index of the next one
+  float kd[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) kd[c] = 0.f;
+
+  while (__any_sync(0xffffffffu, !done)) {
+    // ---- next pass of this lane: advance to the next non-far candidate if needed -------
+    while (!done && pass >= n_pass) {
+      if (b_next >= b_end) {
+        if (o_box >= n_box) {
+          done = true;
+          break;
+        }
+        const int j2 = lo[2] + o_box % nb[2];
+        const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
+        const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
+        ++o_box;
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        same = (w == v);
+        twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        b_next = P.start[S.voxel_off + w];
+        b_end = P.start[S.voxel_off + w + 1];
+        if (b_next > b_end || b_end > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b_end = b_next;
+        }
+        continue;
+      }
+      const uint32_t b = b_next++;
+      if (b == i) continue;
+      float bmin[D], bmax[D];
+      bool b_nan = false;
+#pragma unroll
+      for (int k = 0; k < NC; ++k) {
+        const float o = P.off[k * cap + b] + kd[k % D];
+        b_nan |= !(o == o);
+        if (k < D) {
+          bmin[k] = o;
+          bmax[k] = o;
+        } else {
+          bmin[k % D] = fminf(bmin[k % D], o);
+          bmax[k % D] = fmaxf(bmax[k % D], o);
+        }
+      }
+      bool far = false;
+      if (!a_nan && !b_nan) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+      }
+      if (far) continue;
+      cur_b = b;
+      ext_first = same && (b < i);
+      n_pass = twice ? 2 : 1;
+      pass = 0;
+    }
+    const bool active = !done;
+    const bool is_ext = active && ((pass == 0) == ext_first);
+    ++pass;
+
+    // ---- scan the vertex/segment pairs of this pass (uniform loop) -------------------
+    uint64_t mask = 0;
+    if (active) {
+      float ob[NC];
+#pragma unroll
+      for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + cur_b] + kd[k % D];
+#pragma unroll
+      for (int vx = 0; vx < NV; ++vx)
+#pragma unroll
+        for (int sy = 0; sy < NE; ++sy) {
+          const float *pp = is_ext ? &ob[vx * D] : &oa[vx * D];
+          const float *s0 = is_ext ? &oa[sy * D] : &ob[sy * D];
+          const float *s1 = is_ext ? &oa[(sy + 1) * D] : &ob[(sy + 1) * D];
+          float p32[D], l0[D], l1[D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            p32[c] = pp[c];
+            l0[c] = s0[c];
+            l1[c] = s1[c];
+          }
+          if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
+        }
+    }
+    const int cnt = __popcll(mask);
+
+    // ---- evaluate every survivor of the warp in FP64 ---------------------------------
+    int incl = cnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
+    }
+    const int excl = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    for (int base = 0; base < total; base += 32) {
+      const int j = base + lane;
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+        if (cand < 32 && e <= j) l = cand;
+      }
+      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
+      const uint32_t b_l = __shfl_sync(0xffffffffu, cur_b, l);
+      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
+      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
+      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+      if (j < total) {
+        const int k = j - ex_l;
+        const int vs = nth_set_bit64(((uint64_t)mhi << 32) | mlo, k);
+        const int vx = vs / NE, sy = vs - vx * NE;
+        const uint32_t a = warp_base + l;
+        const uint32_t pr = ext_l ? b_l : a, sr = ext_l ? a : b_l;
+        double p[D], l0[D], l1[D], q[D], t, f[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          p[c] = P.pos[(vx * D + c) * cap + pr];
+          l0[c] = P.pos[(sy * D + c) * cap + sr];
+          l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
+        }
+        nearest_point_f64<D>(p, l0, l1, q, t);
+        if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
+#pragma unroll
+          for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) sRes[(k * R + c) * 32 + l] = f[c];
+        sRes[(k * R + D) * 32 + l] = t;
+      }
+    }
+    __syncwarp();
+
+    // ---- fold the results row by row: each non-empty (rod, row) is one unit ----------
+    // Row r of the pass matrix M collects, in the reference's (vertex, segment) order,
+    //   own pass: f of items (r, 0..NE-1);
+    //   ext pass: for each vertex vx, -f*t of item (vx, r-1) then -f*(1-t) of item (vx, r).
+    uint32_t rowmask = 0;
+#pragma unroll
+    for (int r = 0; r < NV; ++r) {
+      bool has = false;
+      if (!is_ext) {
+        has = ((mask >> (r * NE)) & ((1ull << NE) - 1ull)) != 0ull;
+      } else {
+#pragma unroll
+        for (int vx = 0; vx < NV; ++vx) {
+          if (r >= 1) has |= ((mask >> (vx * NE + r - 1)) & 1ull) != 0ull;
+          if (r < NE) has |= ((mask >> (vx * NE + r)) & 1ull) != 0ull;
+        }
+      }
+      if (has) rowmask |= 1u << r;
+    }
+    const int rcnt = __popc(rowmask);
+    int rincl = rcnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, rincl, off);
+      if (lane >= off) rincl += y;
+    }
+    const int rexcl = rincl - rcnt;
+    const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
+    for (int base = 0; base < rtotal; base += 32) {
+      const int j = base + lane;
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int e = __shfl_sync(0xffffffffu, rexcl, cand & 31);
+        if (cand < 32 && e <= j) l = cand;
+      }
+      const int ex_l = __shfl_sync(0xffffffffu, rexcl, l);
+      const uint32_t rows_l = __shfl_sync(0xffffffffu, rowmask, l);
+      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
+      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
+      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+      if (j < rtotal) {
+        const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
+        const int r = (int)__fns(rows_l, 0, j - ex_l + 1);
+        double m[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) m[c] = 0.0;
+        if (!ext_l) {
+#pragma unroll
+          for (int sy = 0; sy < NE; ++sy) {
+            const int vs = r * NE + sy;
+            if (!((m_l >> vs) & 1ull)) continue;
+            const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
+#pragma unroll
+            for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(slot * R + c) * 32 + l]);
+          }
+        } else {
+#pragma unroll
+          for (int vx = 0; vx < NV; ++vx) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int sy = r - 1 + h;  // h = 0: item (vx, r-1) weight t; h = 1: (vx, r) weight 1-t
+              if (sy < 0 || sy >= NE) continue;
+              const int vs = vx * NE + sy;
+              if (!((m_l >> vs) & 1ull)) continue;
+              const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
+              const double t = sRes[(slot * R + D) * 32 + l];
+              const double wgt = h == 0 ? t : dsub(1.0, t);
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const double fe = -sRes[(slot * R + c) * 32 + l];
+                m[c] = dadd(m[c], dmul(fe, wgt));
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) sRow[(r * D + c) * 32 + l] = m[c];
+      }
+    }
+    __syncwarp();
+    // acc += M / 2 for the rows this lane's pass touched (other rows of M are zero)
+#pragma unroll
+    for (int r = 0; r < NV; ++r)
+      if ((rowmask >> r) & 1u) {
+#pragma unroll
+        for (int c = 0; c < D; ++c)
+          acc[r * D + c] = dadd(acc[r * D + c], dmul(sRow[(r * D + c) * 32 + lane], 0.5));
+      }
+    __syncwarp();
+  }
+  if (!valid) return;
+  double pa[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
+  rod_update<D, NV>(P, S, i, key, pa, acc);
+}
+
 // Candidate rods of the current cell list, a hash of their ids and the number of in-range
 // vertex/segment evaluations of a.calc(a, b) (own perspective, FP64, no prefilter).
 template <int D, int NV>
@@ -475,11 +1084,47 @@ __global__ void k_rod_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_inte
 }
 
 template <int D, int NV>
+constexpr size_t pass_smem_bytes() {
+  return sizeof(double) * ((size_t)(NV * (NV - 1)) * (D + 1) + (size_t)NV * D) * 32;
+}
+
+template <int D, int NV>
 void launch_t(const PackArgs &P, int block, cudaStream_t st) {
   (void)block;
-  constexpr int B = 64;
-  const unsigned grid = (P.n_agents + B - 1) / B;
-  k_rods_step<D, NV, B><<<grid, B, 0, st>>>(P);
+  if (P.variant == 1) {  // thread-per-rod kernel
+    constexpr int B = 64;
+    const unsigned grid = (P.n_agents + B - 1) / B;
+    k_rods_step<D, NV, B><<<grid, B, 0, st>>>(P);
+    return;
+  }
+  if (P.variant == 2) {  // slot-queue kernel
+    constexpr int W = 2, K = 8;
+    const unsigned grid = (P.n_agents + W * 32 - 1) / (W * 32);
+    k_rods_packed<D, NV, W, K><<<grid, W * 32, 0, st>>>(P);
+    return;
+  }
+  const unsigned grid = (P.n_agents + 31) / 32;
+  k_rods_pass<D, NV><<<grid, 32, pass_smem_bytes<D, NV>(), st>>>(P);
+}
+
+template <int D, int NV>
+cudaError_t prepare_t() {
+  return cudaFuncSetAttribute(k_rods_pass<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)pass_smem_bytes<D, NV>());
+}
+
+template <int D>
+cudaError_t prepare_d(int nv) {
+  switch (nv) {
+    case 2: return prepare_t<D, 2>();
+    case 3: return prepare_t<D, 3>();
+    case 4: return prepare_t<D, 4>();
+    case 5: return prepare_t<D, 5>();
+    case 6: return prepare_t<D, 6>();
+    case 7: return prepare_t<D, 7>();
+    case 8: return prepare_t<D, 8>();
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <int D>
@@ -497,6 +1142,11 @@ void launch_d(int nv, const PackArgs &P, int block, cudaStream_t st) {
 }
 
 }  // namespace
+
+// Kernel attributes that must be set outside any stream capture (once per handle).
+int prepare_rods(int dim, int nv) {
+  return (dim == 3 ? prepare_d<3>(nv) : prepare_d<2>(nv)) == cudaSuccess ? 0 : -1;
+}
 
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
                       cudaStream_t st) {

@@ -37,6 +37,99 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
   s = t;
 }
 
+// NewtonDamped increment, solver, boundary and next voxel key of agent i with interaction
+// force acc (shared by the force kernels).
+template <int D>
+__device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S, uint32_t i,
+                                              uint32_t key, const double *pa,
+                                              const double *va, const double *acc) {
+  const int64_t cap = P.cap;
+  if (P.dbg_force) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) P.dbg_force[c * cap + i] = acc[c];
+  }
+
+  // NewtonDamped::calculate_increment (mechanics.rs:166-173): dx = v, dv = F/m - lambda v.
+  double dxv[D], dvv[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    dxv[c] = va[c];
+    dvv[c] = dsub(ddiv(acc[c], S.mass), dmul(S.damping, va[c]));
+  }
+  // Solvers (chili/solvers.rs:23-55, 156-347).  The random contribution is zero
+  // (mechanics.rs:158-164), so the final `.xapy(1, dx_rand * dt)` adds +0.
+  double np[D], nvl[D];
+  const double dt = S.dt;
+  uint8_t meta = 0;
+  if (S.order == 1) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      np[c] = dadd(dadd(dmul(dxv[c], dt), pa[c]), 0.0);
+      nvl[c] = dadd(dadd(dmul(dvv[c], dt), va[c]), 0.0);
+    }
+  } else {
+    // The history is pushed before it is read (solvers.rs:178-185), so the newest stored
+    // increment is the current one: AB2 uses [dx, dx]; AB3 uses [dx, dx] on its first step
+    // and [dx, previous, dx] afterwards.
+    const uint8_t have_prev = P.hmeta[i];
+    const bool ab3 = (S.order == 3) && have_prev;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      if (ab3) {
+        const double f0 = 23.0 / 12.0, f1 = -16.0 / 12.0, f2 = 5.0 / 12.0;
+        const double px = P.hist[c * cap + i], pv = P.hist[(D + c) * cap + i];
+        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dadd(dmul(px, f1), dmul(dxv[c], f2))), dt),
+                          pa[c]), 0.0);
+        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dadd(dmul(pv, f1), dmul(dvv[c], f2))), dt),
+                           va[c]), 0.0);
+      } else {
+        const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
+        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dmul(dxv[c], f1)), dt), pa[c]), 0.0);
+        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dmul(dvv[c], f1)), dt), va[c]), 0.0);
+      }
+      P.nhist[c * cap + i] = dxv[c];
+      P.nhist[(D + c) * cap + i] = dvv[c];
+    }
+    meta = 1;
+    P.nhmeta[i] = meta;
+  }
+
+  // CartesianSubDomain::apply_boundary (cartesian_cuboid_n.rs:594-631).
+  bool inside = true;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    if (np[c] < S.min[c]) {
+      np[c] = dsub(dmul(2.0, S.min[c]), np[c]);
+      nvl[c] = fabs(nvl[c]);
+    }
+    if (np[c] > S.max[c]) {
+      np[c] = dsub(dmul(2.0, S.max[c]), np[c]);
+      nvl[c] = -fabs(nvl[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c)
+    if (np[c] < S.min[c] || np[c] > S.max[c]) inside = false;
+  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1);
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    P.npos[c * cap + i] = np[c];
+    P.nvel[c * cap + i] = nvl[c];
+  }
+  // sort_cells_in_voxels_step_1 (update_mechanics.rs:427-456): a failed or out-of-grid
+  // index leaves the agent in its voxel.
+  uint32_t plain;
+  uint32_t nk = key;
+  if (voxel_of<D>(S, np, plain) == 0) nk = S.voxel_off + plain;
+  if (nk - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteNextKey, i);
+    nk = key;
+  }
+  P.nkey[i] = nk;
+  P.nid[i] = P.id[i];
+  atomicAdd(&P.count[nk], 1u);
+}
+
 template <int D, int PREC>
 __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -139,90 +232,163 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
 #pragma unroll
     for (int c = 0; c < D; ++c) acc[c] = (double)fs[c] - (double)fcmp[c];
   }
-  if (P.dbg_force) {
-#pragma unroll
-    for (int c = 0; c < D; ++c) P.dbg_force[c * cap + i] = acc[c];
-  }
+  sphere_update<D>(P, S, i, key, pa, va, acc);
+}
 
-  // NewtonDamped::calculate_increment (mechanics.rs:166-173): dx = v, dv = F/m - lambda v.
-  double dxv[D], dvv[D];
+// ---------------------------------------------------------------------------------------
+// Warp-packed FP64 variant (default for the FP64 path).  Lane l owns agent a_l.  Each round
+// every lane scans the next G positions of its candidate stream (neighbour voxels ascending,
+// cell-list order inside a voxel, itself skipped) through the FP32 prefilter and records the
+// survivors; the warp evaluates all survivors of all lanes in FP64 with every lane busy
+// (half-forces to shared memory); then each lane adds its half-forces in stream order, twice
+// for a partner whose pair weight is 1.  Same terms, same order as k_spheres_step.
+// ---------------------------------------------------------------------------------------
+template <int D, int G>
+__global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
+  extern __shared__ double sH[];                      // [G][D][32] half-forces
+  uint32_t *sB = reinterpret_cast<uint32_t *>(sH + G * D * 32);  // [G][32] partner index
+  const int lane = threadIdx.x;
+  const uint32_t warp_base = blockIdx.x * 32;
+  const uint32_t i = warp_base + lane;
+  const bool valid = i < P.n_agents;
+  const int64_t cap = P.cap;
+  const uint32_t ii = valid ? i : 0u;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
+  const SimDev &S = P.sims[sim];
+  uint32_t key = P.key[ii];
+  if (key - S.voxel_off >= S.n_vox) {
+    if (valid) invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  double pa[D], va[D];
+  float oa[D];
 #pragma unroll
   for (int c = 0; c < D; ++c) {
-    dxv[c] = va[c];
-    dvv[c] = dsub(ddiv(acc[c], S.mass), dmul(S.damping, va[c]));
+    pa[c] = P.pos[c * cap + ii];
+    va[c] = P.vel[c * cap + ii];
+    oa[c] = P.off[c * cap + ii];
   }
-  // Solvers (chili/solvers.rs:23-55, 156-347).  The random contribution is zero
-  // (mechanics.rs:158-164), so the final `.xapy(1, dx_rand * dt)` adds +0.
-  double np[D], nvl[D];
-  const double dt = S.dt;
-  uint8_t meta = 0;
-  if (S.order == 1) {
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-      np[c] = dadd(dadd(dmul(dxv[c], dt), pa[c]), 0.0);
-      nvl[c] = dadd(dadd(dmul(dvv[c], dt), va[c]), 0.0);
-    }
-  } else {
-    // The history is pushed before it is read (solvers.rs:178-185), so the newest stored
-    // increment is the current one: AB2 uses [dx, dx]; AB3 uses [dx, dx] on its first step
-    // and [dx, previous, dx] afterwards.
-    const uint8_t have_prev = P.hmeta[i];
-    const bool ab3 = (S.order == 3) && have_prev;
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+    nb[c] = hi - lo[c] + 1;
+  }
+  const int n_box = nb[0] * nb[1] * nb[2];
+  bool done = !valid;
+  int o_box = 0;
+  uint32_t b_next = 0, b_end = 0;
+  bool twice = false;
+  float kd[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-      if (ab3) {
-        const double f0 = 23.0 / 12.0, f1 = -16.0 / 12.0, f2 = 5.0 / 12.0;
-        const double px = P.hist[c * cap + i], pv = P.hist[(D + c) * cap + i];
-        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dadd(dmul(px, f1), dmul(dxv[c], f2))), dt),
-                          pa[c]), 0.0);
-        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dadd(dmul(pv, f1), dmul(dvv[c], f2))), dt),
-                           va[c]), 0.0);
-      } else {
-        const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
-        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dmul(dxv[c], f1)), dt), pa[c]), 0.0);
-        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dmul(dvv[c], f1)), dt), va[c]), 0.0);
+  for (int c = 0; c < D; ++c) kd[c] = 0.f;
+  double acc[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) acc[c] = 0.0;
+
+  while (__any_sync(0xffffffffu, !done)) {
+    // ---- scan the next G stream positions ------------------------------------------
+    int cnt = 0;
+    uint32_t twice_mask = 0;
+    int g = 0;
+    while (!done && g < G) {
+      if (b_next >= b_end) {
+        if (o_box >= n_box) {
+          done = true;
+          break;
+        }
+        const int j2 = lo[2] + o_box % nb[2];
+        const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
+        const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
+        ++o_box;
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        b_next = P.start[S.voxel_off + w];
+        b_end = P.start[S.voxel_off + w + 1];
+        if (b_next > b_end || b_end > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b_end = b_next;
+        }
+        continue;
       }
-      P.nhist[c * cap + i] = dxv[c];
-      P.nhist[(D + c) * cap + i] = dvv[c];
+      const uint32_t b = b_next++;
+      ++g;
+      if (b == i) continue;
+      float d2 = 0.0f;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const float z = (oa[c] - P.off[c * cap + b]) - kd[c];
+        d2 = fmaf(z, z, d2);
+      }
+      if (d2 > thr2) continue;  // NaN falls through to the exact path
+      sB[cnt * 32 + lane] = b;
+      if (twice) twice_mask |= 1u << cnt;
+      ++cnt;
     }
-    meta = 1;
-    P.nhmeta[i] = meta;
-  }
 
-  // CartesianSubDomain::apply_boundary (cartesian_cuboid_n.rs:594-631).
-  bool inside = true;
+    // ---- evaluate every survivor of the warp in FP64 ---------------------------------
+    int incl = cnt;
 #pragma unroll
-  for (int c = 0; c < D; ++c) {
-    if (np[c] < S.min[c]) {
-      np[c] = dsub(dmul(2.0, S.min[c]), np[c]);
-      nvl[c] = fabs(nvl[c]);
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
     }
-    if (np[c] > S.max[c]) {
-      np[c] = dsub(dmul(2.0, S.max[c]), np[c]);
-      nvl[c] = -fabs(nvl[c]);
+    const int excl = incl - cnt;
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (int base = 0; base < total; base += 32) {
+      const int j = base + lane;
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+        if (cand < 32 && e <= j) l = cand;
+      }
+      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
+      if (j < total) {
+        const int k = j - ex_l;
+        const uint32_t b = sB[k * 32 + l];
+        const uint32_t a = warp_base + l;
+        const SimDev &So = P.sims[sim_l];
+        double z[D], h[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + a], P.pos[c * cap + b]);
+        if (!morse_half_f64<D>(z, So, So.radius, h)) {
+#pragma unroll
+          for (int c = 0; c < D; ++c) h[c] = 0.0;  // adding +0 leaves the sum unchanged
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) sH[(k * D + c) * 32 + l] = h[c];
+      }
     }
-  }
+    __syncwarp();
+
+    // ---- add this lane's half-forces in stream order ---------------------------------
+    for (int k = 0; k < cnt; ++k) {
+      const bool tw = (twice_mask >> k) & 1u;
 #pragma unroll
-  for (int c = 0; c < D; ++c)
-    if (np[c] < S.min[c] || np[c] > S.max[c]) inside = false;
-  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1);
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    P.npos[c * cap + i] = np[c];
-    P.nvel[c * cap + i] = nvl[c];
+      for (int c = 0; c < D; ++c) {
+        const double h = sH[(k * D + c) * 32 + lane];
+        acc[c] = dadd(acc[c], h);
+        if (tw) acc[c] = dadd(acc[c], h);
+      }
+    }
+    __syncwarp();
   }
-  // sort_cells_in_voxels_step_1 (update_mechanics.rs:427-456): a failed or out-of-grid
-  // index leaves the agent in its voxel.
-  uint32_t plain;
-  uint32_t nk = key;
-  if (voxel_of<D>(S, np, plain) == 0) nk = S.voxel_off + plain;
-  if (nk - S.voxel_off >= S.n_vox) {
-    invariant_failed(P.status, kSiteNextKey, i);
-    nk = key;
-  }
-  P.nkey[i] = nk;
-  P.nid[i] = P.id[i];
-  atomicAdd(&P.count[nk], 1u);
+  if (!valid) return;
+  sphere_update<D>(P, S, i, key, pa, va, acc);
 }
 
 template <int D>
@@ -267,8 +433,22 @@ __global__ void k_sphere_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_i
 
 }  // namespace
 
+constexpr int kSphereG = 32;
+template <int D>
+constexpr size_t sphere_pass_smem() {
+  return sizeof(double) * kSphereG * D * 32 + sizeof(uint32_t) * kSphereG * 32;
+}
+
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st) {
   if (!P.n_agents) return;
+  if (precision == CRG_PREC_F64 && P.variant != 1) {
+    const unsigned grid = (P.n_agents + 31) / 32;
+    if (dim == 3)
+      k_spheres_pass<3, kSphereG><<<grid, 32, sphere_pass_smem<3>(), st>>>(P);
+    else
+      k_spheres_pass<2, kSphereG><<<grid, 32, sphere_pass_smem<2>(), st>>>(P);
+    return;
+  }
   if (block <= 0 || block > 256) block = 128;
   const unsigned grid = (P.n_agents + block - 1) / block;
   if (dim == 3) {
