@@ -44,6 +44,8 @@ def parse():
     p.add_argument("--workload", default="rods_2d", choices=["rods_2d", "spheres_3d"])
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the mixed-precision, ensemble and served measurements")
     return p.parse_args()
 
 
@@ -215,6 +217,120 @@ def algorithmic_flops(w, stats):
     return 30.0 * n_inter + 21.0 * w.n
 
 
+def timed_run(torch, sim, steps, restore=True):
+    """Device time (ms) of `steps` steps of a handle, CUDA events on its stream."""
+    ext = torch.cuda.ExternalStream(sim.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if restore:
+        sim.snapshot(restore=True)
+    torch.cuda.synchronize()
+    e0.record(ext)
+    sim.step(steps)
+    e1.record(ext)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def extra_mixed_large(torch):
+    """2^23 spheres at the density of spheres_3d, 200 steps: mixed precision against the FP64
+    path (throughput and the relative position error of mixed against FP64)."""
+    import numpy as np
+    from cellular_raza_gb300 import engine as E
+    from cellular_raza_gb300 import workloads as W
+
+    w = W.spheres_3d_large(seed=2024)
+    out = {"workload": "spheres_3d_large", "agents": w.n, "steps": w.n_steps}
+    finals = {}
+    for prec in ("mixed", "f64"):
+        sim = E.Simulation.single(w.model.replace(precision=prec), w.n)
+        sim.upload(w.pos, w.vel)
+        sim.snapshot()
+        sim.step(3)  # warm-up (graph instantiation)
+        ms = timed_run(torch, sim, w.n_steps)
+        out[f"{prec}_agent_steps_per_s"] = w.n * w.n_steps / (ms / 1e3)
+        out[f"{prec}_ms_per_step"] = ms / w.n_steps
+        finals[prec] = sim.download(order="id")["pos"]
+        sim.close()
+    a, b = finals["f64"], finals["mixed"]
+    err = np.linalg.norm(b - a, axis=-1) / np.linalg.norm(a, axis=-1)
+    out["speedup_mixed_over_f64"] = out["mixed_agent_steps_per_s"] / out["f64_agent_steps_per_s"]
+    out["max_rel_pos_err"] = float(err.max())
+    out["mean_rel_pos_err"] = float(err.mean())
+    return out
+
+
+def extra_ensemble(torch):
+    """1,024 independent 3D Morse simulations (log-uniform sizes, varied strength/damping),
+    mixed precision, packed into the same launches (graph-captured step loop, autotuned force
+    kernel shape), 500 steps; against sequential plain FP64 runs timed on a stratified
+    sample of 24 of the simulations and scaled to all 1,024."""
+    import numpy as np
+    from cellular_raza_gb300 import engine as E
+    from cellular_raza_gb300 import workloads as W
+
+    ws = W.ensemble(seed=2024)
+    steps = ws[0].n_steps
+    n_total = sum(w.n for w in ws)
+    sim = E.Simulation([w.model for w in ws], [w.n for w in ws])
+    sim.upload(np.concatenate([w.pos for w in ws]), np.concatenate([w.vel for w in ws]),
+               counts=[w.n for w in ws])
+    sim.snapshot()
+    tune = sim.autotune(5)
+    sim.step(3)
+    ms = timed_run(torch, sim, steps)
+    sim.close()
+    batched = n_total * steps / (ms / 1e3)
+    sample = ws[::len(ws) // 24][:24]
+    t_seq = 0.0
+    for w in sample:
+        s1 = E.Simulation.single(w.model.replace(precision="f64"), w.n)
+        s1.upload(w.pos, w.vel)
+        s1.snapshot()
+        s1.step(3)
+        t_seq += timed_run(torch, s1, steps) / 1e3
+        s1.close()
+    seq_total_s = t_seq * len(ws) / len(sample)
+    sequential = n_total * steps / seq_total_s
+    return {"workload": "ensemble", "sims": len(ws), "agents": n_total, "steps": steps,
+            "precision": "mixed", "autotune": tune, "batched_agent_steps_per_s": batched,
+            "batched_ms_per_step": ms / steps,
+            "sequential_f64_agent_steps_per_s": sequential,
+            "sequential_sample": f"{len(sample)} of {len(ws)} simulations, scaled",
+            "speedup": batched / sequential}
+
+
+def extra_served(n_requests=160, rate_hz=8.0):
+    """Poisson stream of simulation requests (N log-uniform [128, 262144], steps uniform
+    [100, 2000], 2D/3D and FP64/mixed 50/50) through the request server (continuous batching,
+    160 GB admission budget): p50/p99 submit-to-result latency and served agent-steps/s."""
+    import numpy as np
+    from cellular_raza_gb300 import serve as SV
+    from cellular_raza_gb300 import workloads as W
+
+    reqs = W.request_stream(seed=2024, n_requests=n_requests, rate_hz=rate_hz)
+    lat = []
+    with SV.Server(hbm_budget_bytes=160 << 30, steps_per_tick=32) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for r in reqs:
+            delay = r.arrival_s - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            tickets.append((r, srv.submit(r.workload)))
+        work = 0
+        for r, t in tickets:
+            res = srv.wait(t)
+            lat.append(res["latency_s"])
+            work += r.workload.n * r.workload.n_steps
+        makespan = time.perf_counter() - t0
+    lat = np.array(lat)
+    return {"workload": "request_stream", "requests": n_requests, "rate_hz": rate_hz,
+            "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)),
+            "served_agent_steps_per_s": work / makespan, "makespan_s": makespan,
+            "note": f"{n_requests} of the 20,000-request stream at one rate"}
+
+
 def crg_arm(args):
     rank, world, local = dist_env()
     if world > 1:
@@ -349,6 +465,16 @@ def crg_arm(args):
                      "bytes_per_step": sort_bytes}
     gpu_launches = prof["kernels"] // prof_steps * w.n_steps * args.steps if prof_steps else None
 
+    sim.close()
+    extras = {}
+    if world == 1 and not args.no_extras:
+        for name, fn in (("mixed_large", lambda: extra_mixed_large(torch)),
+                         ("ensemble", lambda: extra_ensemble(torch)),
+                         ("served", extra_served)):
+            try:
+                extras[name] = fn()
+            except Exception as e:  # reported, not fatal for the headline line
+                extras[name] = {"error": f"{type(e).__name__}: {e}"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_run(w, n_cpu, args.cpu_seconds, w.n_steps)
@@ -372,9 +498,11 @@ def crg_arm(args):
             "clocks": clk.summary(),
             "gpu_launches": gpu_launches,
             "fma_peaks_tflops": fma,
+            "mixed_large": extras.get("mixed_large"),
+            "ensemble": extras.get("ensemble"),
+            "served": extras.get("served"),
         }
         print(json.dumps(line), flush=True)
-    sim.close()
     if dist is not None:
         dist.destroy_process_group()
 

@@ -23,7 +23,10 @@ EXPORTED = [
     "crg_create", "crg_create_batch", "crg_upload", "crg_step", "crg_download",
     "crg_agent_count", "crg_last_error", "crg_destroy", "crg_strerror", "crg_set_option",
     "crg_debug_forces", "crg_debug_neighbor_stats", "crg_profile", "crg_measure_fma_peaks",
-    "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc",
+    "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc", "crg_autotune",
+    "crg_set_sim_stop", "crg_sim_download", "crg_clear_error", "crg_repack", "crg_step_count",
+    "crg_server_create", "crg_server_submit", "crg_server_wait", "crg_server_stats",
+    "crg_server_destroy",
 ]
 NOALLOC_MAX_POINTS = 1 << 20
 NOALLOC_MAX_VOXELS = 1 << 20
@@ -115,6 +118,20 @@ def load(build_if_missing: bool = True):
     L.crg_snapshot.argtypes = [vp, C.c_int32]
     L.crg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.crg_cell_list_noalloc.argtypes = [C.POINTER(CrgDomain), C.c_int64, vp, vp, vp, vp, vp]
+    L.crg_autotune.argtypes = [vp, C.c_int64, i64p, i64p, dp]
+    L.crg_set_sim_stop.argtypes = [vp, C.c_int32, C.c_int64]
+    L.crg_sim_download.argtypes = [vp, C.c_int32, i64p, dp, dp, u64p]
+    L.crg_clear_error.argtypes = [vp, C.POINTER(C.c_int32)]
+    L.crg_repack.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32,
+                             C.POINTER(CrgDomain), C.POINTER(CrgModel), i64p, i64p, dp, dp,
+                             C.POINTER(vp)]
+    L.crg_step_count.argtypes = [vp, i64p]
+    L.crg_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
+    L.crg_server_submit.argtypes = [vp, C.POINTER(CrgDomain), C.POINTER(CrgModel), C.c_int64,
+                                    dp, dp, C.c_int64, u64p]
+    L.crg_server_wait.argtypes = [vp, C.c_uint64, C.c_double, i64p, dp, dp, u64p, dp]
+    L.crg_server_stats.argtypes = [vp, i64p, i64p, i64p, i64p, i64p]
+    L.crg_server_destroy.argtypes = [vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if name != "crg_strerror":

@@ -16,7 +16,8 @@ LIB_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libcrg.so")
 
-SOURCES = ["crg_api.cu", "crg_sort.cu", "crg_spheres.cu", "crg_rods.cu", "crg_peaks.cu"]
+SOURCES = ["crg_api.cu", "crg_sort.cu", "crg_spheres.cu", "crg_rods.cu", "crg_peaks.cu",
+           "crg_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr"]

@@ -62,6 +62,9 @@ struct crg_ctx {
   int32_t err_code = CRG_OK;
   int64_t err_agent = -1, err_step = -1;
   int64_t steps_done = 0;
+  int32_t err_sim = -1;
+  std::vector<crg_domain> doms;  // as given at creation (for crg_repack)
+  std::vector<crg_model> mods;
 };
 
 namespace {
@@ -160,6 +163,7 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.strength = m.strength;
   S.dt = m.dt;
   S.order = m.solver_order;
+  S.stop_step = INT64_MAX;
   S.radius_f = (float)m.radius;
   S.stiffness_f = (float)m.stiffness;
   S.cutoff_f = (float)m.cutoff;
@@ -241,7 +245,7 @@ int32_t allocate(crg_ctx *c) {
   A(count, (size_t)c->n_vox + 1);
   A(start, (size_t)c->n_vox + 1);
   A(bsum, (size_t)c->n_vox / 4096 + 2);
-  A(status, 4);
+  A(status, 8);
   A(step_ctr, 1);
   A(staging, cap * nc);
   if (c->order > 1) {
@@ -252,10 +256,10 @@ int32_t allocate(crg_ctx *c) {
   }
   if (c->n_sims > 1) A(d_sim_of_voxel, c->n_vox);
 #undef A
-  CUDA_TRY(cudaMallocHost((void **)&c->h_status, 4 * sizeof(int32_t)));
+  CUDA_TRY(cudaMallocHost((void **)&c->h_status, 8 * sizeof(int32_t)));
   CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), c->stream));
-  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 4, c->stream));
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, c->stream));
   CUDA_TRY(cudaMemsetAsync(c->step_ctr, 0, sizeof(int64_t), c->stream));
   if (c->n_sims > 1) {
     std::vector<uint32_t> sov(c->n_vox);
@@ -282,6 +286,8 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
   c->order = m0.solver_order;
   c->n_sims = n_sims;
   c->sims_h.resize(n_sims);
+  c->doms.assign(domains, domains + n_sims);
+  c->mods.assign(models, models + n_sims);
   c->caps.assign(capacities, capacities + n_sims);
   uint64_t vox = 0;
   int64_t cap = 0;
@@ -299,6 +305,7 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
       return r;
     }
     c->sims_h[s].voxel_off = (uint32_t)vox;
+    c->sims_h[s].sim_index = s;
     vox += c->sims_h[s].n_vox;
     cap += capacities[s];
     if (vox > 0x7fffffffull || cap > 0x7fffffffll) {
@@ -402,7 +409,7 @@ void launch_one_step(crg_ctx *c) {
 // Waits for the handle's stream and reads the device status word.  A CUDA failure is
 // recorded as the handle's error (so every later call reports it too).
 int32_t read_status(crg_ctx *c) {
-  cudaError_t e = cudaMemcpyAsync(c->h_status, c->status, 4 * sizeof(int32_t),
+  cudaError_t e = cudaMemcpyAsync(c->h_status, c->status, 8 * sizeof(int32_t),
                                   cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
@@ -415,6 +422,7 @@ int32_t read_status(crg_ctx *c) {
     c->err_code = c->h_status[0];
     c->err_agent = (int64_t)(((uint64_t)(uint32_t)c->h_status[2] << 32) | (uint32_t)c->h_status[1]);
     c->err_step = c->h_status[3];
+    c->err_sim = c->h_status[4];
     return c->err_code;
   }
   return CRG_OK;
@@ -519,7 +527,7 @@ int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *p
                            cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(c->d_agent_off, c->agent_off_h.data(),
                            sizeof(uint32_t) * (c->n_sims + 1), cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 4, st));
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, st));
   CUDA_TRY(cudaMemsetAsync(c->step_ctr, 0, sizeof(int64_t), st));
   CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), st));
   const size_t bytes = sizeof(double) * (size_t)n * c->nc;
@@ -681,14 +689,269 @@ int32_t crg_snapshot(crg_ctx *c, int32_t op) {
     c->steps_done = c->snap_steps;
     c->err_code = CRG_OK;
     c->err_agent = c->err_step = -1;
-    CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 4, c->stream));
+    CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, c->stream));
   }
   return CRG_OK;
+}
+
+int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block,
+                     double *ms_per_step) {
+  if (!c || steps <= 0) return CRG_EINVAL;
+  if (c->err_code != CRG_OK) return c->err_code;
+  struct Shape {
+    int variant, block;
+  };
+  std::vector<Shape> shapes;
+  if (c->kind == CRG_KIND_ROD) {
+    shapes = {{0, 0}, {1, 64}, {2, 0}};
+  } else if (c->precision == CRG_PREC_F64) {
+    shapes = {{0, 0}, {1, 64}, {1, 128}, {1, 256}};
+  } else {
+    shapes = {{1, 64}, {1, 128}, {1, 256}};
+  }
+  int32_t r = crg_snapshot(c, CRG_SNAPSHOT_SAVE);
+  if (r != CRG_OK) return r;
+  const int saved_variant = c->variant, saved_block = c->block, saved_profile = c->profile;
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best_ms = 1e300;
+  Shape best = {saved_variant, saved_block};
+  c->profile = 0;
+  for (const Shape &s : shapes) {
+    c->variant = s.variant;
+    c->block = s.block;
+    if ((r = crg_snapshot(c, CRG_SNAPSHOT_RESTORE)) != CRG_OK) break;
+    launch_one_step(c);  // warm-up (first launch of this shape)
+    if ((r = crg_snapshot(c, CRG_SNAPSHOT_RESTORE)) != CRG_OK) break;
+    cudaEventRecord(e0, c->stream);
+    for (int64_t k = 0; k < steps; ++k) launch_one_step(c);
+    cudaEventRecord(e1, c->stream);
+    if ((r = read_status(c)) != CRG_OK) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms / steps < best_ms) {
+      best_ms = ms / steps;
+      best = s;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->variant = best.variant;
+  c->block = best.block;
+  c->profile = saved_profile;
+  invalidate_graph(c);
+  int32_t r2 = crg_snapshot(c, CRG_SNAPSHOT_RESTORE);
+  if (r != CRG_OK) return r;
+  if (variant) *variant = best.variant;
+  if (block) *block = best.block;
+  if (ms_per_step) *ms_per_step = best_ms;
+  return r2;
 }
 
 int32_t crg_get_stream(crg_ctx *c, void **stream) {
   if (!c || !stream) return CRG_EINVAL;
   *stream = (void *)c->stream;
+  return CRG_OK;
+}
+
+int32_t crg_step_count(crg_ctx *c, int64_t *steps) {
+  if (!c || !steps) return CRG_EINVAL;
+  *steps = c->steps_done;
+  return CRG_OK;
+}
+
+int32_t crg_set_sim_stop(crg_ctx *c, int32_t sim, int64_t stop_step) {
+  if (!c || sim < 0 || sim >= c->n_sims) return CRG_EINVAL;
+  c->sims_h[sim].stop_step = stop_step < 0 ? 0 : stop_step;
+  CUDA_TRY(cudaMemcpyAsync(&c->d_sims[sim], &c->sims_h[sim], sizeof(SimDev),
+                           cudaMemcpyHostToDevice, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return CRG_OK;
+}
+
+int32_t crg_sim_download(crg_ctx *c, int32_t sim, int64_t *n, double *pos, double *vel,
+                         uint64_t *ids) {
+  if (!c || sim < 0 || sim >= c->n_sims) return CRG_EINVAL;
+  const uint32_t off = c->agent_off_h[sim], cnt = c->agent_off_h[sim + 1] - off;
+  if (n) *n = cnt;
+  if (cnt == 0) return CRG_OK;
+  cudaStream_t st = c->stream;
+  const size_t bytes = sizeof(double) * (size_t)cnt * c->nc;
+  if (pos) {
+    crg::launch_transpose_out(c->pos + off, c->staging, cnt, c->nc, c->cap, st);
+    CUDA_TRY(cudaMemcpyAsync(pos, c->staging, bytes, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (vel) {
+    crg::launch_transpose_out(c->vel + off, c->staging, cnt, c->nc, c->cap, st);
+    CUDA_TRY(cudaMemcpyAsync(vel, c->staging, bytes, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  if (ids)
+    CUDA_TRY(cudaMemcpyAsync(ids, c->id + off, sizeof(uint64_t) * cnt, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CRG_OK;
+}
+
+int32_t crg_clear_error(crg_ctx *c, int32_t *sim) {
+  if (!c) return CRG_EINVAL;
+  if (sim) *sim = c->err_sim;
+  const int32_t code = c->err_code;
+  c->err_code = CRG_OK;
+  c->err_agent = c->err_step = -1;
+  c->err_sim = -1;
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, c->stream));
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return code;
+}
+
+int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_new,
+                   const crg_domain *new_domains, const crg_model *new_models,
+                   const int64_t *new_caps, const int64_t *new_counts, const double *new_pos,
+                   const double *new_vel, crg_ctx **out) {
+  if (!out || n_keep < 0 || n_new < 0 || n_keep + n_new < 1) return CRG_EINVAL;
+  if (n_keep > 0 && (!src || !keep)) return CRG_EINVAL;
+  if (n_new > 0 && (!new_domains || !new_models || !new_caps || !new_counts)) return CRG_EINVAL;
+  *out = nullptr;
+  const int n_total = n_keep + n_new;
+  std::vector<crg_domain> doms;
+  std::vector<crg_model> mods;
+  std::vector<int64_t> caps, counts;
+  int64_t n_new_agents = 0;
+  for (int s = 0; s < n_new; ++s) {
+    if (new_counts[s] < 0 || new_counts[s] > new_caps[s]) return CRG_EINVAL;
+    doms.push_back(new_domains[s]);
+    mods.push_back(new_models[s]);
+    caps.push_back(new_caps[s]);
+    counts.push_back(new_counts[s]);
+    n_new_agents += new_counts[s];
+  }
+  if (n_new_agents > 0 && (!new_pos || !new_vel)) return CRG_EINVAL;
+  std::vector<char> seen(src ? src->n_sims : 0, 0);
+  for (int k = 0; k < n_keep; ++k) {
+    const int s = keep[k];
+    if (s < 0 || s >= src->n_sims || seen[s]) return CRG_EINVAL;
+    seen[s] = 1;
+    doms.push_back(src->doms[s]);
+    mods.push_back(src->mods[s]);
+    const int64_t cnt = src->agent_off_h[s + 1] - src->agent_off_h[s];
+    caps.push_back(std::max<int64_t>(src->caps[s], cnt));
+    counts.push_back(cnt);
+  }
+  crg_ctx *c = nullptr;
+  int32_t r = create_impl(n_total, doms.data(), mods.data(), caps.data(), &c);
+  if (r != CRG_OK) return r;
+  if (src) {
+    c->variant = src->variant;
+    c->block = src->block;
+    c->prefilter = src->prefilter;
+    c->graph_chunk = src->graph_chunk;
+  }
+  // agent layout: new simulations first (input order), then the kept ones
+  c->agent_off_h.assign(n_total + 1, 0);
+  for (int s = 0; s < n_total; ++s) {
+    c->agent_off_h[s + 1] = c->agent_off_h[s] + (uint32_t)counts[s];
+    c->sims_h[s].agent_off = c->agent_off_h[s];
+    c->sims_h[s].n_agents = (uint32_t)counts[s];
+  }
+  c->n_agents = c->agent_off_h[n_total];
+  cudaStream_t st = c->stream;
+  auto fail = [&](int32_t code) {
+    crg_destroy(c);
+    return code;
+  };
+  if (cudaMemcpyAsync(c->d_sims, c->sims_h.data(), sizeof(SimDev) * n_total,
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(c->d_agent_off, c->agent_off_h.data(), sizeof(uint32_t) * (n_total + 1),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), st) != cudaSuccess)
+    return fail(CRG_ECUDA);
+  if (c->order > 1) {
+    if (cudaMemsetAsync(c->nhmeta, 0, (size_t)c->cap, st) != cudaSuccess ||
+        cudaMemsetAsync(c->nhist, 0, sizeof(double) * (size_t)c->cap * c->nc * 2, st) != cudaSuccess)
+      return fail(CRG_ECUDA);
+  }
+  // new simulations: host data into the "next" arrays
+  if (n_new_agents > 0) {
+    const size_t bytes = sizeof(double) * (size_t)n_new_agents * c->nc;
+    if (cudaMemcpyAsync(c->staging, new_pos, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(CRG_ECUDA);
+    crg::launch_transpose_in(c->staging, c->npos, (uint32_t)n_new_agents, c->nc, c->cap, st);
+    if (cudaMemcpyAsync(c->staging, new_vel, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return fail(CRG_ECUDA);
+    crg::launch_transpose_in(c->staging, c->nvel, (uint32_t)n_new_agents, c->nc, c->cap, st);
+    std::vector<uint64_t> iota((size_t)n_new_agents);
+    size_t q = 0;
+    for (int s = 0; s < n_new; ++s)
+      for (int64_t j = 0; j < counts[s]; ++j) iota[q++] = (uint64_t)j;
+    if (cudaMemcpyAsync(c->nid, iota.data(), sizeof(uint64_t) * iota.size(),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return fail(CRG_ECUDA);
+    SortArgs A = sort_args(c, 1);
+    A.n_agents = (uint32_t)n_new_agents;
+    crg::launch_init_keys(A, c->nv, st);
+  }
+  // kept simulations: device-resident state, cell-list order preserved
+  if (n_keep > 0) {
+    std::vector<uint32_t> dst_off(n_keep + 1), src_off(n_keep);
+    std::vector<int64_t> shift(n_keep);
+    for (int k = 0; k < n_keep; ++k) {
+      dst_off[k] = c->agent_off_h[n_new + k];
+      src_off[k] = src->agent_off_h[keep[k]];
+      shift[k] = (int64_t)c->sims_h[n_new + k].voxel_off - (int64_t)src->sims_h[keep[k]].voxel_off;
+    }
+    dst_off[n_keep] = c->n_agents;
+    uint32_t *d_dst = nullptr, *d_src = nullptr;
+    int64_t *d_shift = nullptr;
+    if (dalloc(&d_dst, n_keep + 1) || dalloc(&d_src, n_keep) || dalloc(&d_shift, n_keep)) {
+      cudaFree(d_dst);
+      cudaFree(d_src);
+      return fail(CRG_ENOMEM);
+    }
+    // the source pack's last launches must be complete before its state is read
+    cudaStreamSynchronize(src->stream);
+    cudaMemcpyAsync(d_dst, dst_off.data(), sizeof(uint32_t) * (n_keep + 1), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_src, src_off.data(), sizeof(uint32_t) * n_keep, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_shift, shift.data(), sizeof(int64_t) * n_keep, cudaMemcpyHostToDevice, st);
+    crg::RepackArgs R;
+    std::memset(&R, 0, sizeof(R));
+    R.spos = src->pos;
+    R.svel = src->vel;
+    R.shist = src->hist;
+    R.sid = src->id;
+    R.skey = src->key;
+    R.shmeta = src->hmeta;
+    R.scap = src->cap;
+    R.dpos = c->npos;
+    R.dvel = c->nvel;
+    R.dhist = c->nhist;
+    R.did = c->nid;
+    R.dkey = c->nkey;
+    R.dhmeta = c->nhmeta;
+    R.dcount = c->count;
+    R.dcap = c->cap;
+    R.nc = c->nc;
+    R.has_hist = c->order > 1 && src->order > 1;
+    R.n_keep = n_keep;
+    R.dst_off = d_dst;
+    R.src_off = d_src;
+    R.key_shift = d_shift;
+    R.first = c->agent_off_h[n_new];
+    R.last = c->n_agents;
+    crg::launch_repack(R, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(d_dst);
+    cudaFree(d_src);
+    cudaFree(d_shift);
+    if (e != cudaSuccess) return fail(CRG_ECUDA);
+  }
+  crg::launch_sort(sort_args(c, 1), c->bsum, st);
+  if (cudaGetLastError() != cudaSuccess) return fail(CRG_ECUDA);
+  r = read_status(c);
+  if (r != CRG_OK) return fail(r);
+  *out = c;
   return CRG_OK;
 }
 

@@ -40,6 +40,8 @@ struct SimDev {
   float filt_thr2;  // squared FP32 prefilter threshold (cutoff + conservative margin)^2
   float off_lim;    // |FP32 offset| bound the prefilter margin was derived for
   int32_t order;    // 1 Euler, 2 AB2, 3 AB3
+  int32_t sim_index;
+  int64_t stop_step;  // the simulation is frozen once the pack's step counter reaches this
 };
 
 // Arguments shared by the per-step kernels of a pack.
@@ -141,13 +143,33 @@ __device__ __forceinline__ uint32_t sim_of_agent(const PackArgs &P, uint32_t i) 
   return (uint32_t)lo;
 }
 
+// status word: [0] code, [1] agent id lo, [2] agent id hi, [3] step (or check site),
+// [4] simulation index within the pack
 __device__ __forceinline__ void set_status(int32_t *status, int32_t code, uint64_t agent,
-                                           int64_t step) {
+                                           int64_t step, int32_t sim = 0) {
   if (atomicCAS(&status[0], 0, code) == 0) {
     status[1] = (int32_t)(agent & 0xffffffffu);
     status[2] = (int32_t)(agent >> 32);
     status[3] = (int32_t)step;
+    status[4] = sim;
   }
+}
+
+// A frozen simulation (its requested number of steps is done) is carried through the step
+// unchanged: same state, same voxel, same cell-list position.
+__device__ __forceinline__ void frozen_copy(const PackArgs &P, uint32_t i, uint32_t key, int nc) {
+  const int64_t cap = P.cap;
+  for (int c = 0; c < nc; ++c) {
+    P.npos[c * cap + i] = P.pos[c * cap + i];
+    P.nvel[c * cap + i] = P.vel[c * cap + i];
+  }
+  if (P.hist) {
+    for (int c = 0; c < 2 * nc; ++c) P.nhist[c * cap + i] = P.hist[c * cap + i];
+    P.nhmeta[i] = P.hmeta[i];
+  }
+  P.nkey[i] = key;
+  P.nid[i] = P.id[i];
+  atomicAdd(&P.count[key], 1u);
 }
 
 // Invariant checks of the cell list.  A violation records CRG_EINTERNAL with the index and

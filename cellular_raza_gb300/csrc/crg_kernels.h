@@ -40,6 +40,27 @@ struct SortArgs {
   int64_t *step_ctr;
 };
 
+// Copy of kept simulations from one pack into the "next" arrays of another (crg_repack).
+struct RepackArgs {
+  const double *spos, *svel, *shist;
+  const uint64_t *sid;
+  const uint32_t *skey;
+  const uint8_t *shmeta;
+  int64_t scap;
+  double *dpos, *dvel, *dhist;
+  uint64_t *did;
+  uint32_t *dkey;
+  uint8_t *dhmeta;
+  uint32_t *dcount;
+  int64_t dcap;
+  int32_t nc, has_hist, n_keep;
+  const uint32_t *dst_off;   // [n_keep + 1] destination agent offsets
+  const uint32_t *src_off;   // [n_keep]     source agent offsets
+  const int64_t *key_shift;  // [n_keep]     destination minus source voxel offset
+  uint32_t first, last;      // destination index range of the kept agents
+};
+void launch_repack(const RepackArgs &A, cudaStream_t st);
+
 void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st);
 int sort_kernel_count();
 void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st);

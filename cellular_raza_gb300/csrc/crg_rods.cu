@@ -287,7 +287,7 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 #pragma unroll
   for (int k = 0; k < NC; ++k)
     if (np[k] < S.min[k % D] || np[k] > S.max[k % D]) inside = false;
-  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1);
+  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1, S.sim_index);
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
     P.npos[k * cap + i] = np[k];
@@ -331,6 +331,10 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   if (key - S.voxel_off >= S.n_vox) {
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
+  }
+  if (*P.step_ctr >= S.stop_step) {  // frozen simulation
+    frozen_copy(P, i, key, NC);
+    return;
   }
   const uint32_t v = key - S.voxel_off;
   int idx[D];
@@ -509,7 +513,8 @@ __global__ void __launch_bounds__(W * 32) k_rods_packed(const PackArgs P) {
   }
   const int n_box = nb[0] * nb[1] * nb[2];
   // enumeration cursor
-  bool done = !valid;
+  const bool frozen = valid && (*P.step_ctr >= S.stop_step);
+  bool done = !valid || frozen;
   int stage = 0;  // 0: next voxel, 1: next candidate, 2: inside a pass
   int o_box = 0;
   uint32_t b_next = 0, b_end = 0, cur_b = 0;
@@ -721,6 +726,10 @@ __global__ void __launch_bounds__(W * 32) k_rods_packed(const PackArgs P) {
     __syncwarp();
   }
   if (!valid) return;
+  if (frozen) {
+    frozen_copy(P, i, key, NC);
+    return;
+  }
   double pa[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
@@ -794,7 +803,8 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
   }
   const int n_box = nb[0] * nb[1] * nb[2];
   // cursor
-  bool done = !valid;
+  const bool frozen = valid && (*P.step_ctr >= S.stop_step);
+  bool done = !valid || frozen;
   int o_box = 0;
   uint32_t b_next = 0, b_end = 0, cur_b = 0;
   bool same = false, twice = false, ext_first = false;
@@ -1028,6 +1038,10 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
     __syncwarp();
   }
   if (!valid) return;
+  if (frozen) {
+    frozen_copy(P, i, key, NC);
+    return;
+  }
   double pa[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];

@@ -253,6 +253,31 @@ __global__ void k_init_keys(const SortArgs A, int nv) {
   atomicAdd(&A.count[k], 1u);
 }
 
+// Kept simulations of a repack: state copied in cell-list order, keys shifted to the new
+// voxel offsets, histogram counted (the insertion sort that follows keeps this order).
+__global__ void k_repack(const RepackArgs A) {
+  const uint32_t j = A.first + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= A.last) return;
+  int lo = 0, hi = A.n_keep;  // dst_off[lo] <= j < dst_off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (A.dst_off[mid] <= j) lo = mid; else hi = mid;
+  }
+  const uint32_t s = A.src_off[lo] + (j - A.dst_off[lo]);
+  for (int c = 0; c < A.nc; ++c) {
+    A.dpos[c * A.dcap + j] = A.spos[c * A.scap + s];
+    A.dvel[c * A.dcap + j] = A.svel[c * A.scap + s];
+  }
+  if (A.has_hist) {
+    for (int c = 0; c < 2 * A.nc; ++c) A.dhist[c * A.dcap + j] = A.shist[c * A.scap + s];
+    A.dhmeta[j] = A.shmeta[s];
+  }
+  A.did[j] = A.sid[s];
+  const uint32_t k = (uint32_t)((int64_t)A.skey[s] + A.key_shift[lo]);
+  A.dkey[j] = k;
+  atomicAdd(&A.dcount[k], 1u);
+}
+
 // Agent-major host layout [n][nc] -> component-major device layout [nc][cap].
 __global__ void k_transpose_in(const double *__restrict__ src, double *__restrict__ dst,
                                uint32_t n, int nc, int64_t cap) {
@@ -285,6 +310,10 @@ void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
 }
 
 int sort_kernel_count() { return 6; }
+
+void launch_repack(const RepackArgs &A, cudaStream_t st) {
+  if (A.last > A.first) k_repack<<<grid_for(A.last - A.first, 256), 256, 0, st>>>(A);
+}
 
 void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st) {
   if (A.n_agents) k_init_keys<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A, nv);

@@ -110,7 +110,7 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
 #pragma unroll
   for (int c = 0; c < D; ++c)
     if (np[c] < S.min[c] || np[c] > S.max[c]) inside = false;
-  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1);
+  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1, S.sim_index);
 #pragma unroll
   for (int c = 0; c < D; ++c) {
     P.npos[c * cap + i] = np[c];
@@ -141,6 +141,10 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
   if (key - S.voxel_off >= S.n_vox) {
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
+  }
+  if (*P.step_ctr >= S.stop_step) {  // frozen simulation
+    frozen_copy(P, i, key, D);
+    return;
   }
   const uint32_t v = key - S.voxel_off;
   int idx[D];
@@ -281,7 +285,8 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
     nb[c] = hi - lo[c] + 1;
   }
   const int n_box = nb[0] * nb[1] * nb[2];
-  bool done = !valid;
+  const bool frozen = valid && (*P.step_ctr >= S.stop_step);
+  bool done = !valid || frozen;
   int o_box = 0;
   uint32_t b_next = 0, b_end = 0;
   bool twice = false;
@@ -388,6 +393,10 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
     __syncwarp();
   }
   if (!valid) return;
+  if (frozen) {
+    frozen_copy(P, i, key, D);
+    return;
+  }
   sphere_update<D>(P, S, i, key, pa, va, acc);
 }
 

@@ -186,6 +186,13 @@ class Simulation:
         N.check(self._L.crg_get_stream(self._h, C.byref(s)), "crg_get_stream")
         return s.value or 0
 
+    def autotune(self, steps: int = 5) -> Dict[str, float]:
+        """Times every force-kernel shape on the current state and keeps the fastest."""
+        v, b, ms = C.c_int64(), C.c_int64(), C.c_double()
+        rc = self._L.crg_autotune(self._h, int(steps), C.byref(v), C.byref(b), C.byref(ms))
+        N.check(rc, "crg_autotune", self._h)
+        return {"variant": v.value, "block": b.value, "ms_per_step": ms.value}
+
     def profile(self):
         out = (C.c_double * 3)()
         N.check(self._L.crg_profile(self._h, out), "crg_profile")

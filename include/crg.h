@@ -119,6 +119,60 @@ int32_t crg_step(crg_ctx *ctx, int64_t n_steps);
  * NULL.  voxel receives the voxel plain index (per simulation). */
 int32_t crg_download(crg_ctx *ctx, double *pos, double *vel, uint64_t *ids, uint32_t *voxel);
 
+/* ---- continuous batching --------------------------------------------------------------
+ * chili runs one simulation per run_simulation! call; serving many requests needs three more
+ * primitives (no counterpart in the reference beyond the per-simulation semantics above). */
+
+/* A simulation whose pack step counter reaches stop_step is frozen: later steps leave its
+ * state untouched, so one launch can carry simulations that need different step counts. */
+int32_t crg_set_sim_stop(crg_ctx *ctx, int32_t sim, int64_t stop_step);
+
+/* Steps the handle has run since its creation or last upload (its step counter). */
+int32_t crg_step_count(crg_ctx *ctx, int64_t *steps);
+
+/* Agents of one simulation of the handle (cell-list order), like crg_download. */
+int32_t crg_sim_download(crg_ctx *ctx, int32_t sim, int64_t *n, double *pos, double *vel,
+                         uint64_t *ids);
+
+/* Returns the handle's error code, stores the index of the simulation that raised it in
+ * *sim and clears it so the other simulations can continue. */
+int32_t crg_clear_error(crg_ctx *ctx, int32_t *sim);
+
+/* New handle = simulations `keep[0..n_keep)` of `src` with their device-resident state
+ * (cell-list order, solver history; copied device to device) + n_new simulations from
+ * host memory (agents of all new simulations back to back, like crg_upload).  In the new
+ * handle the new simulations come first (indices 0..n_new-1), then the kept ones in the
+ * order given; the step counter starts at 0 and every stop step is unset.  `src` is left
+ * unchanged (destroy it when done). */
+int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_new,
+                   const crg_domain *new_domains, const crg_model *new_models,
+                   const int64_t *new_caps, const int64_t *new_counts, const double *new_pos,
+                   const double *new_vel, crg_ctx **out);
+
+/* ---- serving ----------------------------------------------------------------------------
+ * A request server keeps many simulations resident on the device and advances them together
+ * (continuous batching): requests are admitted first-come first-served while their
+ * estimated device footprint fits `hbm_budget_bytes`; admitted simulations join the running
+ * pack of their class (kind, dim, vertices, precision, solver order) without moving the
+ * running ones off the device (crg_repack); every simulation stops exactly after its own
+ * number of steps (crg_set_sim_stop); the pack advances `steps_per_tick` steps between
+ * admissions.  A result is bit-identical to running the same simulation alone.
+ * One background thread drives the device; submit/wait are thread-safe. */
+typedef struct crg_server crg_server;
+int32_t crg_server_create(int64_t hbm_budget_bytes, int32_t steps_per_tick, crg_server **out);
+/* Queues one simulation (inputs copied; n agents [n][nv][dim]); returns a ticket. */
+int32_t crg_server_submit(crg_server *srv, const crg_domain *domain, const crg_model *model,
+                          int64_t n, const double *pos, const double *vel, int64_t n_steps,
+                          uint64_t *ticket);
+/* Waits up to timeout_s (< 0: forever) for a ticket; on completion copies its final state
+ * (cell-list order, ids give the input index) and the submit-to-completion latency, and
+ * forgets the ticket.  Returns the request's status, or CRG_ETIMEDOUT. */
+int32_t crg_server_wait(crg_server *srv, uint64_t ticket, double timeout_s, int64_t *n,
+                        double *pos, double *vel, uint64_t *ids, double *latency_s);
+int32_t crg_server_stats(crg_server *srv, int64_t *queued, int64_t *active, int64_t *completed,
+                         int64_t *bytes_in_use, int64_t *agent_steps);
+int32_t crg_server_destroy(crg_server *srv);
+
 /* Number of agents currently held (total over simulations of a batch). */
 int32_t crg_agent_count(crg_ctx *ctx, int64_t *n);
 
@@ -137,6 +191,14 @@ int32_t crg_snapshot(crg_ctx *ctx, int32_t op);
 /* The CUDA stream (cudaStream_t) every launch of the handle is issued on, for callers that
  * order their own work or events against it. */
 int32_t crg_get_stream(crg_ctx *ctx, void **stream);
+
+/* Autotuner: times `steps` steps of every force-kernel shape this handle can use (kernel
+ * variant x block size) on the handle's current state, restoring that state after each
+ * trial (crg_snapshot), and keeps the fastest: *variant and *block receive the chosen
+ * CRG_OPT_KERNEL_VARIANT / CRG_OPT_BLOCK values, *ms_per_step its time.  The simulation
+ * state is unchanged on return. */
+int32_t crg_autotune(crg_ctx *ctx, int64_t steps, int64_t *variant, int64_t *block,
+                     double *ms_per_step);
 
 /* Destroys the handle and frees its device memory. */
 int32_t crg_destroy(crg_ctx *ctx);
