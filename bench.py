@@ -217,6 +217,21 @@ def algorithmic_flops(w, stats):
     return 30.0 * n_inter + 21.0 * w.n
 
 
+def replica_throughput(dist, local_ms, local_agent_steps):
+    """Whole-job throughput of independent replicas: the agent-steps of all ranks over the
+    slowest rank's time.  Returns (max ms, total agent-steps, agent-steps/s)."""
+    import torch
+
+    t_max, total = float(local_ms), float(local_agent_steps)
+    if dist is not None:
+        t = torch.tensor([t_max], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        s = torch.tensor([total], dtype=torch.float64)
+        dist.all_reduce(s, op=dist.ReduceOp.SUM)
+        t_max, total = float(t.item()), float(s.item())
+    return t_max, total, total / (t_max / 1e3)
+
+
 def timed_run(torch, sim, steps, restore=True):
     """Device time (ms) of `steps` steps of a handle, CUDA events on its stream."""
     ext = torch.cuda.ExternalStream(sim.stream())
@@ -252,10 +267,17 @@ def extra_mixed_large(torch):
         finals[prec] = sim.download(order="id")["pos"]
         sim.close()
     a, b = finals["f64"], finals["mixed"]
-    err = np.linalg.norm(b - a, axis=-1) / np.linalg.norm(a, axis=-1)
+    dx = np.linalg.norm(b - a, axis=-1).ravel()
+    x = np.linalg.norm(a, axis=-1).ravel()
+    err = dx / x
+    worst = int(np.argmax(err))
     out["speedup_mixed_over_f64"] = out["mixed_agent_steps_per_s"] / out["f64_agent_steps_per_s"]
-    out["max_rel_pos_err"] = float(err.max())
+    out["max_rel_pos_err"] = float(err.max())  # per agent |dx| / |x|
+    out["p9999_rel_pos_err"] = float(np.percentile(err, 99.99))
     out["mean_rel_pos_err"] = float(err.mean())
+    out["normwise_rel_pos_err"] = float(dx.max() / x.max())  # max |dx| / max |x|
+    out["max_abs_pos_err"] = float(dx.max())
+    out["worst_agent_abs_pos"] = float(x[worst])
     return out
 
 
@@ -380,13 +402,7 @@ def crg_arm(args):
         torch.cuda.synchronize()
     barrier()
     ms = ev0.elapsed_time(ev1)
-    t_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    agent_steps = w.n * w.n_steps * args.steps * world
-    value = agent_steps / (t_max / 1e3)
+    t_max, agent_steps, value = replica_throughput(dist, ms, w.n * w.n_steps * args.steps)
 
     # e2e through the C ABI with host buffers (pinned)
     nbytes = w.pos.size * 8
@@ -423,12 +439,8 @@ def crg_arm(args):
                 flush.zero_()
     e1.record(ext)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = agent_steps / (e2e_ms / 1e3)
+    e2e_ms, _, e2e_value = replica_throughput(dist, e0.elapsed_time(e1),
+                                              w.n * w.n_steps * args.steps)
     h2d = 2 * nbytes
     d2h = 2 * nbytes + 8 * w.n + 4 * w.n
 

@@ -183,6 +183,7 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   double margin = 128.0 * err + 1e-4 * std::fabs(m.cutoff) + 1e-6;
   double thr = std::fabs(m.cutoff) + margin;
   S.off_lim = (float)off_lim;
+  S.band_f = (float)margin;
   S.filt_thr2 = (float)(thr * thr);
   if (!std::isfinite(S.filt_thr2)) S.filt_thr2 = __builtin_inff();
   return CRG_OK;

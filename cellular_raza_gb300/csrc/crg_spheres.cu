@@ -212,9 +212,25 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
               }
             }
           } else {
-            // FP32 Morse on the FP32 displacement (offsets are accurate to ~1e-6 dx).
+            // FP32 Morse on the FP32 displacement (offsets are accurate to ~1e-6 dx).  Whether
+            // the pair interacts is decided exactly as on the FP64 path: pairs whose FP32
+            // distance lies within the prefilter margin of the cutoff or of zero are decided
+            // from the FP64 distance, so no pair switches on or off relative to FP64.
             const float dist = sqrtf(d2);
-            if (!(dist > S.cutoff_f || dist == 0.0f)) {
+            bool in;
+            if (fabsf(dist - S.cutoff_f) <= S.band_f || dist <= S.band_f) {
+              double n2 = 0.0;
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const double z = dsub(pa[c], P.pos[c * cap + b]);
+                n2 = (c == 0) ? dmul(z, z) : dadd(n2, dmul(z, z));
+              }
+              const double d64 = __dsqrt_rn(n2);
+              in = !(d64 > S.cutoff || d64 == 0.0);
+            } else {
+              in = !(dist > S.cutoff_f);
+            }
+            if (in) {
               const float r = S.radius_f + S.radius_f;
               const float e = expf(-S.stiffness_f * (dist - r));
               const float force = -2.0f * S.strength_f * S.stiffness_f * e * (1.0f - e);
