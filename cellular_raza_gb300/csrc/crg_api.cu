@@ -45,6 +45,8 @@ struct crg_ctx {
   int32_t *status = nullptr;
   int64_t *step_ctr = nullptr;
   double *dbg_force = nullptr;
+  double *frc = nullptr;     // rods: interaction force between the two step kernels
+  uint32_t *work = nullptr;  // rods: queue counter of the force kernel
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
   uint32_t snap_agents = 0;
@@ -218,7 +220,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->staging, c->snap};
+                  c->step_ctr, c->dbg_force, c->frc, c->work, c->staging, c->snap};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (c->h_status) cudaFreeHost(c->h_status);
@@ -249,6 +251,10 @@ int32_t allocate(crg_ctx *c) {
   A(status, 8);
   A(step_ctr, 1);
   A(staging, cap * nc);
+  if (c->kind == CRG_KIND_ROD) {
+    A(frc, cap * nc);
+    A(work, 1);
+  }
   if (c->order > 1) {
     A(hist, cap * nc * 2);
     A(nhist, cap * nc * 2);
@@ -356,6 +362,8 @@ PackArgs pack_args(crg_ctx *c) {
   P.status = c->status;
   P.step_ctr = c->step_ctr;
   P.dbg_force = c->dbg_force;
+  P.frc = c->frc;
+  P.work = c->work;
   P.prefilter = c->prefilter;
   P.variant = c->variant;
   return P;
@@ -704,7 +712,7 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   };
   std::vector<Shape> shapes;
   if (c->kind == CRG_KIND_ROD) {
-    shapes = {{0, 0}, {1, 64}, {2, 0}};
+    shapes = {{0, 0}, {3, 0}, {1, 64}, {2, 0}};
   } else if (c->precision == CRG_PREC_F64) {
     shapes = {{0, 0}, {1, 64}, {1, 128}, {1, 256}};
   } else {
@@ -983,7 +991,7 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
       break;
     case CRG_OPT_PROFILE: c->profile = value ? 1 : 0; break;
     case CRG_OPT_KERNEL_VARIANT:
-      if (value < 0 || value > 2) return CRG_EINVAL;
+      if (value < 0 || value > 3) return CRG_EINVAL;
       c->variant = (int)value;
       break;
     case CRG_OPT_DEBUG_FORCES:

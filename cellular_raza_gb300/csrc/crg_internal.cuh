@@ -75,6 +75,8 @@ struct PackArgs {
   int32_t *status;
   const int64_t *step_ctr;
   double *dbg_force;  // optional [nc][cap]: interaction force of this step
+  double *frc;        // rods: [nc][cap] interaction force, force kernel -> update kernel
+  uint32_t *work;     // rods: queue counter of the force kernel (zeroed before each launch)
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
   int32_t variant;    // force kernel: 0 warp-packed (default), 1 thread per agent
 };

@@ -752,6 +752,163 @@ __device__ __forceinline__ int nth_set_bit64(uint64_t m, int n) {  // n-th set b
   return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - clo + 1);
 }
 
+// One warp-wide pass step.  Every lane brings one pass (own_a(b) or ext_a(b) of its rod a
+// and candidate b; is_ext says which) with the bitmask of its FP32-surviving vertex/segment
+// pairs.  The warp evaluates all survivors in FP64 with every lane busy (results to shared
+// memory), folds them into the rows of each lane's pass matrix M in the reference's
+// (vertex, segment) order -- each non-empty (lane, row) is one unit of work -- and each lane
+// adds M / 2 to acc.  Lanes without a pass bring mask = 0.
+template <int D, int NV>
+__device__ __forceinline__ void eval_fold_pass(const PackArgs &P, double *sRes, int lane,
+                                               uint64_t mask, bool is_ext, uint32_t a,
+                                               uint32_t b, uint32_t sim, double *acc) {
+  constexpr int NE = NV - 1, NP = NV * NE, R = D + 1;
+  double *sRow = sRes + NP * R * 32;  // [NV][D][32]: folded rows of the pass matrix
+  const int64_t cap = P.cap;
+  const int cnt = __popcll(mask);
+
+  // ---- evaluate every survivor of the warp in FP64 ---------------------------------
+  int incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  const int excl = incl - cnt;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  for (int base = 0; base < total; base += 32) {
+    const int j = base + lane;
+    int l = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int cand = l + step;
+      const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+      if (cand < 32 && e <= j) l = cand;
+    }
+    const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+    const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
+    const uint32_t b_l = __shfl_sync(0xffffffffu, b, l);
+    const uint32_t a_l = __shfl_sync(0xffffffffu, a, l);
+    const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
+    const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
+    const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+    if (j < total) {
+      const int k = j - ex_l;
+      const int vs = nth_set_bit64(((uint64_t)mhi << 32) | mlo, k);
+      const int vx = vs / NE, sy = vs - vx * NE;
+      const uint32_t pr = ext_l ? b_l : a_l, sr = ext_l ? a_l : b_l;
+      double p[D], l0[D], l1[D], q[D], t, f[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        p[c] = P.pos[(vx * D + c) * cap + pr];
+        l0[c] = P.pos[(sy * D + c) * cap + sr];
+        l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
+      }
+      nearest_point_f64<D>(p, l0, l1, q, t);
+      if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
+      }
+#pragma unroll
+      for (int c = 0; c < D; ++c) sRes[(k * R + c) * 32 + l] = f[c];
+      sRes[(k * R + D) * 32 + l] = t;
+    }
+  }
+  __syncwarp();
+
+  // ---- fold the results row by row: each non-empty (rod, row) is one unit ----------
+  // Row r of the pass matrix M collects, in the reference's (vertex, segment) order,
+  //   own pass: f of items (r, 0..NE-1);
+  //   ext pass: for each vertex vx, -f*t of item (vx, r-1) then -f*(1-t) of item (vx, r).
+  uint32_t rowmask = 0;
+#pragma unroll
+  for (int r = 0; r < NV; ++r) {
+    bool has = false;
+    if (!is_ext) {
+      has = ((mask >> (r * NE)) & ((1ull << NE) - 1ull)) != 0ull;
+    } else {
+#pragma unroll
+      for (int vx = 0; vx < NV; ++vx) {
+        if (r >= 1) has |= ((mask >> (vx * NE + r - 1)) & 1ull) != 0ull;
+        if (r < NE) has |= ((mask >> (vx * NE + r)) & 1ull) != 0ull;
+      }
+    }
+    if (has) rowmask |= 1u << r;
+  }
+  const int rcnt = __popc(rowmask);
+  int rincl = rcnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, rincl, off);
+    if (lane >= off) rincl += y;
+  }
+  const int rexcl = rincl - rcnt;
+  const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
+  for (int base = 0; base < rtotal; base += 32) {
+    const int j = base + lane;
+    int l = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int cand = l + step;
+      const int e = __shfl_sync(0xffffffffu, rexcl, cand & 31);
+      if (cand < 32 && e <= j) l = cand;
+    }
+    const int ex_l = __shfl_sync(0xffffffffu, rexcl, l);
+    const uint32_t rows_l = __shfl_sync(0xffffffffu, rowmask, l);
+    const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
+    const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
+    const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+    if (j < rtotal) {
+      const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
+      const int r = (int)__fns(rows_l, 0, j - ex_l + 1);
+      double m[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) m[c] = 0.0;
+      if (!ext_l) {
+#pragma unroll
+        for (int sy = 0; sy < NE; ++sy) {
+          const int vs = r * NE + sy;
+          if (!((m_l >> vs) & 1ull)) continue;
+          const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
+#pragma unroll
+          for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(slot * R + c) * 32 + l]);
+        }
+      } else {
+#pragma unroll
+        for (int vx = 0; vx < NV; ++vx) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int sy = r - 1 + h;  // h = 0: item (vx, r-1) weight t; h = 1: (vx, r) weight 1-t
+            if (sy < 0 || sy >= NE) continue;
+            const int vs = vx * NE + sy;
+            if (!((m_l >> vs) & 1ull)) continue;
+            const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
+            const double t = sRes[(slot * R + D) * 32 + l];
+            const double wgt = h == 0 ? t : dsub(1.0, t);
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+              const double fe = -sRes[(slot * R + c) * 32 + l];
+              m[c] = dadd(m[c], dmul(fe, wgt));
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < D; ++c) sRow[(r * D + c) * 32 + l] = m[c];
+    }
+  }
+  __syncwarp();
+  // acc += M / 2 for the rows this lane's pass touched (other rows of M are zero)
+#pragma unroll
+  for (int r = 0; r < NV; ++r)
+    if ((rowmask >> r) & 1u) {
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+        acc[r * D + c] = dadd(acc[r * D + c], dmul(sRow[(r * D + c) * 32 + lane], 0.5));
+    }
+  __syncwarp();
+}
+
 template <int D, int NV>
 __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
   constexpr int NC = NV * D, NE = NV - 1, NP = NV * NE, R = D + 1;
@@ -894,148 +1051,7 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
           if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
         }
     }
-    const int cnt = __popcll(mask);
-
-    // ---- evaluate every survivor of the warp in FP64 ---------------------------------
-    int incl = cnt;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += y;
-    }
-    const int excl = incl - cnt;
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    for (int base = 0; base < total; base += 32) {
-      const int j = base + lane;
-      int l = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int cand = l + step;
-        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
-        if (cand < 32 && e <= j) l = cand;
-      }
-      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
-      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
-      const uint32_t b_l = __shfl_sync(0xffffffffu, cur_b, l);
-      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
-      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
-      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
-      if (j < total) {
-        const int k = j - ex_l;
-        const int vs = nth_set_bit64(((uint64_t)mhi << 32) | mlo, k);
-        const int vx = vs / NE, sy = vs - vx * NE;
-        const uint32_t a = warp_base + l;
-        const uint32_t pr = ext_l ? b_l : a, sr = ext_l ? a : b_l;
-        double p[D], l0[D], l1[D], q[D], t, f[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) {
-          p[c] = P.pos[(vx * D + c) * cap + pr];
-          l0[c] = P.pos[(sy * D + c) * cap + sr];
-          l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
-        }
-        nearest_point_f64<D>(p, l0, l1, q, t);
-        if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
-#pragma unroll
-          for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
-        }
-#pragma unroll
-        for (int c = 0; c < D; ++c) sRes[(k * R + c) * 32 + l] = f[c];
-        sRes[(k * R + D) * 32 + l] = t;
-      }
-    }
-    __syncwarp();
-
-    // ---- fold the results row by row: each non-empty (rod, row) is one unit ----------
-    // Row r of the pass matrix M collects, in the reference's (vertex, segment) order,
-    //   own pass: f of items (r, 0..NE-1);
-    //   ext pass: for each vertex vx, -f*t of item (vx, r-1) then -f*(1-t) of item (vx, r).
-    uint32_t rowmask = 0;
-#pragma unroll
-    for (int r = 0; r < NV; ++r) {
-      bool has = false;
-      if (!is_ext) {
-        has = ((mask >> (r * NE)) & ((1ull << NE) - 1ull)) != 0ull;
-      } else {
-#pragma unroll
-        for (int vx = 0; vx < NV; ++vx) {
-          if (r >= 1) has |= ((mask >> (vx * NE + r - 1)) & 1ull) != 0ull;
-          if (r < NE) has |= ((mask >> (vx * NE + r)) & 1ull) != 0ull;
-        }
-      }
-      if (has) rowmask |= 1u << r;
-    }
-    const int rcnt = __popc(rowmask);
-    int rincl = rcnt;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, rincl, off);
-      if (lane >= off) rincl += y;
-    }
-    const int rexcl = rincl - rcnt;
-    const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
-    for (int base = 0; base < rtotal; base += 32) {
-      const int j = base + lane;
-      int l = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int cand = l + step;
-        const int e = __shfl_sync(0xffffffffu, rexcl, cand & 31);
-        if (cand < 32 && e <= j) l = cand;
-      }
-      const int ex_l = __shfl_sync(0xffffffffu, rexcl, l);
-      const uint32_t rows_l = __shfl_sync(0xffffffffu, rowmask, l);
-      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
-      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
-      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
-      if (j < rtotal) {
-        const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
-        const int r = (int)__fns(rows_l, 0, j - ex_l + 1);
-        double m[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) m[c] = 0.0;
-        if (!ext_l) {
-#pragma unroll
-          for (int sy = 0; sy < NE; ++sy) {
-            const int vs = r * NE + sy;
-            if (!((m_l >> vs) & 1ull)) continue;
-            const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
-#pragma unroll
-            for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(slot * R + c) * 32 + l]);
-          }
-        } else {
-#pragma unroll
-          for (int vx = 0; vx < NV; ++vx) {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int sy = r - 1 + h;  // h = 0: item (vx, r-1) weight t; h = 1: (vx, r) weight 1-t
-              if (sy < 0 || sy >= NE) continue;
-              const int vs = vx * NE + sy;
-              if (!((m_l >> vs) & 1ull)) continue;
-              const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
-              const double t = sRes[(slot * R + D) * 32 + l];
-              const double wgt = h == 0 ? t : dsub(1.0, t);
-#pragma unroll
-              for (int c = 0; c < D; ++c) {
-                const double fe = -sRes[(slot * R + c) * 32 + l];
-                m[c] = dadd(m[c], dmul(fe, wgt));
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < D; ++c) sRow[(r * D + c) * 32 + l] = m[c];
-      }
-    }
-    __syncwarp();
-    // acc += M / 2 for the rows this lane's pass touched (other rows of M are zero)
-#pragma unroll
-    for (int r = 0; r < NV; ++r)
-      if ((rowmask >> r) & 1u) {
-#pragma unroll
-        for (int c = 0; c < D; ++c)
-          acc[r * D + c] = dadd(acc[r * D + c], dmul(sRow[(r * D + c) * 32 + lane], 0.5));
-      }
-    __syncwarp();
+    eval_fold_pass<D, NV>(P, sRes, lane, mask, is_ext, i, cur_b, sim, acc);
   }
   if (!valid) return;
   if (frozen) {
@@ -1045,6 +1061,216 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
   double pa[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
+  rod_update<D, NV>(P, S, i, key, pa, acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// Queue-fed pass-synchronous variant (default).  The per-pass work is that of k_rods_pass,
+// but a lane whose rod has no passes left stores the rod's interaction force to frc and
+// takes the next rod from a global counter (one atomic per warp and refill), so every lane
+// of a warp carries a pass until the queue drains instead of idling while the busiest rod of
+// a fixed group of 32 finishes.  The grid is sized to the resident warps of the device.
+// k_rods_update then applies mechanics, solver, boundary and next key per rod.  Per rod the
+// items, their arithmetic and their order are those of k_rods_step: identical bits.
+// ---------------------------------------------------------------------------------------
+template <int D, int NV>
+__global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
+  constexpr int NC = NV * D, NE = NV - 1;
+  extern __shared__ double sRes[];
+  const int lane = threadIdx.x;
+  const int64_t cap = P.cap;
+  const int64_t step = *P.step_ctr;
+  const float inf = __int_as_float(0x7f800000);
+  // the rod of this lane and its candidate cursor
+  bool have = false, drained = false;
+  uint32_t i = 0, sim = 0, v = 0, sub_v = 0;
+  const SimDev *S = P.sims;
+  int idx[D];
+  float oa[NC], amin[D], amax[D];
+  bool a_nan = false;
+  float thr2 = inf, thr = inf;
+  double acc[NC];
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
+  int n_box = 0, o_box = 0;
+  uint32_t b_next = 0, b_end = 0, cur_b = 0;
+  bool same = false, twice = false, ext_first = false;
+  int n_pass = 0, pass = 0;
+  float kd[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    idx[c] = 0;
+    kd[c] = 0.f;
+  }
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+
+  while (true) {
+    // ---- give every lane its next pass, refilling finished lanes from the queue -------
+    while (true) {
+      while (have && pass >= n_pass) {
+        if (b_next >= b_end) {
+          if (o_box >= n_box) {  // rod finished: hand its force to the update kernel
+#pragma unroll
+            for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = acc[k];
+            have = false;
+            break;
+          }
+          const int j2 = lo[2] + o_box % nb[2];
+          const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
+          const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
+          ++o_box;
+          const uint32_t w = (D == 3) ? ((uint32_t)j0 * S->nvox[1] + j1) * S->nvox[2] + j2
+                                      : (uint32_t)j0 * S->nvox[1] + j1;
+          same = (w == v);
+          twice = same || S->weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(*S, w) != sub_v;
+          kd[0] = (float)(j0 - idx[0]) * S->dxf[0];
+          kd[1] = (float)(j1 - idx[1]) * S->dxf[1];
+          if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S->dxf[D - 1];
+          b_next = P.start[S->voxel_off + w];
+          b_end = P.start[S->voxel_off + w + 1];
+          if (b_next > b_end || b_end > P.n_agents) {
+            invariant_failed(P.status, kSiteForceRange, S->voxel_off + w);
+            b_end = b_next;
+          }
+          continue;
+        }
+        const uint32_t b = b_next++;
+        if (b == i) continue;
+        float bmin[D], bmax[D];
+        bool b_nan = false;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+          const float o = P.off[k * cap + b] + kd[k % D];
+          b_nan |= !(o == o);
+          if (k < D) {
+            bmin[k] = o;
+            bmax[k] = o;
+          } else {
+            bmin[k % D] = fminf(bmin[k % D], o);
+            bmax[k % D] = fmaxf(bmax[k % D], o);
+          }
+        }
+        bool far = false;
+        if (!a_nan && !b_nan) {
+#pragma unroll
+          for (int c = 0; c < D; ++c)
+            far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+        }
+        if (far) continue;
+        cur_b = b;
+        ext_first = same && (b < i);
+        n_pass = twice ? 2 : 1;
+        pass = 0;
+      }
+      const bool need = !have && !drained;
+      const uint32_t want = __ballot_sync(0xffffffffu, need);
+      if (!want) break;
+      const int leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(P.work, (uint32_t)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (need) {
+        const uint32_t t = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
+        if (t >= P.n_agents) {
+          drained = true;
+        } else {
+          i = t;
+          sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+          S = P.sims + sim;
+          if (step < S->stop_step) {  // frozen rods are copied by the update kernel
+            uint32_t key = P.key[i];
+            if (key - S->voxel_off >= S->n_vox) {
+              invariant_failed(P.status, kSiteForceKey, i);
+              key = S->voxel_off;
+            }
+            v = key - S->voxel_off;
+            unravel<D>(*S, v, idx);
+            a_nan = false;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+              oa[k] = P.off[k * cap + i];
+              a_nan |= !(oa[k] == oa[k]);
+              if (k < D) {
+                amin[k] = oa[k];
+                amax[k] = oa[k];
+              } else {
+                amin[k % D] = fminf(amin[k % D], oa[k]);
+                amax[k % D] = fmaxf(amax[k % D], oa[k]);
+              }
+            }
+            sub_v = subdomain_of(*S, v);
+            thr2 = P.prefilter ? S->filt_thr2 : inf;
+            thr = P.prefilter ? sqrtf(S->filt_thr2) : inf;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+              lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+              const int hi = idx[c] + 1 < S->nvox[c] ? idx[c] + 1 : S->nvox[c] - 1;
+              nb[c] = hi - lo[c] + 1;
+            }
+            n_box = nb[0] * nb[1] * nb[2];
+            o_box = 0;
+            b_next = b_end = 0;
+            n_pass = pass = 0;
+            have = true;
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, have)) break;
+    const bool is_ext = have && ((pass == 0) == ext_first);
+    ++pass;
+
+    // ---- scan the vertex/segment pairs of this pass (uniform loop) -------------------
+    uint64_t mask = 0;
+    if (have) {
+      float ob[NC];
+#pragma unroll
+      for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + cur_b] + kd[k % D];
+#pragma unroll
+      for (int vx = 0; vx < NV; ++vx)
+#pragma unroll
+        for (int sy = 0; sy < NE; ++sy) {
+          const float *pp = is_ext ? &ob[vx * D] : &oa[vx * D];
+          const float *s0 = is_ext ? &oa[sy * D] : &ob[sy * D];
+          const float *s1 = is_ext ? &oa[(sy + 1) * D] : &ob[(sy + 1) * D];
+          float p32[D], l0[D], l1[D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            p32[c] = pp[c];
+            l0[c] = s0[c];
+            l1[c] = s1[c];
+          }
+          if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
+        }
+    }
+    eval_fold_pass<D, NV>(P, sRes, lane, mask, is_ext, i, cur_b, sim, acc);
+  }
+}
+
+// Mechanics, solver, boundary and next key of every rod from the interaction force that
+// k_rods_queue stored in frc (frozen simulations copy their state).
+template <int D, int NV>
+__global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
+  constexpr int NC = NV * D;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n_agents) return;
+  const int64_t cap = P.cap;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) key = S.voxel_off;  // recorded by the force kernel
+  if (*P.step_ctr >= S.stop_step) {
+    frozen_copy(P, i, key, NC);
+    return;
+  }
+  double pa[NC], acc[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    pa[k] = P.pos[k * cap + i];
+    acc[k] = P.frc[k * cap + i];
+  }
   rod_update<D, NV>(P, S, i, key, pa, acc);
 }
 
@@ -1097,6 +1323,9 @@ __global__ void k_rod_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_inte
   hash[i] = h;
 }
 
+// Resident warps of k_rods_queue on the current device, [D - 2][NV] (set by prepare_rods).
+unsigned g_queue_warps[2][9] = {};
+
 template <int D, int NV>
 constexpr size_t pass_smem_bytes() {
   return sizeof(double) * ((size_t)(NV * (NV - 1)) * (D + 1) + (size_t)NV * D) * 32;
@@ -1117,14 +1346,33 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st) {
     k_rods_packed<D, NV, W, K><<<grid, W * 32, 0, st>>>(P);
     return;
   }
-  const unsigned grid = (P.n_agents + 31) / 32;
-  k_rods_pass<D, NV><<<grid, 32, pass_smem_bytes<D, NV>(), st>>>(P);
+  const unsigned warps = (P.n_agents + 31) / 32;
+  if (P.variant == 3) {  // pass-synchronous kernel over fixed groups of 32 rods
+    k_rods_pass<D, NV><<<warps, 32, pass_smem_bytes<D, NV>(), st>>>(P);
+    return;
+  }
+  const unsigned resident = g_queue_warps[D - 2][NV];
+  const unsigned grid = (resident && resident < warps) ? resident : warps;
+  cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
+  k_rods_queue<D, NV><<<grid, 32, pass_smem_bytes<D, NV>(), st>>>(P);
+  k_rods_update<D, NV><<<(P.n_agents + 127) / 128, 128, 0, st>>>(P);
 }
 
 template <int D, int NV>
 cudaError_t prepare_t() {
-  return cudaFuncSetAttribute(k_rods_pass<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)pass_smem_bytes<D, NV>());
+  const int smem = (int)pass_smem_bytes<D, NV>();
+  cudaError_t e = cudaFuncSetAttribute(k_rods_pass<D, NV>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_rods_queue<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+  int dev = 0, sms = 0, per_sm = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_queue<D, NV>, 32, smem);
+  if (e == cudaSuccess) g_queue_warps[D - 2][NV] = (unsigned)(sms * per_sm);
+  return e;
 }
 
 template <int D>

@@ -216,9 +216,11 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * of the ids array (same layout as crg_download's ids).  Capture must have been enabled
  * with crg_set_option(ctx, CRG_OPT_DEBUG_FORCES, 1) before that step. */
 #define CRG_OPT_DEBUG_FORCES 5
-/* Force kernel: 0 (default) warp-packed FP64 evaluation, one pass per lane and round;
- * 1 one thread per agent; 2 (rods) warp-packed with per-lane slot queues.  All produce
- * identical results; 1 is kept as the simple reference formulation. */
+/* Force kernel: 0 (default) warp-packed FP64 evaluation, one pass per lane and round
+ * (rods: lanes refill from a global rod queue, separate update kernel); 1 one thread per
+ * agent; 2 (rods) warp-packed with per-lane slot queues; 3 (rods) warp-packed over fixed
+ * groups of 32 rods.  All produce identical results; 1 is kept as the simple reference
+ * formulation. */
 #define CRG_OPT_KERNEL_VARIANT 6
 int32_t crg_debug_forces(crg_ctx *ctx, double *force, uint64_t *ids);
 
