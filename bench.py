@@ -464,7 +464,8 @@ def crg_arm(args):
                 "frac": achieved / fp64_peak if fp64_peak else None,
                 "traffic": committed_traffic(kernel_key),
                 "peak_source": "measured DFMA microbenchmark (crg_measure_fma_peaks) on this GPU",
-                "kernel": "k_rods_step" if w.model.kind == "rod" else "k_spheres_step",
+                "kernel": ("k_rods_queue + k_rods_update" if w.model.kind == "rod"
+                           else "k_spheres_pass"),
                 "force_ms_per_launch": force_ms, "sort_ms_per_step": sort_ms,
                 "algorithmic_flop_per_launch": flops}
     # the sort kernels are HBM-bound: algorithmic bytes per step

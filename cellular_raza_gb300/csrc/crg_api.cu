@@ -163,6 +163,9 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.stiffness = m.stiffness;
   S.cutoff = m.cutoff;
   S.strength = m.strength;
+  S.mrs_r = m.radius + m.radius;
+  S.mrs_k = (-2.0 * m.strength) * m.stiffness;
+  S.mrs_nstiff = -m.stiffness;
   S.dt = m.dt;
   S.order = m.solver_order;
   S.stop_step = INT64_MAX;
@@ -402,6 +405,11 @@ SortArgs sort_args(crg_ctx *c, int initial) {
   return A;
 }
 
+// Kernels one launch_force issues: the default rod path runs a force and an update kernel.
+int force_kernel_count(const crg_ctx *c) {
+  return (c->kind == CRG_KIND_ROD && c->variant == 0) ? 2 : 1;
+}
+
 void launch_force(crg_ctx *c) {
   PackArgs P = pack_args(c);
   if (c->kind == CRG_KIND_SPHERE)
@@ -602,7 +610,7 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
         cudaEventElapsedTime(&b, ev[1], ev[2]);
         c->prof_ms[0] += a;
         c->prof_ms[1] += b;
-        c->prof_ms[2] += 1 + crg::sort_kernel_count();
+        c->prof_ms[2] += force_kernel_count(c) + crg::sort_kernel_count();
       }
       left -= k;
     } else if (chunk > 0 && left >= chunk) {

@@ -35,6 +35,9 @@ struct SimDev {
   double mass, damping;
   double spring_tension, rigidity, spring_length;
   double radius, stiffness, cutoff, strength;
+  // Morse terms that do not depend on the pair, each rounded exactly as the per-pair
+  // expression rounds them: radius + radius, (-2 * strength) * stiffness, -stiffness.
+  double mrs_r, mrs_k, mrs_nstiff;
   double dt;
   float radius_f, stiffness_f, cutoff_f, strength_f;
   float filt_thr2;  // squared FP32 prefilter threshold (cutoff + conservative margin)^2

@@ -60,9 +60,8 @@ __device__ __forceinline__ bool morse_full_f64(const double *own, const double *
   for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
   const double dist = __dsqrt_rn(n2);
   if (dist > S.cutoff || dist == 0.0) return false;
-  const double r = dadd(S.radius, S.radius);
-  const double e = exp(dmul(-S.stiffness, dsub(dist, r)));
-  const double force = dmul(dmul(dmul(dmul(-2.0, S.strength), S.stiffness), e), dsub(1.0, e));
+  const double e = exp(dmul(S.mrs_nstiff, dsub(dist, S.mrs_r)));
+  const double force = dmul(dmul(S.mrs_k, e), dsub(1.0, e));
 #pragma unroll
   for (int c = 0; c < D; ++c) f[c] = dmul(ddiv(z[c], dist), force);
   return true;
@@ -909,11 +908,192 @@ __device__ __forceinline__ void eval_fold_pass(const PackArgs &P, double *sRes, 
   __syncwarp();
 }
 
+// x * 0.5, exactly as the FP64 multiply rounds it: an exponent decrement for normal x above
+// the lowest binade (exact there), the multiply itself for zeros, subnormals, the lowest
+// binade, infinities and NaN.
+__device__ __forceinline__ double half_exact(double x) {
+  const long long bits = __double_as_longlong(x);
+  const long long e = (bits >> 52) & 0x7ff;
+  if (e > 1 && e < 0x7ff) return __longlong_as_double(bits - (1ll << 52));
+  return dmul(x, 0.5);
+}
+
+// Items of one chunk of the queue kernel's result buffer.  Every lane's items fit (at most
+// NV * (NV - 1) <= 56), so a round needs more than one chunk only when the warp's passes
+// together have more survivors.
+constexpr int kQueueCap = 128;
+
+template <int D, int NV>
+constexpr size_t queue_smem_bytes() {
+  return sizeof(double) * ((size_t)2 * D * kQueueCap + (size_t)NV * D * 32);
+}
+
+// The pass step of k_rods_queue.  Like eval_fold_pass, but
+//  * results go to a compacted buffer sRes [2D][kQueueCap] in chunks of whole lanes;
+//    an item stores f (own pass) or -f*t (ext pass) in the first D entries and -f*(1-t) in
+//    the last D, so the weights are applied while all lanes evaluate;
+//  * a (lane, row) unit sums only its own items (loops over set bits) and adds M / 2 to the
+//    lane's accumulator sAcc [NC][32] itself.
+// Per row the sums run over the same items in the same order as eval_fold_pass.
+template <int D, int NV>
+__device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes, double *sAcc,
+                                                int lane, uint64_t mask, bool is_ext,
+                                                uint32_t a, uint32_t b, uint32_t sim) {
+  constexpr int NE = NV - 1, CAP = kQueueCap;
+  const int64_t cap = P.cap;
+  const int cnt = __popcll(mask);
+  int incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  const int excl = incl - cnt;
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  for (int cs = 0; cs < total;) {
+    // ---- the lanes of this chunk: whole lanes whose items fit from cs on ----------------
+    const bool in = excl >= cs && incl <= cs + CAP;
+    const int last = 31 - __clz(__ballot_sync(0xffffffffu, in));
+    const int ce = __shfl_sync(0xffffffffu, incl, last);
+
+    // ---- evaluate the items [cs, ce) in FP64, every lane busy ---------------------------
+    for (int base = cs; base < ce; base += 32) {
+      const int j = base + lane;
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+        if (cand < 32 && e <= j) l = cand;
+      }
+      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
+      const uint32_t b_l = __shfl_sync(0xffffffffu, b, l);
+      const uint32_t a_l = __shfl_sync(0xffffffffu, a, l);
+      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
+      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
+      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+      if (j < ce) {
+        const int vs = nth_set_bit64(((uint64_t)mhi << 32) | mlo, j - ex_l);
+        const int vx = vs / NE, sy = vs - vx * NE;
+        const uint32_t pr = ext_l ? b_l : a_l, sr = ext_l ? a_l : b_l;
+        double p[D], l0[D], l1[D], q[D], t, f[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          p[c] = P.pos[(vx * D + c) * cap + pr];
+          l0[c] = P.pos[(sy * D + c) * cap + sr];
+          l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
+        }
+        nearest_point_f64<D>(p, l0, l1, q, t);
+        if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
+#pragma unroll
+          for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
+        }
+        const double omt = dsub(1.0, t);
+        const int jj = j - cs;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          const double fe = -f[c];
+          sRes[c * CAP + jj] = ext_l ? dmul(fe, t) : f[c];
+          sRes[(D + c) * CAP + jj] = dmul(fe, omt);
+        }
+      }
+    }
+    __syncwarp();
+
+    // ---- fold: each non-empty (lane, row) of the chunk is one unit --------------------
+    // Row r of the pass matrix M collects, in the reference's (vertex, segment) order,
+    //   own pass: f of items (r, 0..NE-1);
+    //   ext pass: for each vertex vx, -f*t of item (vx, r-1) then -f*(1-t) of item (vx, r).
+    uint32_t rowmask = 0;
+    if (in) {
+#pragma unroll
+      for (int r = 0; r < NV; ++r) {
+        bool has = false;
+        if (!is_ext) {
+          has = ((mask >> (r * NE)) & ((1ull << NE) - 1ull)) != 0ull;
+        } else {
+#pragma unroll
+          for (int vx = 0; vx < NV; ++vx) {
+            if (r >= 1) has |= ((mask >> (vx * NE + r - 1)) & 1ull) != 0ull;
+            if (r < NE) has |= ((mask >> (vx * NE + r)) & 1ull) != 0ull;
+          }
+        }
+        if (has) rowmask |= 1u << r;
+      }
+    }
+    const int rcnt = __popc(rowmask);
+    int rincl = rcnt;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, rincl, off);
+      if (lane >= off) rincl += y;
+    }
+    const int rexcl = rincl - rcnt;
+    const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
+    for (int base = 0; base < rtotal; base += 32) {
+      const int j = base + lane;
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int cand = l + step;
+        const int e = __shfl_sync(0xffffffffu, rexcl, cand & 31);
+        if (cand < 32 && e <= j) l = cand;
+      }
+      const int rex_l = __shfl_sync(0xffffffffu, rexcl, l);
+      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+      const uint32_t rows_l = __shfl_sync(0xffffffffu, rowmask, l);
+      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
+      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
+      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+      if (j < rtotal) {
+        const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
+        const int r = (int)__fns(rows_l, 0, j - rex_l + 1);
+        const int slot0 = ex_l - cs;  // the lane's first item in the chunk buffer
+        double m[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) m[c] = 0.0;
+        if (!ext_l) {
+          // items (r, sy) are consecutive bits, hence consecutive slots
+          const int first = slot0 + __popcll(m_l & ((1ull << (r * NE)) - 1ull));
+          const int n = __popcll((m_l >> (r * NE)) & ((1ull << NE) - 1ull));
+          for (int k = 0; k < n; ++k) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[c * CAP + first + k]);
+          }
+        } else {
+          uint32_t em = 0;  // bit 2 vx + h: item (vx, r - 1 + h) contributes to row r
+#pragma unroll
+          for (int vx = 0; vx < NV; ++vx) {
+            if (r >= 1) em |= (uint32_t)((m_l >> (vx * NE + r - 1)) & 1ull) << (2 * vx);
+            if (r < NE) em |= (uint32_t)((m_l >> (vx * NE + r)) & 1ull) << (2 * vx + 1);
+          }
+          while (em) {
+            const int k = __ffs(em) - 1;
+            em &= em - 1u;
+            const int h = k & 1;
+            const int vs = (k >> 1) * NE + r - 1 + h;
+            const int slot = slot0 + __popcll(m_l & ((1ull << vs) - 1ull));
+#pragma unroll
+            for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(h * D + c) * CAP + slot]);
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          double &acc = sAcc[(r * D + c) * 32 + l];
+          acc = dadd(acc, half_exact(m[c]));
+        }
+      }
+    }
+    __syncwarp();
+    cs = ce;
+  }
+}
+
 template <int D, int NV>
 __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
-  constexpr int NC = NV * D, NE = NV - 1, NP = NV * NE, R = D + 1;
-  extern __shared__ double sRes[];  // [NP][R][32]: f (and t for ext items), then sRow
-  double *sRow = sRes + NP * R * 32;  // [NV][D][32]: folded rows of the pass matrix
+  constexpr int NC = NV * D, NE = NV - 1;
+  extern __shared__ double sRes[];  // [NP][D + 1][32] item results, then [NV][D][32] rows
   const int lane = threadIdx.x;
   const uint32_t warp_base = blockIdx.x * 32;
   const uint32_t i = warp_base + lane;
@@ -1076,7 +1256,8 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
 template <int D, int NV>
 __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
   constexpr int NC = NV * D, NE = NV - 1;
-  extern __shared__ double sRes[];
+  extern __shared__ double sRes[];             // [2D][kQueueCap]: item results
+  double *sAcc = sRes + 2 * D * kQueueCap;     // [NC][32]: force accumulated on each lane's rod
   const int lane = threadIdx.x;
   const int64_t cap = P.cap;
   const int64_t step = *P.step_ctr;
@@ -1089,7 +1270,6 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
   float oa[NC], amin[D], amax[D];
   bool a_nan = false;
   float thr2 = inf, thr = inf;
-  double acc[NC];
   int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
   int n_box = 0, o_box = 0;
   uint32_t b_next = 0, b_end = 0, cur_b = 0;
@@ -1101,8 +1281,6 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
     idx[c] = 0;
     kd[c] = 0.f;
   }
-#pragma unroll
-  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
 
   while (true) {
     // ---- give every lane its next pass, refilling finished lanes from the queue -------
@@ -1111,7 +1289,7 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
         if (b_next >= b_end) {
           if (o_box >= n_box) {  // rod finished: hand its force to the update kernel
 #pragma unroll
-            for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = acc[k];
+            for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = sAcc[k * 32 + lane];
             have = false;
             break;
           }
@@ -1202,7 +1380,7 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
             thr2 = P.prefilter ? S->filt_thr2 : inf;
             thr = P.prefilter ? sqrtf(S->filt_thr2) : inf;
 #pragma unroll
-            for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+            for (int k = 0; k < NC; ++k) sAcc[k * 32 + lane] = 0.0;
 #pragma unroll
             for (int c = 0; c < D; ++c) {
               lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
@@ -1245,7 +1423,7 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
           if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
         }
     }
-    eval_fold_pass<D, NV>(P, sRes, lane, mask, is_ext, i, cur_b, sim, acc);
+    eval_fold_queue<D, NV>(P, sRes, sAcc, lane, mask, is_ext, i, cur_b, sim);
   }
 }
 
@@ -1354,7 +1532,7 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st) {
   const unsigned resident = g_queue_warps[D - 2][NV];
   const unsigned grid = (resident && resident < warps) ? resident : warps;
   cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
-  k_rods_queue<D, NV><<<grid, 32, pass_smem_bytes<D, NV>(), st>>>(P);
+  k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);
   k_rods_update<D, NV><<<(P.n_agents + 127) / 128, 128, 0, st>>>(P);
 }
 
@@ -1363,14 +1541,15 @@ cudaError_t prepare_t() {
   const int smem = (int)pass_smem_bytes<D, NV>();
   cudaError_t e = cudaFuncSetAttribute(k_rods_pass<D, NV>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const int qsmem = (int)queue_smem_bytes<D, NV>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_rods_queue<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
+                             qsmem);
   int dev = 0, sms = 0, per_sm = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_queue<D, NV>, 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_queue<D, NV>, 32, qsmem);
   if (e == cudaSuccess) g_queue_warps[D - 2][NV] = (unsigned)(sms * per_sm);
   return e;
 }
