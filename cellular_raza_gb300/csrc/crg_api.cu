@@ -166,6 +166,12 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.mrs_r = m.radius + m.radius;
   S.mrs_k = (-2.0 * m.strength) * m.stiffness;
   S.mrs_nstiff = -m.stiffness;
+  if (std::isnan(m.cutoff))
+    S.cutoff_bits = INT64_MAX;  // d > NaN never holds
+  else if (!(m.cutoff > 0.0))
+    S.cutoff_bits = -1;  // every d > 0 exceeds a cutoff <= 0
+  else
+    std::memcpy(&S.cutoff_bits, &m.cutoff, sizeof(double));
   S.dt = m.dt;
   S.order = m.solver_order;
   S.stop_step = INT64_MAX;

@@ -38,6 +38,9 @@ struct SimDev {
   // Morse terms that do not depend on the pair, each rounded exactly as the per-pair
   // expression rounds them: radius + radius, (-2 * strength) * stiffness, -stiffness.
   double mrs_r, mrs_k, mrs_nstiff;
+  // cutoff as an integer threshold on the bit pattern of a distance d >= 0 (not NaN):
+  // d > cutoff exactly when bits(d) > cutoff_bits.
+  int64_t cutoff_bits;
   double dt;
   float radius_f, stiffness_f, cutoff_f, strength_f;
   float filt_thr2;  // squared FP32 prefilter threshold (cutoff + conservative margin)^2

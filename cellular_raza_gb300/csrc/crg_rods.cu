@@ -23,6 +23,19 @@ namespace crg {
 
 namespace {
 
+// FP64 comparisons evaluated on the bit patterns with integer instructions, leaving the FP64
+// pipe (the bottleneck of these kernels) to arithmetic.  Same results as the FP64
+// comparisons for every input, NaN, signed zeros and infinities included.
+__device__ __forceinline__ bool lt_zero(double x) {  // x < 0.0
+  const long long b = __double_as_longlong(x);
+  const unsigned long long mag = (unsigned long long)b & 0x7fffffffffffffffull;
+  return b < 0 && mag - 1ull < 0x7ff0000000000000ull;  // negative, non-zero, not NaN
+}
+__device__ __forceinline__ bool gt_one(double x) {  // x > 1.0
+  const long long b = __double_as_longlong(x);
+  return b > 0x3ff0000000000000ll && b <= 0x7ff0000000000000ll;  // positive, not NaN
+}
+
 // nearest_point_from_point_to_line (interaction.rs:497-509): returns q and t.
 template <int D>
 __device__ __forceinline__ void nearest_point_f64(const double *p, const double *l0,
@@ -41,8 +54,8 @@ __device__ __forceinline__ void nearest_point_f64(const double *p, const double 
     nsq = dadd(nsq, dmul(ab[c], ab[c]));
   }
   t = ddiv(dot, nsq);
-  if (t < 0.0) t = 0.0;
-  if (t > 1.0) t = 1.0;
+  if (lt_zero(t)) t = 0.0;
+  if (gt_one(t)) t = 1.0;
   const double omt = dsub(1.0, t);
 #pragma unroll
   for (int c = 0; c < D; ++c) q[c] = dadd(dmul(l0[c], omt), dmul(l1[c], t));
@@ -59,7 +72,10 @@ __device__ __forceinline__ bool morse_full_f64(const double *own, const double *
 #pragma unroll
   for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
   const double dist = __dsqrt_rn(n2);
-  if (dist > S.cutoff || dist == 0.0) return false;
+  // dist > cutoff || dist == 0.0 (dist is +0, positive or NaN; NaN carries on)
+  const long long db = __double_as_longlong(dist);
+  const unsigned long long mag = (unsigned long long)db & 0x7fffffffffffffffull;
+  if (mag <= 0x7ff0000000000000ull && (mag == 0ull || db > S.cutoff_bits)) return false;
   const double e = exp(dmul(S.mrs_nstiff, dsub(dist, S.mrs_r)));
   const double force = dmul(dmul(S.mrs_k, e), dsub(1.0, e));
 #pragma unroll
@@ -918,10 +934,15 @@ __device__ __forceinline__ double half_exact(double x) {
   return dmul(x, 0.5);
 }
 
+// 0.0 + x, exactly: x itself except that -0.0 becomes +0.0.
+__device__ __forceinline__ double plus_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
 // Items of one chunk of the queue kernel's result buffer.  Every lane's items fit (at most
 // NV * (NV - 1) <= 56), so a round needs more than one chunk only when the warp's passes
 // together have more survivors.
-constexpr int kQueueCap = 128;
+constexpr int kQueueCap = 256;
 
 template <int D, int NV>
 constexpr size_t queue_smem_bytes() {
@@ -1050,14 +1071,16 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
         const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
         const int r = (int)__fns(rows_l, 0, j - rex_l + 1);
         const int slot0 = ex_l - cs;  // the lane's first item in the chunk buffer
+        // M starts at 0.0 and every unit has an item: 0.0 + x is x (with -0.0 -> +0.0),
+        // so the first item is taken as it is and the adds start with the second.
         double m[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) m[c] = 0.0;
         if (!ext_l) {
           // items (r, sy) are consecutive bits, hence consecutive slots
           const int first = slot0 + __popcll(m_l & ((1ull << (r * NE)) - 1ull));
           const int n = __popcll((m_l >> (r * NE)) & ((1ull << NE) - 1ull));
-          for (int k = 0; k < n; ++k) {
+#pragma unroll
+          for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[c * CAP + first]);
+          for (int k = 1; k < n; ++k) {
 #pragma unroll
             for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[c * CAP + first + k]);
           }
@@ -1068,12 +1091,20 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
             if (r >= 1) em |= (uint32_t)((m_l >> (vx * NE + r - 1)) & 1ull) << (2 * vx);
             if (r < NE) em |= (uint32_t)((m_l >> (vx * NE + r)) & 1ull) << (2 * vx + 1);
           }
-          while (em) {
+          // (h, slot) of the next contribution, lowest bit of em first
+          auto next = [&](int &h, int &slot) {
             const int k = __ffs(em) - 1;
             em &= em - 1u;
-            const int h = k & 1;
+            h = k & 1;
             const int vs = (k >> 1) * NE + r - 1 + h;
-            const int slot = slot0 + __popcll(m_l & ((1ull << vs) - 1ull));
+            slot = slot0 + __popcll(m_l & ((1ull << vs) - 1ull));
+          };
+          int h, slot;
+          next(h, slot);
+#pragma unroll
+          for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[(h * D + c) * CAP + slot]);
+          while (em) {
+            next(h, slot);
 #pragma unroll
             for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(h * D + c) * CAP + slot]);
           }
