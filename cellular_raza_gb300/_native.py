@@ -17,6 +17,7 @@ PREC_F64, PREC_MIXED = 0, 1
 WEIGHTS_CHILI, WEIGHTS_PHYSICAL = 0, 1
 OPT_PREFILTER, OPT_GRAPH_CHUNK, OPT_BLOCK, OPT_PROFILE, OPT_DEBUG_FORCES = 1, 2, 3, 4, 5
 OPT_KERNEL_VARIANT = 6
+OPT_PASS_LIST = 7
 
 # Every symbol include/crg.h declares (checked by tests/test_abi.py).
 EXPORTED = [

@@ -45,8 +45,13 @@ struct crg_ctx {
   int32_t *status = nullptr;
   int64_t *step_ctr = nullptr;
   double *dbg_force = nullptr;
-  double *frc = nullptr;     // rods: interaction force between the two step kernels
-  uint32_t *work = nullptr;  // rods: queue counter of the force kernel
+  // rods: pass list of the default force path and the fallback's force buffer
+  uint32_t *npass = nullptr, *pass_off = nullptr, *pass_a = nullptr, *pass_b = nullptr;
+  uint8_t *pass_meta = nullptr;
+  double *mbuf = nullptr;
+  int64_t pass_cap = 0;
+  uint32_t *rctl = nullptr;
+  double *frc = nullptr;
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
   uint32_t snap_agents = 0;
@@ -224,14 +229,40 @@ int32_t dalloc(T **p, size_t n) {
   return CRG_OK;
 }
 
+void free_pass_list(crg_ctx *c) {
+  void *ptrs[] = {c->pass_a, c->pass_b, c->pass_meta, c->mbuf};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  c->pass_a = c->pass_b = nullptr;
+  c->pass_meta = nullptr;
+  c->mbuf = nullptr;
+  c->pass_cap = 0;
+}
+
+// (Re)allocates the rod pass list for n passes.  On failure the list stays empty and every
+// step takes the rod-level fallback kernel.
+int32_t alloc_pass_list(crg_ctx *c, int64_t n) {
+  free_pass_list(c);
+  if (n < 1024) n = 1024;
+  if (dalloc(&c->pass_a, (size_t)n) != CRG_OK || dalloc(&c->pass_b, (size_t)n) != CRG_OK ||
+      dalloc(&c->pass_meta, (size_t)n) != CRG_OK || dalloc(&c->mbuf, (size_t)n * c->nc) != CRG_OK) {
+    free_pass_list(c);
+    return CRG_ENOMEM;
+  }
+  c->pass_cap = n;
+  return CRG_OK;
+}
+
 void free_all(crg_ctx *c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->work, c->staging, c->snap};
+                  c->step_ctr, c->dbg_force, c->frc, c->rctl, c->npass, c->pass_off,
+                  c->staging, c->snap};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  free_pass_list(c);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
@@ -262,7 +293,10 @@ int32_t allocate(crg_ctx *c) {
   A(staging, cap * nc);
   if (c->kind == CRG_KIND_ROD) {
     A(frc, cap * nc);
-    A(work, 1);
+    A(rctl, 4);
+    A(npass, cap);
+    A(pass_off, cap);
+    alloc_pass_list(c, 12 * cap);  // grown after a step that needed more (read_status)
   }
   if (c->order > 1) {
     A(hist, cap * nc * 2);
@@ -372,7 +406,14 @@ PackArgs pack_args(crg_ctx *c) {
   P.step_ctr = c->step_ctr;
   P.dbg_force = c->dbg_force;
   P.frc = c->frc;
-  P.work = c->work;
+  P.rctl = c->rctl;
+  P.npass = c->npass;
+  P.pass_off = c->pass_off;
+  P.pass_a = c->pass_a;
+  P.pass_b = c->pass_b;
+  P.pass_meta = c->pass_meta;
+  P.mbuf = c->mbuf;
+  P.pass_cap = c->pass_cap;
   P.prefilter = c->prefilter;
   P.variant = c->variant;
   return P;
@@ -411,9 +452,10 @@ SortArgs sort_args(crg_ctx *c, int initial) {
   return A;
 }
 
-// Kernels one launch_force issues: the default rod path runs a force and an update kernel.
+// Kernels one launch_force issues: the default rod path runs the pass walk, the pass kernel,
+// the rod-level fallback (returns at once unless the pass list overflowed) and the update.
 int force_kernel_count(const crg_ctx *c) {
-  return (c->kind == CRG_KIND_ROD && c->variant == 0) ? 2 : 1;
+  return (c->kind == CRG_KIND_ROD && c->variant == 0) ? 4 : 1;
 }
 
 void launch_force(crg_ctx *c) {
@@ -431,6 +473,8 @@ void launch_one_step(crg_ctx *c) {
 
 // Waits for the handle's stream and reads the device status word.  A CUDA failure is
 // recorded as the handle's error (so every later call reports it too).
+void invalidate_graph(crg_ctx *c);
+
 int32_t read_status(crg_ctx *c) {
   cudaError_t e = cudaMemcpyAsync(c->h_status, c->status, 8 * sizeof(int32_t),
                                   cudaMemcpyDeviceToHost, c->stream);
@@ -440,6 +484,12 @@ int32_t read_status(crg_ctx *c) {
     c->err_agent = -1;
     c->err_step = c->steps_done;
     return c->err_code;
+  }
+  if (c->kind == CRG_KIND_ROD && (int64_t)(uint32_t)c->h_status[5] > c->pass_cap) {
+    // a step outgrew the pass list and took the rod-level kernel: make room for next time
+    const int64_t need = (int64_t)(uint32_t)c->h_status[5];
+    invalidate_graph(c);  // captured launches hold the old buffers
+    alloc_pass_list(c, need + need / 4 + 1024);
   }
   if (c->h_status[0] != CRG_OK) {
     c->err_code = c->h_status[0];
@@ -1008,6 +1058,13 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
       if (value < 0 || value > 3) return CRG_EINVAL;
       c->variant = (int)value;
       break;
+    case CRG_OPT_PASS_LIST: {
+      if (c->kind != CRG_KIND_ROD || value < 0) return CRG_EINVAL;
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
+      const int32_t r = alloc_pass_list(c, value);
+      if (r != CRG_OK) return r;
+      break;
+    }
     case CRG_OPT_DEBUG_FORCES:
       if (value && !c->dbg_force) {
         int32_t r = dalloc(&c->dbg_force, (size_t)c->cap * c->nc);

@@ -81,8 +81,16 @@ struct PackArgs {
   int32_t *status;
   const int64_t *step_ctr;
   double *dbg_force;  // optional [nc][cap]: interaction force of this step
-  double *frc;        // rods: [nc][cap] interaction force, force kernel -> update kernel
-  uint32_t *work;     // rods: queue counter of the force kernel (zeroed before each launch)
+  // rods: pass list of the default force path (one pass = own_a(b) or ext_a(b))
+  uint32_t *npass, *pass_off;  // [cap] number of passes of each rod, index of its first
+  uint32_t *pass_a, *pass_b;   // [pass_cap] rod and candidate of each pass
+  uint8_t *pass_meta;          // [pass_cap] bit 0: ext pass; bits 1-6: voxel of b - voxel of
+                               // a + 1 per axis, 2 bits each
+  double *mbuf;                // [nc][pass_cap] M / 2 of each pass, rows in vertex order
+  int64_t pass_cap;
+  uint32_t *rctl;  // [0] passes reserved, [1] pass queue, [2] rod queue, [3] pass list
+                   // overflow (all zeroed before each step)
+  double *frc;     // rods: [nc][cap] interaction force of the rod-level fallback kernel
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
   int32_t variant;    // force kernel: 0 warp-packed (default), 1 thread per agent
 };
@@ -154,7 +162,8 @@ __device__ __forceinline__ uint32_t sim_of_agent(const PackArgs &P, uint32_t i) 
 }
 
 // status word: [0] code, [1] agent id lo, [2] agent id hi, [3] step (or check site),
-// [4] simulation index within the pack
+// [4] simulation index within the pack, [5] largest pass list a rod step asked for since
+// the status was last cleared (read by the host to size the pass list)
 __device__ __forceinline__ void set_status(int32_t *status, int32_t code, uint64_t agent,
                                            int64_t step, int32_t sim = 0) {
   if (atomicCAS(&status[0], 0, code) == 0) {

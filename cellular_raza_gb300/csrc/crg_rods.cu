@@ -1287,6 +1287,7 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
 template <int D, int NV>
 __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
   constexpr int NC = NV * D, NE = NV - 1;
+  if (!P.rctl[3]) return;  // the pass list fitted: k_rods_passq computed this step
   extern __shared__ double sRes[];             // [2D][kQueueCap]: item results
   double *sAcc = sRes + 2 * D * kQueueCap;     // [NC][32]: force accumulated on each lane's rod
   const int lane = threadIdx.x;
@@ -1376,7 +1377,7 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
       if (!want) break;
       const int leader = __ffs(want) - 1;
       uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(P.work, (uint32_t)__popc(want));
+      if (lane == leader) base = atomicAdd(&P.rctl[2], (uint32_t)__popc(want));
       base = __shfl_sync(0xffffffffu, base, leader);
       if (need) {
         const uint32_t t = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
@@ -1458,8 +1459,226 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
   }
 }
 
-// Mechanics, solver, boundary and next key of every rod from the interaction force that
-// k_rods_queue stored in frc (frozen simulations copy their state).
+// ---------------------------------------------------------------------------------------
+// Pass list of the default rod path.  For every rod, in the order k_rods_step visits them:
+// for every candidate b of the 3^D voxel neighbourhood whose FP32 bounding box comes within
+// the prefilter threshold, the passes own_a(b) and -- where the pair weight is 1 -- ext_a(b),
+// in chili's order.  A rod's passes are contiguous (one reservation per warp, so a rod's
+// index range does not depend on timing within the warp).  A list that would outgrow
+// pass_cap sets the overflow flag: the rod-level kernel then computes this step, and the
+// largest size asked for goes to status[5] for the host to grow the list.
+// ---------------------------------------------------------------------------------------
+template <int D, int NV>
+__global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
+  constexpr int NC = NV * D;
+  const int lane = threadIdx.x & 31;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < P.n_agents;
+  const uint32_t ii = valid ? i : 0u;
+  const int64_t cap = P.cap;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
+  const SimDev &S = P.sims[sim];
+  const bool live = valid && *P.step_ctr < S.stop_step;  // frozen rods have no passes
+  uint32_t key = P.key[ii];
+  if (key - S.voxel_off >= S.n_vox) {
+    if (live) invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  float amin[D], amax[D];
+  bool a_nan = false;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const float o = P.off[k * cap + ii];
+    a_nan |= !(o == o);
+    if (k < D) {
+      amin[k] = o;
+      amax[k] = o;
+    } else {
+      amin[k % D] = fminf(amin[k % D], o);
+      amax[k % D] = fmaxf(amax[k % D], o);
+    }
+  }
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+    nb[c] = hi - lo[c] + 1;
+  }
+  const int n_box = nb[0] * nb[1] * nb[2];
+  // visit(b, meta) for every pass of rod i, in order
+  auto walk = [&](auto &&visit) {
+    for (int o = 0; o < n_box; ++o) {
+      const int j2 = lo[2] + o % nb[2];
+      const int j1 = lo[1] + (o / nb[2]) % nb[1];
+      const int j0 = lo[0] + o / (nb[1] * nb[2]);
+      const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                  : (uint32_t)j0 * S.nvox[1] + j1;
+      const bool same = (w == v);
+      const bool twice =
+          same || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
+      const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};
+      float kd[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) kd[c] = (float)dj[c] * S.dxf[c];
+      const uint32_t box = (uint32_t)((dj[0] + 1) | ((dj[1] + 1) << 2) | ((dj[2] + 1) << 4));
+      uint32_t b = P.start[S.voxel_off + w], b_end = P.start[S.voxel_off + w + 1];
+      if (b > b_end || b_end > P.n_agents) {
+        invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+        b_end = b;
+      }
+      for (; b < b_end; ++b) {
+        if (b == i) continue;
+        float bmin[D], bmax[D];
+        bool b_nan = false;
+#pragma unroll
+        for (int k = 0; k < NC; ++k) {
+          const float o2 = P.off[k * cap + b] + kd[k % D];
+          b_nan |= !(o2 == o2);
+          if (k < D) {
+            bmin[k] = o2;
+            bmax[k] = o2;
+          } else {
+            bmin[k % D] = fminf(bmin[k % D], o2);
+            bmax[k % D] = fmaxf(bmax[k % D], o2);
+          }
+        }
+        bool far = false;
+        if (!a_nan && !b_nan) {
+#pragma unroll
+          for (int c = 0; c < D; ++c)
+            far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+        }
+        if (far) continue;
+        if (!twice) {
+          visit(b, box << 1);  // own_a(b) only: weight 1/2
+        } else {
+          const uint32_t ext_first = (same && b < i) ? 1u : 0u;
+          visit(b, (box << 1) | ext_first);
+          visit(b, (box << 1) | (ext_first ^ 1u));
+        }
+      }
+    }
+  };
+  uint32_t count = 0;
+  if (live) walk([&](uint32_t, uint32_t) { ++count; });
+  // one contiguous range per rod, one reservation per warp
+  uint32_t incl = count;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  const uint32_t wtot = __shfl_sync(0xffffffffu, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && wtot) {
+    base = atomicAdd(&P.rctl[0], wtot);
+    const uint64_t end = (uint64_t)base + wtot;
+    atomicMax(&P.status[5], (int32_t)(end < 0x7fffffffull ? end : 0x7fffffffull));
+  }
+  base = __shfl_sync(0xffffffffu, base, 31);
+  const uint64_t first = (uint64_t)base + (incl - count);
+  if (valid) {
+    P.npass[i] = count;
+    P.pass_off[i] = (uint32_t)first;
+  }
+  if (!count) return;
+  if (first + count > (uint64_t)P.pass_cap) {
+    P.rctl[3] = 1u;
+    return;
+  }
+  uint32_t k = (uint32_t)first;
+  walk([&](uint32_t b, uint32_t meta) {
+    P.pass_a[k] = i;
+    P.pass_b[k] = b;
+    P.pass_meta[k] = (uint8_t)meta;
+    ++k;
+  });
+}
+
+// The passes of the list, 32 consecutive ones per warp and round: every lane carries a pass
+// until the list drains, however the passes are spread over rods.  Per pass: the FP32 scan
+// of the vertex/segment pairs, the FP64 evaluation and row folds of eval_fold_queue, and
+// the pass's M / 2 stored to mbuf for k_rods_update to add up in pass order.
+template <int D, int NV>
+__global__ void __launch_bounds__(32) k_rods_passq(const PackArgs P) {
+  constexpr int NC = NV * D, NE = NV - 1;
+  if (P.rctl[3]) return;  // overflow: the rod-level kernel computes this step
+  extern __shared__ double sRes[];            // [2D][kQueueCap]: item results
+  double *sAcc = sRes + 2 * D * kQueueCap;    // [NC][32]: M / 2 of each lane's pass
+  const int lane = threadIdx.x;
+  const int64_t cap = P.cap, pcap = P.pass_cap;
+  const uint32_t total = P.rctl[0];
+  const float inf = __int_as_float(0x7f800000);
+#pragma unroll
+  for (int k = 0; k < NC; ++k) sAcc[k * 32 + lane] = 0.0;
+  __syncwarp();
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&P.rctl[1], 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total) break;
+    const uint32_t t = base + lane;
+    const bool have = t < total;
+    uint32_t a = 0, b = 0, sim = 0;
+    bool is_ext = false;
+    uint64_t mask = 0;
+    if (have) {
+      a = P.pass_a[t];
+      b = P.pass_b[t];
+      const uint32_t meta = P.pass_meta[t];
+      is_ext = (meta & 1u) != 0u;
+      sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, a);
+      const SimDev &S = P.sims[sim];
+      const float thr2 = P.prefilter ? S.filt_thr2 : inf;
+      float kd[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) kd[c] = (float)((int)((meta >> (1 + 2 * c)) & 3u) - 1) * S.dxf[c];
+      float oa[NC], ob[NC];
+#pragma unroll
+      for (int k = 0; k < NC; ++k) {
+        oa[k] = P.off[k * cap + a];
+        ob[k] = P.off[k * cap + b] + kd[k % D];
+      }
+#pragma unroll
+      for (int vx = 0; vx < NV; ++vx)
+#pragma unroll
+        for (int sy = 0; sy < NE; ++sy) {
+          const float *pp = is_ext ? &ob[vx * D] : &oa[vx * D];
+          const float *s0 = is_ext ? &oa[sy * D] : &ob[sy * D];
+          const float *s1 = is_ext ? &oa[(sy + 1) * D] : &ob[(sy + 1) * D];
+          float p32[D], l0[D], l1[D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            p32[c] = pp[c];
+            l0[c] = s0[c];
+            l1[c] = s1[c];
+          }
+          if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
+        }
+    }
+    eval_fold_queue<D, NV>(P, sRes, sAcc, lane, mask, is_ext, a, b, sim);
+    if (have) {
+#pragma unroll
+      for (int k = 0; k < NC; ++k) {
+        P.mbuf[k * pcap + t] = sAcc[k * 32 + lane];
+        sAcc[k * 32 + lane] = 0.0;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Mechanics, solver, boundary and next key of every rod from its interaction force: the
+// sum, in pass order, of the M / 2 that k_rods_passq stored for its passes (rows a pass
+// does not touch are +0, which leaves the sum unchanged since it is never -0), or, after a
+// pass list overflow, the force k_rods_queue stored in frc.  Frozen simulations copy their
+// state.
 template <int D, int NV>
 __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   constexpr int NC = NV * D;
@@ -1476,9 +1695,20 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   }
   double pa[NC], acc[NC];
 #pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    pa[k] = P.pos[k * cap + i];
-    acc[k] = P.frc[k * cap + i];
+  for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
+  if (P.rctl[3]) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) acc[k] = P.frc[k * cap + i];
+  } else {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+    const double *mb = P.mbuf + P.pass_off[i];
+    const uint32_t n = P.npass[i];
+    const int64_t pcap = P.pass_cap;
+    for (uint32_t p = 0; p < n; ++p) {
+#pragma unroll
+      for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], mb[k * pcap + p]);
+    }
   }
   rod_update<D, NV>(P, S, i, key, pa, acc);
 }
@@ -1532,8 +1762,10 @@ __global__ void k_rod_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_inte
   hash[i] = h;
 }
 
-// Resident warps of k_rods_queue on the current device, [D - 2][NV] (set by prepare_rods).
+// Resident warps of k_rods_queue / k_rods_passq on the current device, [D - 2][NV]
+// (set by prepare_rods).
 unsigned g_queue_warps[2][9] = {};
+unsigned g_passq_warps[2][9] = {};
 
 template <int D, int NV>
 constexpr size_t pass_smem_bytes() {
@@ -1562,9 +1794,13 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st) {
   }
   const unsigned resident = g_queue_warps[D - 2][NV];
   const unsigned grid = (resident && resident < warps) ? resident : warps;
-  cudaMemsetAsync(P.work, 0, sizeof(uint32_t), st);
-  k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);
-  k_rods_update<D, NV><<<(P.n_agents + 127) / 128, 128, 0, st>>>(P);
+  const unsigned pgrid = g_passq_warps[D - 2][NV] ? g_passq_warps[D - 2][NV] : warps;
+  const unsigned rblocks = (P.n_agents + 127) / 128;
+  cudaMemsetAsync(P.rctl, 0, 4 * sizeof(uint32_t), st);
+  k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
+  k_rods_passq<D, NV><<<pgrid, 32, queue_smem_bytes<D, NV>(), st>>>(P);
+  k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);  // only on overflow
+  k_rods_update<D, NV><<<rblocks, 128, 0, st>>>(P);
 }
 
 template <int D, int NV>
@@ -1582,6 +1818,12 @@ cudaError_t prepare_t() {
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_queue<D, NV>, 32, qsmem);
   if (e == cudaSuccess) g_queue_warps[D - 2][NV] = (unsigned)(sms * per_sm);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_rods_passq<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             qsmem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_passq<D, NV>, 32, qsmem);
+  if (e == cudaSuccess) g_passq_warps[D - 2][NV] = (unsigned)(sms * per_sm);
   return e;
 }
 

@@ -70,6 +70,8 @@ int64_t footprint_bytes(const crg_domain &d, const crg_model &m, int64_t n) {
   const int64_t nc = (int64_t)nv * d.dim;
   int64_t per_agent = 4 * nc * 8 + 2 * 8 + 2 * 4 + nc * 4 + 8 + nc * 8;
   if (m.solver_order > 1) per_agent += 4 * nc * 8 + 2;
+  if (m.kind == CRG_KIND_ROD)  // force buffer, pass counts and a pass list of 12 per rod
+    per_agent += nc * 8 + 2 * 4 + 12 * (2 * 4 + 1 + nc * 8);
   double nvox = 1.0;
   for (int i = 0; i < d.dim; ++i) {
     double k = d.voxel_mode == 0 ? std::floor((d.max[i] - d.min[i]) / d.interaction_range)

@@ -222,6 +222,11 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * groups of 32 rods.  All produce identical results; 1 is kept as the simple reference
  * formulation. */
 #define CRG_OPT_KERNEL_VARIANT 6
+/* Rods, default kernel: capacity of the pass list in passes (one pass = one candidate pair
+ * half, about 11 per rod in a dense 2D colony).  A step whose list does not fit computes its
+ * forces with the rod-level kernel instead (same results) and the list is grown to fit at
+ * the end of crg_step.  Created with 12 passes per rod of capacity. */
+#define CRG_OPT_PASS_LIST 7
 int32_t crg_debug_forces(crg_ctx *ctx, double *force, uint64_t *ids);
 
 /* Neighbour statistics of the CURRENT cell list (what the next step will visit): per agent

@@ -209,6 +209,22 @@ def test_rod_kernel_variants_bitwise_identical(gpu, n_sub):
         assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
 
 
+def test_rod_pass_list_overflow_falls_back_and_grows(gpu):
+    """A pass list far too small for a step: that step's forces come from the rod-level
+    kernel (same bits), the list is grown at the end of crg_step, and the later steps run on
+    the pass list again.  The trajectory equals the default run bit for bit."""
+    r = W.rods_2d(seed=63, n=20_000, n_subdomains=4)
+    a = E.run(r, 40)
+    with E.Simulation.single(r.model, r.n) as sim:
+        sim.set_option(N.OPT_PASS_LIST, 1024)
+        sim.upload(r.pos, r.vel)
+        sim.step(5)   # overflows: rod-level kernel; the list grows afterwards
+        sim.step(35)  # fits
+        b = sim.download(order="id")
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    assert np.array_equal(a["voxel"], b["voxel"])
+
+
 @pytest.mark.parametrize("n_sub", [1, 5])
 def test_sphere_kernel_variants_bitwise_identical(gpu, n_sub):
     """Warp-packed and thread-per-agent FP64 sphere kernels: identical bits."""
