@@ -206,15 +206,19 @@ def reference_arm(args):
 # ----------------------------------------------------------------------------- GPU arm
 
 def algorithmic_flops(w, stats):
-    """FP64 work one force launch must do once the FP32 prefilter has removed the
-    evaluations beyond the cutoff (sqrt, exp, division count one flop each).
+    """FP64 work of one step's force stage once the FP32 prefilter has removed the
+    evaluations beyond the cutoff (sqrt, exp, division count one flop each), as
+    (whole force stage, dominant kernel).
     spheres: 30 flop per interacting ordered pair (8 distance + 22 force) + 21 per agent
-    (update); rods: 45 flop per in-range vertex-segment evaluation (18 nearest point,
-    6 distance, 21 force) + 250 per rod (springs, curvature, update)."""
+    (update), all in one kernel; rods: 45 flop per in-range vertex-segment evaluation of
+    a.calc(a, b) (18 nearest point, 6 distance, 21 force) in the pass kernel (a lower bound:
+    the ext halves of weight-1 pairs come on top) + 250 per rod (springs, curvature,
+    update) in the update kernel."""
     n_inter = float(stats["n_inter"].astype("float64").sum())
     if w.model.kind == "rod":
-        return 45.0 * n_inter + 250.0 * w.n
-    return 30.0 * n_inter + 21.0 * w.n
+        return 45.0 * n_inter + 250.0 * w.n, 45.0 * n_inter
+    f = 30.0 * n_inter + 21.0 * w.n
+    return f, f
 
 
 def replica_throughput(dist, local_ms, local_agent_steps):
@@ -454,20 +458,22 @@ def crg_arm(args):
     sim.set_option(N.OPT_PROFILE, 0)
     force_ms = prof["force_ms"] / prof_steps
     sort_ms = prof["sort_ms"] / prof_steps
-    flops = algorithmic_flops(w, stats)
+    kernel_ms = prof["kernel_ms"] / prof_steps
+    flops, kernel_flops = algorithmic_flops(w, stats)
     peaks = measured_peaks()
     fma = E.measure_fma_peaks()
     fp64_peak = fma["fp64_tflops"]
-    achieved = flops / (force_ms * 1e-3) / 1e12
-    kernel_key = f"{args.workload}_force"
+    achieved = kernel_flops / (kernel_ms * 1e-3) / 1e12
+    kernel = "k_rods_passq" if w.model.kind == "rod" else "k_spheres_pass"
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak if fp64_peak else None,
-                "traffic": committed_traffic(kernel_key),
+                "traffic": committed_traffic(f"{args.workload}_{kernel}"),
                 "peak_source": "measured DFMA microbenchmark (crg_measure_fma_peaks) on this GPU",
-                "kernel": ("k_rods_queue + k_rods_update" if w.model.kind == "rod"
-                           else "k_spheres_pass"),
-                "force_ms_per_launch": force_ms, "sort_ms_per_step": sort_ms,
-                "algorithmic_flop_per_launch": flops}
+                "kernel": kernel, "kernel_ms_per_launch": kernel_ms,
+                "algorithmic_flop_per_launch": kernel_flops,
+                "force_stage_ms_per_step": force_ms, "force_stage_flop_per_step": flops,
+                "force_stage_tflops": flops / (force_ms * 1e-3) / 1e12,
+                "sort_ms_per_step": sort_ms}
     # the sort kernels are HBM-bound: algorithmic bytes per step
     nc = w.model.nc
     sort_bytes = w.n * (2 * 2 * 8 * nc + 2 * 8 + 4 * 4 + 4 * nc + 8 * 3)

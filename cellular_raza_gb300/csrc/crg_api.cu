@@ -65,7 +65,7 @@ struct crg_ctx {
   int variant = 0;
   int block = 0;
   int profile = 0;
-  double prof_ms[3] = {0, 0, 0};
+  double prof_ms[4] = {0, 0, 0, 0};
   int32_t err_code = CRG_OK;
   int64_t err_agent = -1, err_step = -1;
   int64_t steps_done = 0;
@@ -458,12 +458,16 @@ int force_kernel_count(const crg_ctx *c) {
   return (c->kind == CRG_KIND_ROD && c->variant == 0) ? 4 : 1;
 }
 
-void launch_force(crg_ctx *c) {
+// k0 / k1 (optional): events recorded around the dominant force kernel.
+void launch_force(crg_ctx *c, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr) {
   PackArgs P = pack_args(c);
-  if (c->kind == CRG_KIND_SPHERE)
+  if (c->kind == CRG_KIND_SPHERE) {
+    if (k0) cudaEventRecord(k0, c->stream);
     crg::launch_spheres_step(c->dim, c->precision, P, c->block, c->stream);
-  else
-    crg::launch_rods_step(c->dim, c->nv, c->precision, P, c->block, c->stream);
+    if (k1) cudaEventRecord(k1, c->stream);
+  } else {
+    crg::launch_rods_step(c->dim, c->nv, c->precision, P, c->block, c->stream, k0, k1);
+  }
 }
 
 void launch_one_step(crg_ctx *c) {
@@ -643,11 +647,10 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
     c->steps_done += n_steps;
     return CRG_OK;
   }
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   if (c->profile) {
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
-    c->prof_ms[0] = c->prof_ms[1] = 0.0;
-    c->prof_ms[2] = 0.0;
+    c->prof_ms[0] = c->prof_ms[1] = c->prof_ms[2] = c->prof_ms[3] = 0.0;
   }
   int64_t left = n_steps;
   const int chunk = c->graph_chunk;
@@ -656,16 +659,18 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
       const int k = (int)std::min<int64_t>(left, 64);
       for (int s = 0; s < k; ++s) {
         cudaEventRecord(ev[0], c->stream);
-        launch_force(c);
+        launch_force(c, ev[3], ev[4]);
         cudaEventRecord(ev[1], c->stream);
         crg::launch_sort(sort_args(c, 0), c->bsum, c->stream);
         cudaEventRecord(ev[2], c->stream);
         cudaEventSynchronize(ev[2]);
-        float a = 0.f, b = 0.f;
+        float a = 0.f, b = 0.f, d = 0.f;
         cudaEventElapsedTime(&a, ev[0], ev[1]);
         cudaEventElapsedTime(&b, ev[1], ev[2]);
+        cudaEventElapsedTime(&d, ev[3], ev[4]);
         c->prof_ms[0] += a;
         c->prof_ms[1] += b;
+        c->prof_ms[3] += d;
         c->prof_ms[2] += force_kernel_count(c) + crg::sort_kernel_count();
       }
       left -= k;
@@ -1082,9 +1087,9 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
   return CRG_OK;
 }
 
-int32_t crg_profile(crg_ctx *c, double *out3) {
-  if (!c || !out3) return CRG_EINVAL;
-  for (int k = 0; k < 3; ++k) out3[k] = c->prof_ms[k];
+int32_t crg_profile(crg_ctx *c, double *out4) {
+  if (!c || !out4) return CRG_EINVAL;
+  for (int k = 0; k < 4; ++k) out4[k] = c->prof_ms[k];
   return CRG_OK;
 }
 

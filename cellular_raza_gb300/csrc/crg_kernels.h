@@ -71,8 +71,9 @@ void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, in
 
 // Force + integrator + boundary + next voxel key (+ histogram) for one step.
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st);
+// k0 / k1 (optional) are recorded on st right before and after the dominant force kernel.
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
-                      cudaStream_t st);
+                      cudaStream_t st, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr);
 int prepare_rods(int dim, int nv);  // 0 on success
 // Diagnostics over the current cell list.
 void launch_neighbor_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand,

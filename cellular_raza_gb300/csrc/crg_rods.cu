@@ -1773,23 +1773,27 @@ constexpr size_t pass_smem_bytes() {
 }
 
 template <int D, int NV>
-void launch_t(const PackArgs &P, int block, cudaStream_t st) {
+void launch_t(const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1) {
   (void)block;
+  if (k0) cudaEventRecord(k0, st);
   if (P.variant == 1) {  // thread-per-rod kernel
     constexpr int B = 64;
     const unsigned grid = (P.n_agents + B - 1) / B;
     k_rods_step<D, NV, B><<<grid, B, 0, st>>>(P);
+    if (k1) cudaEventRecord(k1, st);
     return;
   }
   if (P.variant == 2) {  // slot-queue kernel
     constexpr int W = 2, K = 8;
     const unsigned grid = (P.n_agents + W * 32 - 1) / (W * 32);
     k_rods_packed<D, NV, W, K><<<grid, W * 32, 0, st>>>(P);
+    if (k1) cudaEventRecord(k1, st);
     return;
   }
   const unsigned warps = (P.n_agents + 31) / 32;
   if (P.variant == 3) {  // pass-synchronous kernel over fixed groups of 32 rods
     k_rods_pass<D, NV><<<warps, 32, pass_smem_bytes<D, NV>(), st>>>(P);
+    if (k1) cudaEventRecord(k1, st);
     return;
   }
   const unsigned resident = g_queue_warps[D - 2][NV];
@@ -1798,7 +1802,9 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st) {
   const unsigned rblocks = (P.n_agents + 127) / 128;
   cudaMemsetAsync(P.rctl, 0, 4 * sizeof(uint32_t), st);
   k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
+  if (k0) cudaEventRecord(k0, st);
   k_rods_passq<D, NV><<<pgrid, 32, queue_smem_bytes<D, NV>(), st>>>(P);
+  if (k1) cudaEventRecord(k1, st);
   k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);  // only on overflow
   k_rods_update<D, NV><<<rblocks, 128, 0, st>>>(P);
 }
@@ -1842,15 +1848,16 @@ cudaError_t prepare_d(int nv) {
 }
 
 template <int D>
-void launch_d(int nv, const PackArgs &P, int block, cudaStream_t st) {
+void launch_d(int nv, const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0,
+              cudaEvent_t k1) {
   switch (nv) {
-    case 2: launch_t<D, 2>(P, block, st); break;
-    case 3: launch_t<D, 3>(P, block, st); break;
-    case 4: launch_t<D, 4>(P, block, st); break;
-    case 5: launch_t<D, 5>(P, block, st); break;
-    case 6: launch_t<D, 6>(P, block, st); break;
-    case 7: launch_t<D, 7>(P, block, st); break;
-    case 8: launch_t<D, 8>(P, block, st); break;
+    case 2: launch_t<D, 2>(P, block, st, k0, k1); break;
+    case 3: launch_t<D, 3>(P, block, st, k0, k1); break;
+    case 4: launch_t<D, 4>(P, block, st, k0, k1); break;
+    case 5: launch_t<D, 5>(P, block, st, k0, k1); break;
+    case 6: launch_t<D, 6>(P, block, st, k0, k1); break;
+    case 7: launch_t<D, 7>(P, block, st, k0, k1); break;
+    case 8: launch_t<D, 8>(P, block, st, k0, k1); break;
     default: break;
   }
 }
@@ -1863,14 +1870,14 @@ int prepare_rods(int dim, int nv) {
 }
 
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
-                      cudaStream_t st) {
+                      cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1) {
   (void)precision;  // rods run the FP64 path
   if (!P.n_agents) return;
   if (block <= 0 || block > 128) block = 64;
   if (dim == 3)
-    launch_d<3>(nv, P, block, st);
+    launch_d<3>(nv, P, block, st, k0, k1);
   else
-    launch_d<2>(nv, P, block, st);
+    launch_d<2>(nv, P, block, st, k0, k1);
 }
 
 template <int D>

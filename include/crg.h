@@ -237,10 +237,11 @@ int32_t crg_debug_neighbor_stats(crg_ctx *ctx, uint32_t *n_cand, uint32_t *n_int
                                  uint64_t *cand_hash, uint64_t *ids);
 
 /* Device time of the kernels of the last crg_step call, split by phase (ms):
- * [0] force+update, [1] sort; [2] number of kernels launched.  Requires
+ * [0] force+update, [1] sort; [2] number of kernels launched; [3] the dominant force
+ * kernel alone (rods: the pass kernel; spheres: the force kernel).  Requires
  * CRG_OPT_PROFILE = 1 (events disable graph capture). */
 #define CRG_OPT_PROFILE 4
-int32_t crg_profile(crg_ctx *ctx, double *out3);
+int32_t crg_profile(crg_ctx *ctx, double *out4);
 
 /* Measures the FP64 and FP32 fused-multiply-add throughput of the current device with a
  * dependent-chain microbenchmark (TFLOP/s, 2 flops per FMA). */
