@@ -925,12 +925,13 @@ __device__ __forceinline__ void eval_fold_pass(const PackArgs &P, double *sRes, 
 }
 
 // x * 0.5, exactly as the FP64 multiply rounds it: an exponent decrement for normal x above
-// the lowest binade (exact there), the multiply itself for zeros, subnormals, the lowest
-// binade, infinities and NaN.
+// the lowest binade (exact there), x itself for zeros, the multiply itself for subnormals,
+// the lowest binade, infinities and NaN.
 __device__ __forceinline__ double half_exact(double x) {
   const long long bits = __double_as_longlong(x);
   const long long e = (bits >> 52) & 0x7ff;
   if (e > 1 && e < 0x7ff) return __longlong_as_double(bits - (1ll << 52));
+  if ((bits << 1) == 0) return x;  // +-0 * 0.5 = +-0
   return dmul(x, 0.5);
 }
 
@@ -944,9 +945,34 @@ __device__ __forceinline__ double plus_zero(double x) {
 // together have more survivors.
 constexpr int kQueueCap = 256;
 
+// Per-warp scratch of the fold's counting sort (after the accumulators in shared memory).
+struct FoldScratch {
+  uint64_t mask[32];                    // survivor bitmask of each lane's pass
+  int32_t slot0[32];                    // first chunk slot of each lane's items
+  int32_t cnt[2 * kMaxVertices + 1];    // units per chain length
+  int32_t base[2 * kMaxVertices + 1];   // first sorted position of each chain length
+  uint8_t ext[32];                      // lane's pass is ext_a(b)
+  uint8_t desc[32 * kMaxVertices];      // sorted units: lane << 3 | row
+};
+
 template <int D, int NV>
 constexpr size_t queue_smem_bytes() {
-  return sizeof(double) * ((size_t)2 * D * kQueueCap + (size_t)NV * D * 32);
+  return sizeof(double) * ((size_t)2 * D * kQueueCap + (size_t)NV * D * 32) +
+         sizeof(FoldScratch);
+}
+
+// Bit 2 vx + h set when item (vx, r - 1 + h) of an ext pass survived: the contributions to
+// row r of the pass matrix, in the reference's order.
+template <int NV>
+__device__ __forceinline__ uint32_t ext_row_bits(uint64_t mask, int r) {
+  constexpr int NE = NV - 1;
+  uint32_t em = 0;
+#pragma unroll
+  for (int vx = 0; vx < NV; ++vx) {
+    if (r >= 1) em |= (uint32_t)((mask >> (vx * NE + r - 1)) & 1ull) << (2 * vx);
+    if (r < NE) em |= (uint32_t)((mask >> (vx * NE + r)) & 1ull) << (2 * vx + 1);
+  }
+  return em;
 }
 
 // The pass step of k_rods_queue.  Like eval_fold_pass, but
@@ -1022,97 +1048,101 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
     }
     __syncwarp();
 
-    // ---- fold: each non-empty (lane, row) of the chunk is one unit --------------------
+    // ---- fold ---------------------------------------------------------------------------
     // Row r of the pass matrix M collects, in the reference's (vertex, segment) order,
     //   own pass: f of items (r, 0..NE-1);
     //   ext pass: for each vertex vx, -f*t of item (vx, r-1) then -f*(1-t) of item (vx, r).
-    uint32_t rowmask = 0;
-    if (in) {
+    // Each non-empty (lane, row) of the chunk is a unit: a chain of L contributions summed in
+    // that order, then acc += M / 2, i.e. L FP64 adds per component.  The units are sorted
+    // by L (counting sort in shared memory, longest first) and dealt to the lanes in snake
+    // order; each lane runs its units as one sequence of adds, so every iteration issues
+    // exactly D adds for the lanes that still have work.
+    FoldScratch &F = *reinterpret_cast<FoldScratch *>(sAcc + NV * D * 32);
+    int len[NV];
 #pragma unroll
-      for (int r = 0; r < NV; ++r) {
-        bool has = false;
-        if (!is_ext) {
-          has = ((mask >> (r * NE)) & ((1ull << NE) - 1ull)) != 0ull;
-        } else {
-#pragma unroll
-          for (int vx = 0; vx < NV; ++vx) {
-            if (r >= 1) has |= ((mask >> (vx * NE + r - 1)) & 1ull) != 0ull;
-            if (r < NE) has |= ((mask >> (vx * NE + r)) & 1ull) != 0ull;
-          }
-        }
-        if (has) rowmask |= 1u << r;
-      }
+    for (int r = 0; r < NV; ++r) {
+      const uint32_t bits = is_ext ? ext_row_bits<NV>(mask, r)
+                                   : (uint32_t)((mask >> (r * NE)) & ((1ull << NE) - 1ull));
+      len[r] = in ? __popc(bits) : 0;
     }
-    const int rcnt = __popc(rowmask);
-    int rincl = rcnt;
+    if (lane <= 2 * NV) F.cnt[lane] = 0;
+    F.mask[lane] = mask;
+    F.slot0[lane] = excl - cs;  // the lane's first item in the chunk buffer
+    F.ext[lane] = is_ext ? 1 : 0;
+    __syncwarp();
+    int rank[NV];
+#pragma unroll
+    for (int r = 0; r < NV; ++r) rank[r] = len[r] ? atomicAdd(&F.cnt[len[r]], 1) : 0;
+    __syncwarp();
+    const int cl = (lane >= 1 && lane <= 2 * NV) ? F.cnt[lane] : 0;  // lane L: units of length L
+    int suf = cl;  // units of length >= lane
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, rincl, off);
-      if (lane >= off) rincl += y;
+      const int y = __shfl_down_sync(0xffffffffu, suf, off);
+      if (lane + off < 32) suf += y;
     }
-    const int rexcl = rincl - rcnt;
-    const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
-    for (int base = 0; base < rtotal; base += 32) {
-      const int j = base + lane;
-      int l = 0;
+    const int n_units = __shfl_sync(0xffffffffu, suf, 0);
+    if (lane >= 1 && lane <= 2 * NV) F.base[lane] = suf - cl;  // units longer than lane
+    __syncwarp();
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int cand = l + step;
-        const int e = __shfl_sync(0xffffffffu, rexcl, cand & 31);
-        if (cand < 32 && e <= j) l = cand;
+    for (int r = 0; r < NV; ++r)
+      if (len[r]) F.desc[F.base[len[r]] + rank[r]] = (uint8_t)((lane << 3) | r);
+    __syncwarp();
+
+    int k_unit = 0, p = lane, l = 0, r = 0, slot0 = 0;
+    bool act = p < n_units, ext = false;
+    uint64_t m_l = 0;
+    uint32_t em = 0;  // contributions of the current unit still to add
+    double m[D];
+    auto contrib = [&](int &h, int &slot) {  // (h, slot) of the unit's next contribution
+      const int k = __ffs(em) - 1;
+      em &= em - 1u;
+      int vs;
+      if (ext) {
+        h = k & 1;
+        vs = (k >> 1) * NE + r - 1 + h;
+      } else {
+        h = 0;
+        vs = r * NE + k;
       }
-      const int rex_l = __shfl_sync(0xffffffffu, rexcl, l);
-      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
-      const uint32_t rows_l = __shfl_sync(0xffffffffu, rowmask, l);
-      const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
-      const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
-      const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
-      if (j < rtotal) {
-        const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
-        const int r = (int)__fns(rows_l, 0, j - rex_l + 1);
-        const int slot0 = ex_l - cs;  // the lane's first item in the chunk buffer
-        // M starts at 0.0 and every unit has an item: 0.0 + x is x (with -0.0 -> +0.0),
-        // so the first item is taken as it is and the adds start with the second.
-        double m[D];
-        if (!ext_l) {
-          // items (r, sy) are consecutive bits, hence consecutive slots
-          const int first = slot0 + __popcll(m_l & ((1ull << (r * NE)) - 1ull));
-          const int n = __popcll((m_l >> (r * NE)) & ((1ull << NE) - 1ull));
+      slot = slot0 + __popcll(m_l & ((1ull << vs) - 1ull));
+    };
+    auto load = [&]() {  // start unit p: M = its first contribution (0 + x)
+      const uint32_t d = F.desc[p];
+      l = (int)(d >> 3);
+      r = (int)(d & 7u);
+      ext = F.ext[l] != 0;
+      m_l = F.mask[l];
+      slot0 = F.slot0[l];
+      em = ext ? ext_row_bits<NV>(m_l, r)
+               : (uint32_t)((m_l >> (r * NE)) & ((1ull << NE) - 1ull));
+      int h, slot;
+      contrib(h, slot);
 #pragma unroll
-          for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[c * CAP + first]);
-          for (int k = 1; k < n; ++k) {
-#pragma unroll
-            for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[c * CAP + first + k]);
-          }
-        } else {
-          uint32_t em = 0;  // bit 2 vx + h: item (vx, r - 1 + h) contributes to row r
-#pragma unroll
-          for (int vx = 0; vx < NV; ++vx) {
-            if (r >= 1) em |= (uint32_t)((m_l >> (vx * NE + r - 1)) & 1ull) << (2 * vx);
-            if (r < NE) em |= (uint32_t)((m_l >> (vx * NE + r)) & 1ull) << (2 * vx + 1);
-          }
-          // (h, slot) of the next contribution, lowest bit of em first
-          auto next = [&](int &h, int &slot) {
-            const int k = __ffs(em) - 1;
-            em &= em - 1u;
-            h = k & 1;
-            const int vs = (k >> 1) * NE + r - 1 + h;
-            slot = slot0 + __popcll(m_l & ((1ull << vs) - 1ull));
-          };
-          int h, slot;
-          next(h, slot);
-#pragma unroll
-          for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[(h * D + c) * CAP + slot]);
-          while (em) {
-            next(h, slot);
-#pragma unroll
-            for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(h * D + c) * CAP + slot]);
-          }
-        }
+      for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[(h * D + c) * CAP + slot]);
+    };
+    if (act) load();
+    while (__any_sync(0xffffffffu, act)) {
+      if (act) {
+        const bool fin = (em == 0u);  // chain done: acc += M / 2
+        int h = 0, slot = 0;
+        if (!fin) contrib(h, slot);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-          double &acc = sAcc[(r * D + c) * 32 + l];
-          acc = dadd(acc, half_exact(m[c]));
+          const int q = (r * D + c) * 32 + l;
+          const double x = fin ? sAcc[q] : m[c];
+          const double y = fin ? half_exact(m[c]) : sRes[(h * D + c) * CAP + slot];
+          const double z = dadd(x, y);
+          if (fin)
+            sAcc[q] = z;
+          else
+            m[c] = z;
+        }
+        if (fin) {
+          ++k_unit;
+          p = 32 * k_unit + ((k_unit & 1) ? 31 - lane : lane);
+          act = p < n_units;
+          if (act) load();
         }
       }
     }

@@ -49,6 +49,10 @@ struct Request {
   int32_t status = CRG_OK;
   bool done = false;
   bool failed_in_pack = false;
+  // Lifetime: the request is freed by whichever comes last, its waiter collecting it or
+  // the server thread dropping it from its pack (both under the server mutex).
+  bool in_pack = false;
+  bool collected = false;
 };
 
 struct Class {
@@ -114,6 +118,18 @@ void finish(crg_server *s, Request *r, int32_t status) {
   s->cv_work.notify_all();
 }
 
+// The server thread drops r (it left its pack): free it if its waiter already collected it.
+void leave_pack(crg_server *s, Request *r) {
+  std::lock_guard<std::mutex> lk(s->mu);
+  r->in_pack = false;
+  if (r->collected) s->reqs.erase(r->ticket);
+}
+
+void leave_all(crg_server *s, Class &c) {
+  for (Request *r : c.sims) leave_pack(s, r);
+  c.sims.clear();
+}
+
 // Rebuilds the pack of one class: keeps the unfinished simulations, adds `incoming`.
 int32_t repack(crg_server *s, Class &c, std::vector<Request *> &incoming) {
   std::vector<int32_t> keep;
@@ -126,7 +142,7 @@ int32_t repack(crg_server *s, Class &c, std::vector<Request *> &incoming) {
   if (keep.empty() && incoming.empty()) {
     if (c.pack) crg_destroy(c.pack);
     c.pack = nullptr;
-    c.sims.clear();
+    leave_all(s, c);
     c.steps_since_repack = 0;
     return CRG_OK;
   }
@@ -158,7 +174,13 @@ int32_t repack(crg_server *s, Class &c, std::vector<Request *> &incoming) {
   if (rc != CRG_OK) return rc;
   if (c.pack) crg_destroy(c.pack);
   c.pack = np;
+  for (Request *r : c.sims)
+    if (r->done) leave_pack(s, r);
   c.sims.clear();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (Request *r : incoming) r->in_pack = true;
+  }
   for (Request *r : incoming) {
     r->remaining = r->steps;
     c.sims.push_back(r);
@@ -246,7 +268,7 @@ void serve_loop(crg_server *s) {
       if (dead) {
         crg_destroy(c.pack);
         c.pack = nullptr;
-        c.sims.clear();
+        leave_all(s, c);
         c.steps_since_repack = 0;
         continue;
       }
@@ -270,8 +292,10 @@ void serve_loop(crg_server *s) {
       }
     }
   }
-  for (auto &kv : s->classes)
+  for (auto &kv : s->classes) {
     if (kv.second.pack) crg_destroy(kv.second.pack);
+    leave_all(s, kv.second);
+  }
   s->classes.clear();
 }
 
@@ -321,7 +345,7 @@ int32_t crg_server_wait(crg_server *s, uint64_t ticket, double timeout_s, int64_
   if (!s) return CRG_EINVAL;
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
-  if (it == s->reqs.end()) return CRG_EINVAL;
+  if (it == s->reqs.end() || it->second->collected) return CRG_EINVAL;
   Request *r = it->second.get();
   const auto deadline = std::chrono::steady_clock::now() +
                         std::chrono::duration_cast<std::chrono::steady_clock::duration>(
@@ -337,7 +361,8 @@ int32_t crg_server_wait(crg_server *s, uint64_t ticket, double timeout_s, int64_
     if (ids) std::memcpy(ids, r->ids.data(), sizeof(uint64_t) * r->ids.size());
   }
   if (latency_s) *latency_s = r->t_done - r->t_submit;
-  s->reqs.erase(it);
+  r->collected = true;
+  if (!r->in_pack) s->reqs.erase(it);  // else the server thread frees it when it drops it
   return status;
 }
 
