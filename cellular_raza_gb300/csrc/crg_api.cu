@@ -249,6 +249,11 @@ int32_t alloc_pass_list(crg_ctx *c, int64_t n) {
     free_pass_list(c);
     return CRG_ENOMEM;
   }
+  // poison: an entry a step forgot to write reads as NaN instead of a stale force
+  if (cudaMemset(c->mbuf, 0xff, sizeof(double) * (size_t)n * c->nc) != cudaSuccess) {
+    free_pass_list(c);
+    return CRG_ECUDA;
+  }
   c->pass_cap = n;
   return CRG_OK;
 }

@@ -924,15 +924,20 @@ __device__ __forceinline__ void eval_fold_pass(const PackArgs &P, double *sRes, 
   __syncwarp();
 }
 
-// x * 0.5, exactly as the FP64 multiply rounds it: an exponent decrement for normal x above
-// the lowest binade (exact there), x itself for zeros, the multiply itself for subnormals,
-// the lowest binade, infinities and NaN.
+// x * 0.5 with the IEEE result of the FP64 multiply (round to nearest even), computed on
+// the bit pattern with integer instructions.
 __device__ __forceinline__ double half_exact(double x) {
-  const long long bits = __double_as_longlong(x);
-  const long long e = (bits >> 52) & 0x7ff;
-  if (e > 1 && e < 0x7ff) return __longlong_as_double(bits - (1ll << 52));
-  if ((bits << 1) == 0) return x;  // +-0 * 0.5 = +-0
-  return dmul(x, 0.5);
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long sign = u & 0x8000000000000000ull, mag = u ^ sign;
+  const unsigned long long e = mag >> 52;
+  // lowest binade and subnormals: the value is mag * 2^-1074, so halving is a shift of mag
+  // rounded to nearest, ties to even (the result is subnormal or zero)
+  unsigned long long q = mag >> 1;
+  q += (mag & q & 1ull);
+  unsigned long long h = sign | q;
+  if (e >= 2) h = u - (1ull << 52);  // normal result: exponent - 1, exact
+  if (e == 0x7ffull) h = u;          // infinities and NaN are their own half
+  return __longlong_as_double((long long)h);
 }
 
 // 0.0 + x, exactly: x itself except that -0.0 becomes +0.0.
@@ -951,14 +956,20 @@ struct FoldScratch {
   int32_t slot0[32];                    // first chunk slot of each lane's items
   int32_t cnt[2 * kMaxVertices + 1];    // units per chain length
   int32_t base[2 * kMaxVertices + 1];   // first sorted position of each chain length
+  uint32_t tpass[32];                   // pass index of each lane (pass kernel)
   uint8_t ext[32];                      // lane's pass is ext_a(b)
   uint8_t desc[32 * kMaxVertices];      // sorted units: lane << 3 | row
 };
 
 template <int D, int NV>
-constexpr size_t queue_smem_bytes() {
+constexpr size_t queue_smem_bytes() {  // k_rods_queue: results, accumulators, fold scratch
   return sizeof(double) * ((size_t)2 * D * kQueueCap + (size_t)NV * D * 32) +
          sizeof(FoldScratch);
+}
+
+template <int D, int NV>
+constexpr size_t passq_smem_bytes() {  // k_rods_passq: results, fold scratch
+  return sizeof(double) * (size_t)2 * D * kQueueCap + sizeof(FoldScratch);
 }
 
 // Bit 2 vx + h set when item (vx, r - 1 + h) of an ext pass survived: the contributions to
@@ -982,12 +993,26 @@ __device__ __forceinline__ uint32_t ext_row_bits(uint64_t mask, int r) {
 //  * a (lane, row) unit sums only its own items (loops over set bits) and adds M / 2 to the
 //    lane's accumulator sAcc [NC][32] itself.
 // Per row the sums run over the same items in the same order as eval_fold_pass.
-template <int D, int NV>
+template <int D, int NV, bool STORE>
 __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes, double *sAcc,
-                                                int lane, uint64_t mask, bool is_ext,
-                                                uint32_t a, uint32_t b, uint32_t sim) {
+                                                FoldScratch &F, int lane, uint64_t mask,
+                                                bool is_ext, uint32_t a, uint32_t b,
+                                                uint32_t sim, uint32_t t, bool has_pass) {
   constexpr int NE = NV - 1, CAP = kQueueCap;
   const int64_t cap = P.cap;
+  if (STORE && has_pass) {
+    // rows of the pass matrix no item reaches: M / 2 = +0 (written here, whether or not the
+    // round has any survivor; the touched rows are written by the fold below)
+#pragma unroll
+    for (int r = 0; r < NV; ++r) {
+      const uint32_t bits = is_ext ? ext_row_bits<NV>(mask, r)
+                                   : (uint32_t)((mask >> (r * NE)) & ((1ull << NE) - 1ull));
+      if (!bits) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) P.mbuf[(r * D + c) * P.pass_cap + t] = 0.0;
+      }
+    }
+  }
   const int cnt = __popcll(mask);
   int incl = cnt;
 #pragma unroll
@@ -1057,7 +1082,6 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
     // by L (counting sort in shared memory, longest first) and dealt to the lanes in snake
     // order; each lane runs its units as one sequence of adds, so every iteration issues
     // exactly D adds for the lanes that still have work.
-    FoldScratch &F = *reinterpret_cast<FoldScratch *>(sAcc + NV * D * 32);
     int len[NV];
 #pragma unroll
     for (int r = 0; r < NV; ++r) {
@@ -1069,6 +1093,7 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
     F.mask[lane] = mask;
     F.slot0[lane] = excl - cs;  // the lane's first item in the chunk buffer
     F.ext[lane] = is_ext ? 1 : 0;
+    F.tpass[lane] = t;
     __syncwarp();
     int rank[NV];
 #pragma unroll
@@ -1121,28 +1146,30 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
 #pragma unroll
       for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[(h * D + c) * CAP + slot]);
     };
+    // unit done: M / 2 to the pass's slot (STORE: 0 + M / 2) or added to the lane's rod
+    auto finish_unit = [&]() {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const double hm = half_exact(m[c]);
+        if (STORE)
+          P.mbuf[(r * D + c) * P.pass_cap + F.tpass[l]] = plus_zero(hm);
+        else
+          sAcc[(r * D + c) * 32 + l] = dadd(sAcc[(r * D + c) * 32 + l], hm);
+      }
+      ++k_unit;
+      p = 32 * k_unit + ((k_unit & 1) ? 31 - lane : lane);
+      act = p < n_units;
+      if (act) load();
+    };
     if (act) load();
     while (__any_sync(0xffffffffu, act)) {
       if (act) {
-        const bool fin = (em == 0u);  // chain done: acc += M / 2
-        int h = 0, slot = 0;
-        if (!fin) contrib(h, slot);
+        while (act && em == 0u) finish_unit();  // no FP64 adds left in this unit
+        if (act) {
+          int h, slot;
+          contrib(h, slot);
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-          const int q = (r * D + c) * 32 + l;
-          const double x = fin ? sAcc[q] : m[c];
-          const double y = fin ? half_exact(m[c]) : sRes[(h * D + c) * CAP + slot];
-          const double z = dadd(x, y);
-          if (fin)
-            sAcc[q] = z;
-          else
-            m[c] = z;
-        }
-        if (fin) {
-          ++k_unit;
-          p = 32 * k_unit + ((k_unit & 1) ? 31 - lane : lane);
-          act = p < n_units;
-          if (act) load();
+          for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(h * D + c) * CAP + slot]);
         }
       }
     }
@@ -1320,6 +1347,7 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
   if (!P.rctl[3]) return;  // the pass list fitted: k_rods_passq computed this step
   extern __shared__ double sRes[];             // [2D][kQueueCap]: item results
   double *sAcc = sRes + 2 * D * kQueueCap;     // [NC][32]: force accumulated on each lane's rod
+  FoldScratch &F = *reinterpret_cast<FoldScratch *>(sAcc + NC * 32);
   const int lane = threadIdx.x;
   const int64_t cap = P.cap;
   const int64_t step = *P.step_ctr;
@@ -1485,7 +1513,8 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
           if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
         }
     }
-    eval_fold_queue<D, NV>(P, sRes, sAcc, lane, mask, is_ext, i, cur_b, sim);
+    eval_fold_queue<D, NV, false>(P, sRes, sAcc, F, lane, mask, is_ext, i, cur_b, sim, 0u,
+                                  false);
   }
 }
 
@@ -1639,15 +1668,12 @@ template <int D, int NV>
 __global__ void __launch_bounds__(32) k_rods_passq(const PackArgs P) {
   constexpr int NC = NV * D, NE = NV - 1;
   if (P.rctl[3]) return;  // overflow: the rod-level kernel computes this step
-  extern __shared__ double sRes[];            // [2D][kQueueCap]: item results
-  double *sAcc = sRes + 2 * D * kQueueCap;    // [NC][32]: M / 2 of each lane's pass
+  extern __shared__ double sRes[];  // [2D][kQueueCap]: item results, then the fold scratch
+  FoldScratch &F = *reinterpret_cast<FoldScratch *>(sRes + 2 * D * kQueueCap);
   const int lane = threadIdx.x;
-  const int64_t cap = P.cap, pcap = P.pass_cap;
+  const int64_t cap = P.cap;
   const uint32_t total = P.rctl[0];
   const float inf = __int_as_float(0x7f800000);
-#pragma unroll
-  for (int k = 0; k < NC; ++k) sAcc[k * 32 + lane] = 0.0;
-  __syncwarp();
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(&P.rctl[1], 32u);
@@ -1692,15 +1718,7 @@ __global__ void __launch_bounds__(32) k_rods_passq(const PackArgs P) {
           if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
         }
     }
-    eval_fold_queue<D, NV>(P, sRes, sAcc, lane, mask, is_ext, a, b, sim);
-    if (have) {
-#pragma unroll
-      for (int k = 0; k < NC; ++k) {
-        P.mbuf[k * pcap + t] = sAcc[k * 32 + lane];
-        sAcc[k * 32 + lane] = 0.0;
-      }
-    }
-    __syncwarp();
+    eval_fold_queue<D, NV, true>(P, sRes, nullptr, F, lane, mask, is_ext, a, b, sim, t, have);
   }
 }
 
@@ -1833,7 +1851,7 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0, cud
   cudaMemsetAsync(P.rctl, 0, 4 * sizeof(uint32_t), st);
   k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
   if (k0) cudaEventRecord(k0, st);
-  k_rods_passq<D, NV><<<pgrid, 32, queue_smem_bytes<D, NV>(), st>>>(P);
+  k_rods_passq<D, NV><<<pgrid, 32, passq_smem_bytes<D, NV>(), st>>>(P);
   if (k1) cudaEventRecord(k1, st);
   k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);  // only on overflow
   k_rods_update<D, NV><<<rblocks, 128, 0, st>>>(P);
@@ -1854,11 +1872,12 @@ cudaError_t prepare_t() {
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_queue<D, NV>, 32, qsmem);
   if (e == cudaSuccess) g_queue_warps[D - 2][NV] = (unsigned)(sms * per_sm);
+  const int psmem = (int)passq_smem_bytes<D, NV>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_rods_passq<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             qsmem);
+                             psmem);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_passq<D, NV>, 32, qsmem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_passq<D, NV>, 32, psmem);
   if (e == cudaSuccess) g_passq_warps[D - 2][NV] = (unsigned)(sms * per_sm);
   return e;
 }

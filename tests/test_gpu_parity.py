@@ -6,6 +6,8 @@ Bars (written in each test):
     <= 1e-12 (max_i |x_gpu - x_ref| / max_i |x_ref|);
   * multi-step FP64 trajectories: stated per test.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -223,6 +225,34 @@ def test_rod_pass_list_overflow_falls_back_and_grows(gpu):
         b = sim.download(order="id")
     assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
     assert np.array_equal(a["voxel"], b["voxel"])
+
+
+def test_rod_passes_without_survivors(gpu):
+    """Rods in a checkerboard whose diagonal neighbours pass the bounding-box test but have
+    no vertex/segment pair within the cutoff: every pass of the list has zero survivors, so
+    every round of the pass kernel has nothing to evaluate.  Each pass must still store its
+    (zero) M / 2 -- the pass list is allocated NaN-filled, so a missed store shows up as NaN
+    -- and the result equals the thread-per-rod kernel bit for bit."""
+    import math
+
+    gap, length = 6.01, 3.0  # cutoff 6, prefilter threshold ~6.02
+    px, py = length + gap, gap
+    pts = []
+    for i in range(40):
+        for j in range(40):
+            if (i + j) % 2:
+                continue
+            x0, y = 5.0 + i * px, 5.0 + j * py
+            pts.append([[x0, y], [x0 + length, y]])
+    pos = np.array(pts, dtype=np.float64)
+    side = 5.0 + 40 * px + 5.0
+    r = W.rods(n=len(pts), side=side, seed=0, n_vertices=2, spring_length=length)
+    r = dataclasses.replace(r, pos=pos, vel=np.zeros_like(pos))
+    a = E.run(r, 3)
+    b = E.run(r, 3, options={N.OPT_KERNEL_VARIANT: 1})
+    assert np.all(np.isfinite(a["pos"]))
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    assert not math.isnan(float(a["vel"].sum()))
 
 
 @pytest.mark.parametrize("n_sub", [1, 5])
