@@ -391,6 +391,8 @@ def crg_arm(args):
 
     for _ in range(max(args.warmup, 3)):
         run_once()
+        with torch.cuda.stream(ext):  # the flush kernel's first launch stays out of the timing
+            flush.zero_()
     torch.cuda.synchronize()
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -432,6 +434,8 @@ def crg_arm(args):
 
     for _ in range(max(args.warmup, 3)):
         e2e_once()
+        with torch.cuda.stream(ext):
+            flush.zero_()
     torch.cuda.synchronize()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -1665,7 +1665,7 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
 // of the vertex/segment pairs, the FP64 evaluation and row folds of eval_fold_queue, and
 // the pass's M / 2 stored to mbuf for k_rods_update to add up in pass order.
 template <int D, int NV>
-__global__ void __launch_bounds__(32) k_rods_passq(const PackArgs P) {
+__global__ void __launch_bounds__(32, 24) k_rods_passq(const PackArgs P) {
   constexpr int NC = NV * D, NE = NV - 1;
   if (P.rctl[3]) return;  // overflow: the rod-level kernel computes this step
   extern __shared__ double sRes[];  // [2D][kQueueCap]: item results, then the fold scratch
