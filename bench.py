@@ -280,8 +280,23 @@ def extra_mixed_large(torch):
     out["p9999_rel_pos_err"] = float(np.percentile(err, 99.99))
     out["mean_rel_pos_err"] = float(err.mean())
     out["normwise_rel_pos_err"] = float(dx.max() / x.max())  # max |dx| / max |x|
+    out["l2_rel_pos_err"] = float(np.linalg.norm(b - a) / np.linalg.norm(a))
     out["max_abs_pos_err"] = float(dx.max())
     out["worst_agent_abs_pos"] = float(x[worst])
+    out["agents_above_1e-5"] = int((err > 1e-5).sum())
+    # chili's pair weights (1 inside a voxel, 1/2 across neighbour voxels of one subdomain)
+    # make the force jump when an agent changes voxel, so an agent within rounding distance
+    # of a voxel face can take a different branch in the two runs; the same comparison with
+    # the continuous physical weights isolates the precision error itself
+    phys = {}
+    for prec in ("mixed", "f64"):
+        m = w.model.replace(precision=prec, weight_mode=1)
+        phys[prec] = E.run(w.__class__(w.name, m, w.pos, w.vel, w.n_steps), w.n_steps)["pos"]
+    pe = (np.linalg.norm(phys["mixed"] - phys["f64"], axis=-1).ravel() /
+          np.linalg.norm(phys["f64"], axis=-1).ravel())
+    out["physical_weights"] = {"max_rel_pos_err": float(pe.max()),
+                               "p9999_rel_pos_err": float(np.percentile(pe, 99.99)),
+                               "agents_above_1e-5": int((pe > 1e-5).sum())}
     return out
 
 

@@ -51,6 +51,7 @@ struct crg_ctx {
   double *mbuf = nullptr;
   int64_t pass_cap = 0;
   uint32_t *rctl = nullptr;
+  uint32_t *fix_list = nullptr;  // mixed spheres: agents for the FP64 fix-up kernel
   double *frc = nullptr;
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
@@ -263,7 +264,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->rctl, c->npass, c->pass_off,
+                  c->step_ctr, c->dbg_force, c->frc, c->rctl, c->fix_list, c->npass, c->pass_off,
                   c->staging, c->snap};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -296,6 +297,10 @@ int32_t allocate(crg_ctx *c) {
   A(status, 8);
   A(step_ctr, 1);
   A(staging, cap * nc);
+  if (c->kind == CRG_KIND_SPHERE && c->precision != CRG_PREC_F64) {
+    A(rctl, 4);
+    A(fix_list, cap);
+  }
   if (c->kind == CRG_KIND_ROD) {
     A(frc, cap * nc);
     A(rctl, 4);
@@ -412,6 +417,7 @@ PackArgs pack_args(crg_ctx *c) {
   P.dbg_force = c->dbg_force;
   P.frc = c->frc;
   P.rctl = c->rctl;
+  P.fix_list = c->fix_list;
   P.npass = c->npass;
   P.pass_off = c->pass_off;
   P.pass_a = c->pass_a;
@@ -460,7 +466,8 @@ SortArgs sort_args(crg_ctx *c, int initial) {
 // Kernels one launch_force issues: the default rod path runs the pass walk, the pass kernel,
 // the rod-level fallback (returns at once unless the pass list overflowed) and the update.
 int force_kernel_count(const crg_ctx *c) {
-  return (c->kind == CRG_KIND_ROD && c->variant == 0) ? 4 : 1;
+  if (c->kind == CRG_KIND_ROD) return c->variant == 0 ? 4 : 1;
+  return c->precision == CRG_PREC_F64 ? 1 : 2;
 }
 
 // k0 / k1 (optional): events recorded around the dominant force kernel.

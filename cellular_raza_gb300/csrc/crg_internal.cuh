@@ -91,6 +91,8 @@ struct PackArgs {
   uint32_t *rctl;  // [0] passes reserved, [1] pass queue, [2] rod queue, [3] pass list
                    // overflow (all zeroed before each step)
   double *frc;     // rods: [nc][cap] interaction force of the rod-level fallback kernel
+  uint32_t *fix_list;  // mixed spheres: agents whose force the FP64 fix-up kernel computes
+                       // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
   int32_t variant;    // force kernel: 0 warp-packed (default), 1 thread per agent
 };
@@ -144,9 +146,11 @@ __device__ __forceinline__ void unravel(const SimDev &S, uint32_t v, int *idx) {
   }
 }
 
-// Corner of voxel idx in FP64: min + idx * dx (used only for the FP32 offsets).
-__device__ __forceinline__ double voxel_corner(const SimDev &S, int axis, int idx) {
-  return S.min[axis] + (double)idx * S.dx[axis];
+// Centre of voxel idx in FP64: min + (idx + 1/2) dx.  The FP32 offsets are taken from it
+// (|offset| <= dx / 2 inside the voxel, so their rounding is half that of corner offsets);
+// only differences of offsets and of centres, (j - idx) dx, enter the kernels.
+__device__ __forceinline__ double voxel_centre(const SimDev &S, int axis, int idx) {
+  return S.min[axis] + ((double)idx + 0.5) * S.dx[axis];
 }
 
 __device__ __forceinline__ uint32_t sim_of_agent(const PackArgs &P, uint32_t i) {

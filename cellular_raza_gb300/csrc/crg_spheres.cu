@@ -37,6 +37,53 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
   s = t;
 }
 
+
+// Mixed path, rare case (a NaN displacement: an agent far outside its voxel, NaN
+// positions): agent i's interaction force computed exactly as the FP64 path computes it
+// (same candidates, same order, FP64 Morse).
+struct Vec3 {
+  double x[3];
+};
+template <int D>
+__device__ Vec3 agent_force_f64(const PackArgs &P, const SimDev &S, uint32_t i, uint32_t v,
+                                const double *pa) {
+  const int64_t cap = P.cap;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  const uint32_t sub_v = subdomain_of(S, v);
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  Vec3 r = {{0.0, 0.0, 0.0}};
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
+                           subdomain_of(S, w) != sub_v;
+        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        if (b0 > b1 || b1 > P.n_agents) b1 = b0;  // recorded by the caller's own scan
+        for (uint32_t b = b0; b < b1; ++b) {
+          if (b == i) continue;
+          double z[D], h[D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
+          if (morse_half_f64<D>(z, S, S.radius, h)) {
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+              r.x[c] = dadd(r.x[c], h[c]);
+              if (twice) r.x[c] = dadd(r.x[c], h[c]);
+            }
+          }
+        }
+      }
+  return r;
+}
+
 // NewtonDamped increment, solver, boundary and next voxel key of agent i with interaction
 // force acc (shared by the force kernels).
 template <int D>
@@ -131,7 +178,7 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
 }
 
 template <int D, int PREC>
-__global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
+__global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n_agents) return;
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
@@ -161,6 +208,7 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   double acc[D];
   float fs[D], fcmp[D];
+  bool nan_seen = false;  // mixed path: a NaN displacement met (see k_spheres_fix)
 #pragma unroll
   for (int c = 0; c < D; ++c) {
     acc[c] = 0.0;
@@ -180,7 +228,7 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
                                     : (uint32_t)j0 * S.nvox[1] + j1;
         const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
                            subdomain_of(S, w) != sub_v;
-        // corner(a) - corner(b) = -(j - idx) * dx
+        // centre(a) - centre(b) = -(j - idx) * dx
         float kd[D];
         kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
         kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
@@ -212,10 +260,17 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
               }
             }
           } else {
-            // FP32 Morse on the FP32 displacement (offsets are accurate to ~1e-6 dx).  Whether
-            // the pair interacts is decided exactly as on the FP64 path: pairs whose FP32
-            // distance lies within the prefilter margin of the cutoff or of zero are decided
-            // from the FP64 distance, so no pair switches on or off relative to FP64.
+            // FP32 Morse on the FP32 displacement (offsets from the voxel centres, accurate
+            // to 2^-25 dx).  Whether the pair interacts is decided exactly as on the FP64
+            // path: pairs whose FP32 distance lies within the prefilter margin of the cutoff
+            // or of zero are decided from the FP64 distance, so no pair switches on or off
+            // relative to FP64.  A NaN displacement (an offset marked NaN because its agent
+            // is far outside its voxel, or NaN positions) hands the whole agent to the FP64
+            // fix-up kernel.
+            if (d2 != d2) {
+              nan_seen = true;
+              continue;
+            }
             const float dist = sqrtf(d2);
             bool in;
             if (fabsf(dist - S.cutoff_f) <= S.band_f || dist <= S.band_f) {
@@ -240,19 +295,43 @@ __global__ void __launch_bounds__(256) k_spheres_step(const PackArgs P) {
                 kahan_add(fs[c], fcmp[c], h);
                 if (twice) kahan_add(fs[c], fcmp[c], h);
               }
-            } else if (dist != dist) {
-              // NaN positions propagate like the FP64 path would.
-#pragma unroll
-              for (int c = 0; c < D; ++c) kahan_add(fs[c], fcmp[c], dist);
             }
           }
         }
       }
   if (PREC != CRG_PREC_F64) {
+    if (nan_seen) {  // k_spheres_fix computes this agent's force and update in FP64
+      P.fix_list[atomicAdd(&P.rctl[0], 1u)] = i;
+      return;
+    }
 #pragma unroll
     for (int c = 0; c < D; ++c) acc[c] = (double)fs[c] - (double)fcmp[c];
   }
   sphere_update<D>(P, S, i, key, pa, va, acc);
+}
+
+// The agents the mixed kernel handed over (rctl[0] of them in fix_list): FP64 force and
+// update, exactly as the FP64 path would compute them.
+template <int D>
+__global__ void __launch_bounds__(128) k_spheres_fix(const PackArgs P) {
+  const uint32_t n = P.rctl[0];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const uint32_t i = P.fix_list[t];
+    const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+    const SimDev &S = P.sims[sim];
+    const uint32_t key = P.key[i];  // checked by the mixed kernel
+    const int64_t cap = P.cap;
+    double pa[D], va[D], acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      pa[c] = P.pos[c * cap + i];
+      va[c] = P.vel[c * cap + i];
+    }
+    const Vec3 f = agent_force_f64<D>(P, S, i, key - S.voxel_off, pa);
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = f.x[c];
+    sphere_update<D>(P, S, i, key, pa, va, acc);
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -476,16 +555,21 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
   }
   if (block <= 0 || block > 256) block = 128;
   const unsigned grid = (P.n_agents + block - 1) / block;
+  if (precision != CRG_PREC_F64) cudaMemsetAsync(P.rctl, 0, sizeof(uint32_t), st);
   if (dim == 3) {
-    if (precision == CRG_PREC_F64)
+    if (precision == CRG_PREC_F64) {
       k_spheres_step<3, CRG_PREC_F64><<<grid, block, 0, st>>>(P);
-    else
+    } else {
       k_spheres_step<3, CRG_PREC_MIXED><<<grid, block, 0, st>>>(P);
+      k_spheres_fix<3><<<32, 128, 0, st>>>(P);  // returns at once when nothing was handed over
+    }
   } else {
-    if (precision == CRG_PREC_F64)
+    if (precision == CRG_PREC_F64) {
       k_spheres_step<2, CRG_PREC_F64><<<grid, block, 0, st>>>(P);
-    else
+    } else {
       k_spheres_step<2, CRG_PREC_MIXED><<<grid, block, 0, st>>>(P);
+      k_spheres_fix<2><<<32, 128, 0, st>>>(P);
+    }
   }
 }
 
