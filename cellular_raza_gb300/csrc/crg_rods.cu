@@ -958,6 +958,7 @@ struct FoldScratch {
   int32_t base[2 * kMaxVertices + 1];   // first sorted position of each chain length
   uint32_t tpass[32];                   // pass index of each lane (pass kernel)
   uint8_t ext[32];                      // lane's pass is ext_a(b)
+  uint8_t phys[32];                     // physical lane of each virtual lane
   uint8_t desc[32 * kMaxVertices];      // sorted units: lane << 3 | row
 };
 
@@ -1013,6 +1014,24 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
       }
     }
   }
+  // Virtual lane order: own passes first, then ext passes (each in lane order), so that all
+  // evaluation batches but one hold a single kind and own-only batches skip the ext
+  // weights.  From here on `lane` indexes virtual lanes; F.phys maps back.
+  {
+    const uint32_t ext_bal = __ballot_sync(0xffffffffu, is_ext);
+    const int n_own = 32 - __popc(ext_bal);
+    const int src = lane < n_own ? (int)__fns(~ext_bal, 0, lane + 1)
+                                 : (int)__fns(ext_bal, 0, lane - n_own + 1);
+    const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, src);
+    const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), src);
+    mask = ((uint64_t)mhi << 32) | mlo;
+    is_ext = lane >= n_own;
+    a = __shfl_sync(0xffffffffu, a, src);
+    b = __shfl_sync(0xffffffffu, b, src);
+    sim = __shfl_sync(0xffffffffu, sim, src);
+    t = __shfl_sync(0xffffffffu, t, src);
+    F.phys[lane] = (uint8_t)src;
+  }
   const int cnt = __popcll(mask);
   int incl = cnt;
 #pragma unroll
@@ -1045,29 +1064,40 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
       const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
       const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
       const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
+      const int jj = j - cs;
+      double tt = 0.0, f[D];
       if (j < ce) {
         const int vs = nth_set_bit64(((uint64_t)mhi << 32) | mlo, j - ex_l);
         const int vx = vs / NE, sy = vs - vx * NE;
         const uint32_t pr = ext_l ? b_l : a_l, sr = ext_l ? a_l : b_l;
-        double p[D], l0[D], l1[D], q[D], t, f[D];
+        double p[D], l0[D], l1[D], q[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) {
           p[c] = P.pos[(vx * D + c) * cap + pr];
           l0[c] = P.pos[(sy * D + c) * cap + sr];
           l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
         }
-        nearest_point_f64<D>(p, l0, l1, q, t);
+        nearest_point_f64<D>(p, l0, l1, q, tt);
         if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
 #pragma unroll
           for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
         }
-        const double omt = dsub(1.0, t);
-        const int jj = j - cs;
+        if (!ext_l) {
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-          const double fe = -f[c];
-          sRes[c * CAP + jj] = ext_l ? dmul(fe, t) : f[c];
-          sRes[(D + c) * CAP + jj] = dmul(fe, omt);
+          for (int c = 0; c < D; ++c) sRes[c * CAP + jj] = f[c];
+        }
+      }
+      // ext items store -f t and -f (1 - t); a batch without ext items skips this
+      const bool ext_item = j < ce && ext_l;
+      if (__any_sync(0xffffffffu, ext_item)) {
+        if (ext_item) {
+          const double omt = dsub(1.0, tt);
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            const double fe = -f[c];
+            sRes[c * CAP + jj] = dmul(fe, tt);
+            sRes[(D + c) * CAP + jj] = dmul(fe, omt);
+          }
         }
       }
     }
@@ -1151,10 +1181,12 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         const double hm = half_exact(m[c]);
-        if (STORE)
+        if (STORE) {
           P.mbuf[(r * D + c) * P.pass_cap + F.tpass[l]] = plus_zero(hm);
-        else
-          sAcc[(r * D + c) * 32 + l] = dadd(sAcc[(r * D + c) * 32 + l], hm);
+        } else {
+          double &acc = sAcc[(r * D + c) * 32 + F.phys[l]];
+          acc = dadd(acc, hm);
+        }
       }
       ++k_unit;
       p = 32 * k_unit + ((k_unit & 1) ? 31 - lane : lane);
