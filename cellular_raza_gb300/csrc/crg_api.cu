@@ -52,6 +52,7 @@ struct crg_ctx {
   int64_t pass_cap = 0;
   uint32_t *rctl = nullptr;
   uint32_t *fix_list = nullptr;  // mixed spheres: agents for the FP64 fix-up kernel
+  double *bend = nullptr;        // rods: curvature forces between the bend and update kernels
   double *frc = nullptr;
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
@@ -264,7 +265,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->rctl, c->fix_list, c->npass, c->pass_off,
+                  c->step_ctr, c->dbg_force, c->frc, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
                   c->staging, c->snap};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -303,6 +304,7 @@ int32_t allocate(crg_ctx *c) {
   }
   if (c->kind == CRG_KIND_ROD) {
     A(frc, cap * nc);
+    A(bend, cap * (c->nv > 2 ? c->nv - 2 : 1) * c->dim);
     A(rctl, 4);
     A(npass, cap);
     A(pass_off, cap);
@@ -418,6 +420,7 @@ PackArgs pack_args(crg_ctx *c) {
   P.frc = c->frc;
   P.rctl = c->rctl;
   P.fix_list = c->fix_list;
+  P.bend = c->bend;
   P.npass = c->npass;
   P.pass_off = c->pass_off;
   P.pass_a = c->pass_a;
@@ -466,7 +469,7 @@ SortArgs sort_args(crg_ctx *c, int initial) {
 // Kernels one launch_force issues: the default rod path runs the pass walk, the pass kernel,
 // the rod-level fallback (returns at once unless the pass list overflowed) and the update.
 int force_kernel_count(const crg_ctx *c) {
-  if (c->kind == CRG_KIND_ROD) return c->variant == 0 ? 4 : 1;
+  if (c->kind == CRG_KIND_ROD) return c->variant == 0 ? (c->nv > 2 ? 5 : 4) : 1;
   return c->precision == CRG_PREC_F64 ? 1 : 2;
 }
 

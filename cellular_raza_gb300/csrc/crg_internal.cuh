@@ -91,6 +91,7 @@ struct PackArgs {
   uint32_t *rctl;  // [0] passes reserved, [1] pass queue, [2] rod queue, [3] pass list
                    // overflow (all zeroed before each step)
   double *frc;     // rods: [nc][cap] interaction force of the rod-level fallback kernel
+  double *bend;    // rods: [nv - 2][dim][cap] curvature forces (k_rods_bend)
   uint32_t *fix_list;  // mixed spheres: agents whose force the FP64 fix-up kernel computes
                        // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)

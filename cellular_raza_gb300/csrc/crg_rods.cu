@@ -183,7 +183,38 @@ __device__ __forceinline__ double norm_f64(const double *v) {
 
 // RodMechanics::calculate_increment (bacterial_rods.rs:157-213), the solver, apply_boundary
 // (:489-534) and the next voxel key from the centroid, for rod i with interaction force acc.
-template <int D, int NV>
+// Curvature force of angle s of a rod (RodMechanics::calculate_increment,
+// bacterial_rods.rs:185-206): f[c] for the vertices s, s + 1, s + 2 from the segments
+// d1 = x_s - x_{s+1} and d2 = x_{s+1} - x_{s+2}.
+template <int D>
+__device__ __forceinline__ void bend_force(const SimDev &S, const double *c1, const double *c2,
+                                           double *f) {
+  double prod = dmul(c1[0], c2[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) prod = dadd(prod, dmul(c1[c], c2[c]));
+  const double n1 = norm_f64<D>(c1), n2 = norm_f64<D>(c2);
+  double angle = 0.0;
+  if (!(n1 == 0.0 || n2 == 0.0)) {
+    double cang = ddiv(prod, dmul(n1, n2));
+    if (cang < -1.0) cang = -1.0;
+    if (cang > 1.0) cang = 1.0;
+    angle = acos(cang);
+  }
+  double fd[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) fd[c] = dsub(c1[c], c2[c]);
+  const double fdn = norm_f64<D>(fd);
+  const double tn = tan(dmul(0.5, angle));
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const double fdir = (fdn != 0.0) ? ddiv(fd[c], fdn) : fd[c];
+    f[c] = dmul(dmul(dmul(fdir, 2.0), S.rigidity), tn);
+  }
+}
+
+// BEND: the curvature forces were computed by k_rods_bend (P.bend), else they are computed
+// here.  Same values, same order of additions either way.
+template <int D, int NV, bool BEND = false>
 __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, uint32_t i,
                                            uint32_t key, const double *pa, const double *acc) {
   constexpr int NC = NV * D;
@@ -220,28 +251,16 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   // curvature: Matrix::angle = acos(clamp(dot / (|a| |b|), -1, 1)), 0 for zero length
 #pragma unroll
   for (int s = 0; s + 2 < NV; ++s) {
-    const double *c1 = dist[s];
-    const double *c2 = dist[s + 1];
-    double prod = dmul(c1[0], c2[0]);
+    double fb[D];
+    if (BEND) {
 #pragma unroll
-    for (int c = 1; c < D; ++c) prod = dadd(prod, dmul(c1[c], c2[c]));
-    const double n1 = norm_f64<D>(c1), n2 = norm_f64<D>(c2);
-    double angle = 0.0;
-    if (!(n1 == 0.0 || n2 == 0.0)) {
-      double cang = ddiv(prod, dmul(n1, n2));
-      if (cang < -1.0) cang = -1.0;
-      if (cang > 1.0) cang = 1.0;
-      angle = acos(cang);
+      for (int c = 0; c < D; ++c) fb[c] = P.bend[(s * D + c) * cap + i];
+    } else {
+      bend_force<D>(S, dist[s], dist[s + 1], fb);
     }
-    double fd[D];
-#pragma unroll
-    for (int c = 0; c < D; ++c) fd[c] = dsub(c1[c], c2[c]);
-    const double fdn = norm_f64<D>(fd);
-    const double tn = tan(dmul(0.5, angle));
 #pragma unroll
     for (int c = 0; c < D; ++c) {
-      const double fdir = (fdn != 0.0) ? ddiv(fd[c], fdn) : fd[c];
-      const double f = dmul(dmul(dmul(fdir, 2.0), S.rigidity), tn);
+      const double f = fb[c];
       tf[s * D + c] = dadd(tf[s * D + c], dmul(-f, 0.5));
       tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], f);
       tf[(s + 2) * D + c] = dadd(tf[(s + 2) * D + c], dmul(-f, 0.5));
@@ -1754,6 +1773,35 @@ __global__ void __launch_bounds__(32, 24) k_rods_passq(const PackArgs P) {
   }
 }
 
+// Curvature forces of every angle of every live rod, one thread per (angle, rod), into
+// P.bend [NV - 2][D][cap] for k_rods_update (the acos / tan work, spread over more threads
+// than the per-rod update can keep resident).
+template <int D, int NV>
+__global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t n = P.n_agents;
+  if (g >= (uint64_t)n * (NV - 2)) return;
+  const int s = (int)(g / n);
+  const uint32_t i = (uint32_t)(g - (uint64_t)s * n);
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  if (*P.step_ctr >= S.stop_step) return;  // frozen: copied by k_rods_update
+  const int64_t cap = P.cap;
+  double x[3][D], c1[D], c2[D], f[D];
+#pragma unroll
+  for (int v = 0; v < 3; ++v)
+#pragma unroll
+    for (int c = 0; c < D; ++c) x[v][c] = P.pos[((s + v) * D + c) * cap + i];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    c1[c] = dsub(x[0][c], x[1][c]);
+    c2[c] = dsub(x[1][c], x[2][c]);
+  }
+  bend_force<D>(S, c1, c2, f);
+#pragma unroll
+  for (int c = 0; c < D; ++c) P.bend[(s * D + c) * cap + i] = f[c];
+}
+
 // Mechanics, solver, boundary and next key of every rod from its interaction force: the
 // sum, in pass order, of the M / 2 that k_rods_passq stored for its passes (rows a pass
 // does not touch are +0, which leaves the sum unchanged since it is never -0), or, after a
@@ -1790,7 +1838,7 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
       for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], mb[k * pcap + p]);
     }
   }
-  rod_update<D, NV>(P, S, i, key, pa, acc);
+  rod_update<D, NV, true>(P, S, i, key, pa, acc);
 }
 
 // Candidate rods of the current cell list, a hash of their ids and the number of in-range
@@ -1886,6 +1934,10 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0, cud
   k_rods_passq<D, NV><<<pgrid, 32, passq_smem_bytes<D, NV>(), st>>>(P);
   if (k1) cudaEventRecord(k1, st);
   k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);  // only on overflow
+  if (NV > 2) {
+    const uint64_t nb = ((uint64_t)P.n_agents * (NV - 2) + 127) / 128;
+    k_rods_bend<D, NV><<<(unsigned)nb, 128, 0, st>>>(P);
+  }
   k_rods_update<D, NV><<<rblocks, 128, 0, st>>>(P);
 }
 
