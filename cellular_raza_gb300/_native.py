@@ -12,7 +12,9 @@ from . import build as _build
 
 CRG_OK, CRG_ECALC, CRG_EBOUNDARY, CRG_EINDEX, CRG_EDECOMPOSE = 0, 1, 2, 3, 4
 CRG_EINVAL, CRG_ENOMEM, CRG_ECUDA, CRG_ETIMEDOUT, CRG_ENOTSUP = 5, 6, 7, 8, 9
-KIND_SPHERE, KIND_ROD = 0, 1
+KIND_SPHERE, KIND_ROD, KIND_BROWNIAN, KIND_LANGEVIN = 0, 1, 2, 3
+KINDS = {"sphere": KIND_SPHERE, "rod": KIND_ROD, "brownian": KIND_BROWNIAN,
+         "langevin": KIND_LANGEVIN}
 PREC_F64, PREC_MIXED = 0, 1
 WEIGHTS_CHILI, WEIGHTS_PHYSICAL = 0, 1
 OPT_PREFILTER, OPT_GRAPH_CHUNK, OPT_BLOCK, OPT_PROFILE, OPT_DEBUG_FORCES = 1, 2, 3, 4, 5
@@ -63,6 +65,8 @@ class CrgModel(C.Structure):
         ("cutoff", C.c_double),
         ("strength", C.c_double),
         ("dt", C.c_double),
+        ("kb_temperature", C.c_double),
+        ("rng_seed", C.c_uint64),
     ]
 
 

@@ -170,6 +170,12 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.stiffness = m.stiffness;
   S.cutoff = m.cutoff;
   S.strength = m.strength;
+  S.mech = m.kind == CRG_KIND_BROWNIAN ? 1 : m.kind == CRG_KIND_LANGEVIN ? 2 : 0;
+  S.diffusion = m.diffusion;
+  S.kb_temperature = m.kb_temperature;
+  S.rng_seed = m.rng_seed;
+  S.stochastic = (m.kind == CRG_KIND_BROWNIAN || m.kind == CRG_KIND_LANGEVIN ||
+                  (m.kind == CRG_KIND_ROD && m.diffusion != 0.0)) ? 1 : 0;
   S.mrs_r = m.radius + m.radius;
   S.mrs_k = (-2.0 * m.strength) * m.stiffness;
   S.mrs_nstiff = -m.stiffness;
@@ -208,14 +214,16 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
 }
 
 int32_t check_model(const crg_model &m) {
-  if (m.kind != CRG_KIND_SPHERE && m.kind != CRG_KIND_ROD) return CRG_EINVAL;
-  if (m.kind == CRG_KIND_SPHERE && m.n_vertices != 1) return CRG_EINVAL;
+  if (m.kind < CRG_KIND_SPHERE || m.kind > CRG_KIND_LANGEVIN) return CRG_EINVAL;
+  if (m.kind != CRG_KIND_ROD && m.n_vertices != 1) return CRG_EINVAL;
   if (m.kind == CRG_KIND_ROD && (m.n_vertices < 2 || m.n_vertices > crg::kMaxVertices))
     return CRG_ENOTSUP;
   if (m.solver_order < 1 || m.solver_order > 3) return CRG_EINVAL;
   if (m.precision != CRG_PREC_F64 && m.precision != CRG_PREC_MIXED) return CRG_EINVAL;
   if (m.kind == CRG_KIND_ROD && m.precision != CRG_PREC_F64) return CRG_ENOTSUP;
-  if (m.diffusion != 0.0) return CRG_ENOTSUP;  // stochastic mechanics is not on this path
+  // NewtonDamped has no diffusion; Brownian divides by k_B T (mechanics.rs:354)
+  if (m.kind == CRG_KIND_SPHERE && m.diffusion != 0.0) return CRG_EINVAL;
+  if (m.kind == CRG_KIND_BROWNIAN && !(m.kb_temperature != 0.0)) return CRG_EINVAL;
   if (!(m.dt > 0.0)) return CRG_EINVAL;
   return CRG_OK;
 }
@@ -341,7 +349,7 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
   if (!c) return CRG_ENOMEM;
   const crg_model &m0 = models[0];
   c->dim = domains[0].dim;
-  c->kind = m0.kind;
+  c->kind = m0.kind == CRG_KIND_ROD ? CRG_KIND_ROD : CRG_KIND_SPHERE;  // point agents
   c->nv = m0.kind == CRG_KIND_ROD ? m0.n_vertices : 1;
   c->nc = c->nv * c->dim;
   c->precision = m0.precision;

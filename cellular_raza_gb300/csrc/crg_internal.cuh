@@ -38,6 +38,11 @@ struct SimDev {
   // Morse terms that do not depend on the pair, each rounded exactly as the per-pair
   // expression rounds them: radius + radius, (-2 * strength) * stiffness, -stiffness.
   double mrs_r, mrs_k, mrs_nstiff;
+  // Mechanics of point agents: 0 NewtonDamped, 1 Brownian, 2 Langevin; stochastic terms.
+  int32_t mech;
+  int32_t stochastic;  // Brownian, Langevin, or RodMechanics with diffusion != 0
+  double diffusion, kb_temperature;
+  uint64_t rng_seed;
   // cutoff as an integer threshold on the bit pattern of a distance d >= 0 (not NaN):
   // d > cutoff exactly when bits(d) > cutoff_bits.
   int64_t cutoff_bits;
@@ -103,6 +108,46 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// ---- random stream of the stochastic mechanics --------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11): ten rounds of two 32x32->64 multiplies with the round keys bumped by the Weyl
+// constants.
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+    const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = lo1;
+    c[2] = n2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+// The standard normals z[0..N) of agent `id` at pack step `step`: block j (counter
+// {j, step, id_lo, id_hi}) gives u1 in (0, 1] and u2 in [0, 1) with 53 bits each, then
+// Box-Muller sqrt(-2 ln u1) (cos, sin)(2 pi u2).  The CPU oracle draws the same stream.
+template <int N>
+__device__ __forceinline__ void stream_normals(uint64_t seed, uint64_t step, uint64_t id,
+                                               double *z) {
+  const double two_pi = 6.283185307179586;
+  const double inv53 = 1.0 / 9007199254740992.0;  // 2^-53
+#pragma unroll
+  for (int j = 0; 2 * j < N; ++j) {
+    uint32_t w[4] = {(uint32_t)j, (uint32_t)step, (uint32_t)id, (uint32_t)(id >> 32)};
+    philox4x32_10(w, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double u1 = (double)((((uint64_t)w[0] << 21) | (w[1] >> 11)) + 1) * inv53;
+    const double u2 = (double)(((uint64_t)w[2] << 21) | (w[3] >> 11)) * inv53;
+    const double r = __dsqrt_rn(__dmul_rn(-2.0, log(u1)));
+    const double th = __dmul_rn(two_pi, u2);
+    z[2 * j] = __dmul_rn(r, cos(th));
+    if (2 * j + 1 < N) z[2 * j + 1] = __dmul_rn(r, sin(th));
+  }
+}
 
 // num::ToPrimitive::to_usize for f64: truncation toward zero on the open interval
 // (-1, 2^64); everything else (NaN included) has no value.

@@ -270,13 +270,26 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 #pragma unroll
   for (int k = 0; k < NC; ++k) tf[k] = dsub(tf[k], dmul(va[k], S.damping));
 
+  // get_random_contribution times dt (bacterial_rods.rs:215-240): dx_rand = N(0, sqrt(dt))
+  // * 2^-2 * D / dt per vertex coordinate, dv_rand = 0; zero when D = 0.
+  const double dt = S.dt;
+  double rx[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) rx[k] = 0.0;
+  if (S.stochastic) {
+    double z[NC];
+    stream_normals<NC>(S.rng_seed, (uint64_t)*P.step_ctr, P.id[i], z);
+    const double sd = __dsqrt_rn(dt);
+#pragma unroll
+    for (int k = 0; k < NC; ++k)
+      rx[k] = dmul(ddiv(dmul(dmul(dadd(0.0, dmul(sd, z[k])), 0.25), S.diffusion), dt), dt);
+  }
   // solver (dx = v, dv = total force)
   double np[NC], nvl[NC];
-  const double dt = S.dt;
   if (S.order == 1) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
-      np[k] = dadd(dadd(dmul(va[k], dt), pa[k]), 0.0);
+      np[k] = dadd(dadd(dmul(va[k], dt), pa[k]), rx[k]);
       nvl[k] = dadd(dadd(dmul(tf[k], dt), va[k]), 0.0);
     }
   } else {
@@ -287,12 +300,12 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
         const double f0 = 23.0 / 12.0, f1 = -16.0 / 12.0, f2 = 5.0 / 12.0;
         const double px = P.hist[k * cap + i], pv = P.hist[(NC + k) * cap + i];
         np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dadd(dmul(px, f1), dmul(va[k], f2))), dt),
-                          pa[k]), 0.0);
+                          pa[k]), rx[k]);
         nvl[k] = dadd(dadd(dmul(dadd(dmul(tf[k], f0), dadd(dmul(pv, f1), dmul(tf[k], f2))), dt),
                            va[k]), 0.0);
       } else {
         const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
-        np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dmul(va[k], f1)), dt), pa[k]), 0.0);
+        np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dmul(va[k], f1)), dt), pa[k]), rx[k]);
         nvl[k] = dadd(dadd(dmul(dadd(dmul(tf[k], f0), dmul(tf[k], f1)), dt), va[k]), 0.0);
       }
       P.nhist[k * cap + i] = va[k];

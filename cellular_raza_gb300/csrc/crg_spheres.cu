@@ -96,23 +96,63 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
     for (int c = 0; c < D; ++c) P.dbg_force[c * cap + i] = acc[c];
   }
 
-  // NewtonDamped::calculate_increment (mechanics.rs:166-173): dx = v, dv = F/m - lambda v.
+  // Mechanics::calculate_increment.  NewtonDamped (mechanics.rs:166-173): dx = v,
+  // dv = F/m - lambda v.  Brownian (:350-357): dx = D / k_B T * F, dv = 0.  Langevin
+  // (:452-463): dx = v, dv = 1 / M * F + (-gamma) * v.
   double dxv[D], dvv[D];
+  if (S.mech == 1) {
+    const double sb = ddiv(S.diffusion, S.kb_temperature);
 #pragma unroll
-  for (int c = 0; c < D; ++c) {
-    dxv[c] = va[c];
-    dvv[c] = dsub(ddiv(acc[c], S.mass), dmul(S.damping, va[c]));
+    for (int c = 0; c < D; ++c) {
+      dxv[c] = dmul(sb, acc[c]);
+      dvv[c] = 0.0;
+    }
+  } else if (S.mech == 2) {
+    const double im = ddiv(1.0, S.mass);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      dxv[c] = va[c];
+      dvv[c] = dadd(dmul(im, acc[c]), dmul(-S.damping, va[c]));
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      dxv[c] = va[c];
+      dvv[c] = dsub(ddiv(acc[c], S.mass), dmul(S.damping, va[c]));
+    }
   }
-  // Solvers (chili/solvers.rs:23-55, 156-347).  The random contribution is zero
-  // (mechanics.rs:158-164), so the final `.xapy(1, dx_rand * dt)` adds +0.
-  double np[D], nvl[D];
+  // get_random_contribution times dt, as the solvers add it (`.xapy(1, dx_rand * dt)`):
+  // zero for NewtonDamped (mechanics.rs:158-164); Brownian dx_rand = sqrt(2 D) *
+  // N(0, sqrt(dt)) / dt (:336-348 with wiener_process :211-226); Langevin dv_rand =
+  // sqrt(2 gamma k_B T / M) * N(0, sqrt(dt)) / dt (:434-450).  N(0, s) = 0 + s z.
   const double dt = S.dt;
+  double rx[D], rv[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) rx[c] = rv[c] = 0.0;
+  if (S.stochastic) {
+    double z[D];
+    stream_normals<D>(S.rng_seed, (uint64_t)*P.step_ctr, P.id[i], z);
+    const double sd = __dsqrt_rn(dt);
+    const double amp = (S.mech == 1)
+                           ? __dsqrt_rn(dmul(2.0, S.diffusion))
+                           : __dsqrt_rn(ddiv(dmul(dmul(2.0, S.damping), S.kb_temperature), S.mass));
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const double r = dmul(dmul(amp, ddiv(dadd(0.0, dmul(sd, z[c])), dt)), dt);
+      if (S.mech == 1)
+        rx[c] = r;
+      else
+        rv[c] = r;
+    }
+  }
+  // Solvers (chili/solvers.rs:23-55, 156-347).
+  double np[D], nvl[D];
   uint8_t meta = 0;
   if (S.order == 1) {
 #pragma unroll
     for (int c = 0; c < D; ++c) {
-      np[c] = dadd(dadd(dmul(dxv[c], dt), pa[c]), 0.0);
-      nvl[c] = dadd(dadd(dmul(dvv[c], dt), va[c]), 0.0);
+      np[c] = dadd(dadd(dmul(dxv[c], dt), pa[c]), rx[c]);
+      nvl[c] = dadd(dadd(dmul(dvv[c], dt), va[c]), rv[c]);
     }
   } else {
     // The history is pushed before it is read (solvers.rs:178-185), so the newest stored
@@ -126,13 +166,13 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
         const double f0 = 23.0 / 12.0, f1 = -16.0 / 12.0, f2 = 5.0 / 12.0;
         const double px = P.hist[c * cap + i], pv = P.hist[(D + c) * cap + i];
         np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dadd(dmul(px, f1), dmul(dxv[c], f2))), dt),
-                          pa[c]), 0.0);
+                          pa[c]), rx[c]);
         nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dadd(dmul(pv, f1), dmul(dvv[c], f2))), dt),
-                           va[c]), 0.0);
+                           va[c]), rv[c]);
       } else {
         const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
-        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dmul(dxv[c], f1)), dt), pa[c]), 0.0);
-        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dmul(dvv[c], f1)), dt), va[c]), 0.0);
+        np[c] = dadd(dadd(dmul(dadd(dmul(dxv[c], f0), dmul(dxv[c], f1)), dt), pa[c]), rx[c]);
+        nvl[c] = dadd(dadd(dmul(dadd(dmul(dvv[c], f0), dmul(dvv[c], f1)), dt), va[c]), rv[c]);
       }
       P.nhist[c * cap + i] = dxv[c];
       P.nhist[(D + c) * cap + i] = dvv[c];
@@ -158,6 +198,10 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
   for (int c = 0; c < D; ++c)
     if (np[c] < S.min[c] || np[c] > S.max[c]) inside = false;
   if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1, S.sim_index);
+  if (S.mech == 1) {  // Brownian::set_velocity is a no-op: the velocity stays as it was
+#pragma unroll
+    for (int c = 0; c < D; ++c) nvl[c] = va[c];
+  }
 #pragma unroll
   for (int c = 0; c < D; ++c) {
     P.npos[c * cap + i] = np[c];

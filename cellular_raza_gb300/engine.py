@@ -33,13 +33,14 @@ def to_c(model: Model):
     d.n_subdomains = int(model.n_subdomains)
     d.weight_mode = int(model.weight_mode)
     m = N.CrgModel()
-    m.kind = N.KIND_ROD if model.kind == "rod" else N.KIND_SPHERE
+    m.kind = N.KINDS[model.kind]
     m.n_vertices = int(model.n_vertices)
     m.solver_order = int(model.solver_order)
     m.precision = N.PREC_MIXED if model.precision == "mixed" else N.PREC_F64
     for f in ("mass", "damping", "spring_tension", "rigidity", "spring_length", "diffusion",
-              "radius", "stiffness", "cutoff", "strength", "dt"):
+              "radius", "stiffness", "cutoff", "strength", "dt", "kb_temperature"):
         setattr(m, f, float(getattr(model, f)))
+    m.rng_seed = int(model.rng_seed)
     return d, m
 
 

@@ -29,7 +29,7 @@ DENSITY_3D = 4096 / 200.0 ** 3  # 5.12e-4 agents per unit^3
 class Model:
     """Domain + agent parameters of one simulation (mirrors crg_domain + crg_model)."""
 
-    kind: str = "sphere"  # "sphere" | "rod"
+    kind: str = "sphere"  # "sphere" (NewtonDamped) | "rod" | "brownian" | "langevin"
     dim: int = 3
     n_vertices: int = 1
     domain_min: Tuple[float, ...] = (0.0, 0.0, 0.0)
@@ -40,14 +40,17 @@ class Model:
     weight_mode: int = 0  # 0 chili weights, 1 physical
     solver_order: int = 1  # 1 Euler, 2 AB2, 3 AB3
     precision: str = "f64"  # "f64" | "mixed"
-    # NewtonDamped
+    # NewtonDamped / Langevin (mass, damping gamma)
     mass: float = 1.0
     damping: float = 1.5
+    # Brownian / Langevin k_B T; seed of the stochastic mechanics' random stream
+    kb_temperature: float = 0.0
+    rng_seed: int = 0
     # RodMechanics
     spring_tension: float = 0.0
     rigidity: float = 0.0
     spring_length: float = 0.0
-    diffusion: float = 0.0
+    diffusion: float = 0.0  # RodMechanics / Brownian diffusion constant
     # MorsePotential
     radius: float = 5.0
     stiffness: float = 0.4

@@ -45,8 +45,16 @@ extern "C" {
 #define CRG_EINTERNAL 10  /* a device-side invariant check failed; the access was skipped
                              (crg_last_error: agent = index, step = check site) */
 
-#define CRG_KIND_SPHERE 0 /* NewtonDamped{2,3}D + MorsePotential */
-#define CRG_KIND_ROD 1    /* RodMechanics<f64,D> + RodInteraction<MorsePotential> */
+#define CRG_KIND_SPHERE 0   /* NewtonDamped{2,3}D + MorsePotential */
+#define CRG_KIND_ROD 1      /* RodMechanics<f64,D> + RodInteraction<MorsePotential> */
+#define CRG_KIND_BROWNIAN 2 /* Brownian{2,3}D + MorsePotential (mechanics.rs:228-374) */
+#define CRG_KIND_LANGEVIN 3 /* Langevin{2,3}D + MorsePotential (mechanics.rs:376-475) */
+/* Stochastic mechanics (Brownian, Langevin, RodMechanics with diffusion != 0) draw their
+ * Wiener increments from a counter-based stream: Philox4x32-10 keyed by rng_seed, counter
+ * (draw, pack step, agent id), Box-Muller normals.  The reference's per-voxel ChaCha8
+ * streams (chili/datastructures.rs:180-182) are replaced, so results match the reference
+ * in distribution, and a simulation's random stream does not depend on its voxel, its
+ * subdomain or its batch neighbours. */
 
 #define CRG_PREC_F64 0    /* every operation in FP64, in the reference's order */
 #define CRG_PREC_MIXED 1  /* FP32 pair forces with Kahan sums; FP64 state and update */
@@ -85,6 +93,8 @@ typedef struct crg_model {
   double spring_tension, rigidity, spring_length, diffusion;
   double radius, stiffness, cutoff, strength;
   double dt;
+  double kb_temperature; /* Brownian / Langevin k_B T */
+  uint64_t rng_seed;     /* seed of the stochastic mechanics' random stream */
 } crg_model;
 
 typedef struct crg_ctx crg_ctx;

@@ -255,7 +255,57 @@ struct Params {
   double mass, damping, spring_tension, rigidity, spring_length;
   double radius, stiffness, cutoff, strength, dt;
   int order;
+  int kind;  // OR_KIND_*
+  double diffusion, kb_temperature;
+  uint64_t seed;
 };
+
+// ---------------------------------------------------------------------------------
+// Random stream of the stochastic mechanics.  The reference draws from per-voxel
+// ChaCha8Rng streams (chili/datastructures.rs:180-182) through rand_distr::Normal; those
+// crates are not available here, so the oracle and the GPU path share a counter-based
+// stream instead: Philox4x32-10 keyed by the seed, counter (draw, step, agent id), and
+// Box-Muller normals.  Parity with the reference is statistical (diffusion constant,
+// equipartition); with the GPU path it is exact up to libm rounding.
+// ---------------------------------------------------------------------------------
+inline void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+// n standard normals for agent id at step: block j (counter {j, step, id_lo, id_hi}) gives
+// u1 in (0, 1] and u2 in [0, 1) with 53 bits each, then sqrt(-2 ln u1) (cos, sin)(2 pi u2).
+inline void normals(uint64_t seed, uint64_t step, uint64_t id, int n, double *out) {
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  const double two_pi = 6.283185307179586;
+  const double inv53 = 1.0 / 9007199254740992.0;  // 2^-53
+  for (int j = 0; 2 * j < n; ++j) {
+    const uint32_t ctr[4] = {(uint32_t)j, (uint32_t)step, (uint32_t)id, (uint32_t)(id >> 32)};
+    uint32_t w[4];
+    philox4x32_10(ctr, key, w);
+    const double u1 = (double)((((uint64_t)w[0] << 21) | (w[1] >> 11)) + 1) * inv53;
+    const double u2 = (double)(((uint64_t)w[2] << 21) | (w[3] >> 11)) * inv53;
+    const double r = std::sqrt(-2.0 * std::log(u1));
+    const double th = two_pi * u2;
+    out[2 * j] = r * std::cos(th);
+    if (2 * j + 1 < n) out[2 * j + 1] = r * std::sin(th);
+  }
+}
 
 // ---------------------------------------------------------------------------------
 // Simulation (chili SubDomainBox machinery)
@@ -319,6 +369,7 @@ struct Sim {
   // debug capture of the last step
   bool want_debug = false;
   std::vector<double> dbg_force;  // indexed by id
+  int64_t step_base = 0;          // steps run by earlier calls (random stream index)
   int64_t n_agents = 0;
 
   static void zero(double *x) {
@@ -483,9 +534,25 @@ struct Sim {
   // Rods: RodMechanics (bacterial_rods.rs:157-213).
   void increment(const Cell &c, const double *force, double *dx, double *dv) const {
     if constexpr (NV == 1) {
-      for (int k = 0; k < NC; ++k) {
-        dx[k] = c.vel[k];
-        dv[k] = force[k] / prm.mass - prm.damping * c.vel[k];
+      if (prm.kind == OR_KIND_BROWNIAN) {
+        // Brownian: dx = D / k_B T * F, dv = 0 (mechanics.rs:350-357)
+        const double s = prm.diffusion / prm.kb_temperature;
+        for (int k = 0; k < NC; ++k) {
+          dx[k] = s * force[k];
+          dv[k] = 0.0;
+        }
+      } else if (prm.kind == OR_KIND_LANGEVIN) {
+        // Langevin: dx = v, dv = 1 / M * F + (-gamma) * v (mechanics.rs:452-463)
+        const double im = 1.0 / prm.mass;
+        for (int k = 0; k < NC; ++k) {
+          dx[k] = c.vel[k];
+          dv[k] = im * force[k] + (-prm.damping) * c.vel[k];
+        }
+      } else {
+        for (int k = 0; k < NC; ++k) {
+          dx[k] = c.vel[k];
+          dv[k] = force[k] / prm.mass - prm.damping * c.vel[k];
+        }
       }
     } else {
       const double one_half = 1.0 / (1.0 + 1.0);
@@ -563,12 +630,37 @@ struct Sim {
     std::memcpy(a.hv[slot], dv, sizeof(double) * NC);
   }
 
+  // Mechanics::get_random_contribution, times dt as the solvers add it (x' = (dx dt + x) 1
+  // + dx_rand dt).  NewtonDamped: zero (mechanics.rs:158-164).  Brownian: dx_rand =
+  // sqrt(2 D) * N(0, sqrt(dt)) / dt (:336-348, wiener_process :211-226).  Langevin: dv_rand
+  // = sqrt(2 gamma k_B T / M) * N(0, sqrt(dt)) / dt (:434-450).  RodMechanics: dx_rand =
+  // N(0, sqrt(dt)) * 2^-2 * D / dt per vertex (bacterial_rods.rs:215-240).  A normal draw
+  // N(0, sigma) is 0 + sigma * z (rand_distr::Normal).
+  void random_terms(const Cell &c, int64_t step, double *rx, double *rv) const {
+    const double dt = prm.dt;
+    for (int k = 0; k < NC; ++k) rx[k] = rv[k] = 0.0 * dt;
+    const bool rod_diffusion = NV > 1 && prm.diffusion != 0.0;
+    if (!(prm.kind == OR_KIND_BROWNIAN || prm.kind == OR_KIND_LANGEVIN || rod_diffusion)) return;
+    double z[NC];
+    normals(prm.seed, (uint64_t)step, c.id, NC, z);
+    const double sd = std::sqrt(dt);
+    for (int k = 0; k < NC; ++k) {
+      const double w = 0.0 + sd * z[k];
+      if (prm.kind == OR_KIND_BROWNIAN) {
+        rx[k] = (std::sqrt(2.0 * prm.diffusion) * (w / dt)) * dt;
+      } else if (prm.kind == OR_KIND_LANGEVIN) {
+        const double s = std::sqrt(2.0 * prm.damping * prm.kb_temperature / prm.mass);
+        rv[k] = (s * (w / dt)) * dt;
+      } else {
+        rx[k] = (w * 0.25 * prm.diffusion / dt) * dt;
+      }
+    }
+  }
+
   // local_mechanics_update (update_mechanics.rs:530-559) -> mechanics_euler /
   // mechanics_adams_bashforth_2 / _3 (chili/solvers.rs:23-55, 156-300) with the
-  // euler / adams_bashforth_{2,3} kernels (solvers.rs:303-347).  NewtonDamped and
-  // RodMechanics(diffusion 0) return zero random contributions (mechanics.rs:158-164,
-  // bacterial_rods.rs:215-240), so dx_rand = 0.
-  void mechanics_update(Entry &e, int64_t *dbg_slot) {
+  // euler / adams_bashforth_{2,3} kernels (solvers.rs:303-347).
+  void mechanics_update(Entry &e, int64_t step, int64_t *dbg_slot) {
     double force[NC];
     std::memcpy(force, e.a.force, sizeof(force));
     zero(e.a.force);  // get_current_force_and_reset
@@ -577,7 +669,8 @@ struct Sim {
     increment(e.c, force, dx, dv);
     const double dt = prm.dt;
     const double one = 1.0;
-    const double rnd = 0.0 * dt;  // dx_rand.xa(dt) with dx_rand = 0
+    double rx[NC], rv[NC];  // dx_rand.xa(dt), dv_rand.xa(dt)
+    random_terms(e.c, step, rx, rv);
     // set_last_position/velocity run BEFORE the history is read, so the newest stored
     // increment is the current one: AB2 always sees [dx, dx]; AB3 sees [dx, dx] on its
     // first step and [dx, oldest, newest(=dx)] afterwards.
@@ -590,34 +683,35 @@ struct Sim {
       const double *ov1 = e.a.hv[e.a.first], *ov2 = e.a.hv[(e.a.first + 1) % 2];
       for (int k = 0; k < NC; ++k) {
         np[k] = (dx[k] * f0 + (ox1[k] * f1 + ox2[k] * f2)) * dt + e.c.pos[k];
-        np[k] = np[k] * one + rnd;
+        np[k] = np[k] * one + rx[k];
         nv[k] = (dv[k] * f0 + (ov1[k] * f1 + ov2[k] * f2)) * dt + e.c.vel[k];
-        nv[k] = nv[k] * one + rnd;
+        nv[k] = nv[k] * one + rv[k];
       }
     } else if (cap >= 1 && n_prev == 1) {
       const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
       const double *ox = e.a.hx[e.a.first], *ov = e.a.hv[e.a.first];
       for (int k = 0; k < NC; ++k) {
         np[k] = (dx[k] * f0 + ox[k] * f1) * dt + e.c.pos[k];
-        np[k] = np[k] * one + rnd;
+        np[k] = np[k] * one + rx[k];
         nv[k] = (dv[k] * f0 + ov[k] * f1) * dt + e.c.vel[k];
-        nv[k] = nv[k] * one + rnd;
+        nv[k] = nv[k] * one + rv[k];
       }
     } else {
       for (int k = 0; k < NC; ++k) {
-        np[k] = (dx[k] * dt + e.c.pos[k]) * one + rnd;
-        nv[k] = (dv[k] * dt + e.c.vel[k]) * one + rnd;
+        np[k] = (dx[k] * dt + e.c.pos[k]) * one + rx[k];
+        nv[k] = (dv[k] * dt + e.c.vel[k]) * one + rv[k];
       }
     }
     std::memcpy(e.c.pos, np, sizeof(np));
-    std::memcpy(e.c.vel, nv, sizeof(nv));
+    // Brownian::set_velocity is a no-op: the velocity stays zero
+    if (!(NV == 1 && prm.kind == OR_KIND_BROWNIAN)) std::memcpy(e.c.vel, nv, sizeof(nv));
   }
 
-  void update_local(int s, bool last) {
+  void update_local(int s, bool last, int64_t step) {
     Box &b = boxes[s];
     int64_t dummy = 0;
     for (Voxel &v : b.voxels)
-      for (Entry &e : v.cells) mechanics_update(e, (last && want_debug) ? &dummy : nullptr);
+      for (Entry &e : v.cells) mechanics_update(e, step, (last && want_debug) ? &dummy : nullptr);
   }
 
   // SubDomainMechanics::apply_boundary (cartesian_cuboid_n.rs:594-631; rods:
@@ -625,17 +719,19 @@ struct Sim {
   // (update_mechanics.rs:387-406).
   bool reflect(Cell &c) const {
     const double two = 1.0 + 1.0;
+    // Brownian::set_velocity is a no-op, so the reflection leaves its velocity alone
+    const bool keep_vel = NV == 1 && prm.kind == OR_KIND_BROWNIAN;
     for (int v = 0; v < NV; ++v) {
       double *p = c.pos + v * D;
       double *u = c.vel + v * D;
       for (int i = 0; i < D; ++i) {
         if (p[i] < dom.min[i]) {
           p[i] = (NV == 1) ? two * dom.min[i] - p[i] : dom.min[i] * two - p[i];
-          u[i] = std::fabs(u[i]);
+          if (!keep_vel) u[i] = std::fabs(u[i]);
         }
         if (p[i] > dom.max[i]) {
           p[i] = (NV == 1) ? two * dom.max[i] - p[i] : dom.max[i] * two - p[i];
-          u[i] = -std::fabs(u[i]);
+          if (!keep_vel) u[i] = -std::fabs(u[i]);
         }
       }
     }
@@ -840,7 +936,7 @@ struct Sim {
       if (b.error == OR_OK) step2(s);
       if (bar) bar->arrive_and_wait();
       if (b.error == OR_OK) step3(s);
-      if (b.error == OR_OK) update_local(s, last);
+      if (b.error == OR_OK) update_local(s, last, step_base + step - 1);
       if (b.error == OR_OK) boundary(s);
       if (b.error == OR_OK) sort1(s);
       if (bar) bar->arrive_and_wait();
@@ -859,6 +955,10 @@ struct Sim {
     if (want_debug) dbg_force.assign((size_t)n_agents * NC, 0.0);
     auto go = [&](int64_t steps) {
       if (steps <= 0) return;
+      struct Advance {  // the random stream's step index continues across calls
+        int64_t &base, n;
+        ~Advance() { base += n; }
+      } adv{step_base, steps};
       if (S == 1) {
         worker(0, steps, nullptr, &err_steps[0]);
       } else {
@@ -921,9 +1021,10 @@ int32_t run_t(const or_config &cfg, const Domain &dom, int64_t n, double *pos, d
               int64_t n_steps, or_debug *dbg, double *elapsed) {
   auto sim = std::make_unique<Sim<D, NV>>();
   sim->dom = dom;
-  sim->prm = Params{cfg.mass,   cfg.damping,   cfg.spring_tension, cfg.rigidity,
+  sim->prm = Params{cfg.mass,      cfg.damping,   cfg.spring_tension, cfg.rigidity,
                     cfg.spring_length, cfg.radius, cfg.stiffness, cfg.cutoff,
-                    cfg.strength, cfg.dt,    cfg.solver_order};
+                    cfg.strength,  cfg.dt,        cfg.solver_order, cfg.kind,
+                    cfg.diffusion, cfg.kb_temperature, cfg.rng_seed};
   sim->cap = cfg.solver_order - 1;
   int r = sim->setup(cfg, n, pos, vel);
   if (r) return r;
@@ -977,11 +1078,14 @@ int32_t or_run(const or_config *cfg, int64_t n_agents, double *pos, double *vel,
   if (!cfg || n_agents < 0 || n_steps < 0) return OR_EINVAL;
   if (cfg->solver_order < 1 || cfg->solver_order > 3) return OR_EINVAL;
   if (cfg->n_subdomains < 1) return OR_EINVAL;
-  if (cfg->diffusion != 0.0) return OR_EINVAL;  // stochastic mechanics: out of scope
+  if ((cfg->kind == OR_KIND_BROWNIAN && !(cfg->kb_temperature != 0.0)) ||
+      (cfg->kind == OR_KIND_SPHERE && cfg->diffusion != 0.0))
+    return OR_EINVAL;
   Domain dom;
   int r = make_domain(*cfg, dom);
   if (r) return r;
-  if (cfg->kind == OR_KIND_SPHERE) {
+  if (cfg->kind == OR_KIND_SPHERE || cfg->kind == OR_KIND_BROWNIAN ||
+      cfg->kind == OR_KIND_LANGEVIN) {
     if (cfg->dim == 2) return run_t<2, 1>(*cfg, dom, n_agents, pos, vel, n_steps, dbg, elapsed_s);
     return run_t<3, 1>(*cfg, dom, n_agents, pos, vel, n_steps, dbg, elapsed_s);
   }
@@ -990,6 +1094,14 @@ int32_t or_run(const or_config *cfg, int64_t n_agents, double *pos, double *vel,
     return oracle_run_rods3(*cfg, dom, n_agents, pos, vel, n_steps, dbg, elapsed_s);
   }
   return OR_EINVAL;
+}
+
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  philox4x32_10(ctr, key, out);
+}
+
+void or_normals(uint64_t seed, uint64_t step, uint64_t id, int32_t n, double *out) {
+  normals(seed, step, id, n, out);
 }
 
 int32_t or_domain_voxels(const or_config *cfg, int64_t *n_voxels_out, double *dx_out) {

@@ -22,8 +22,10 @@ extern "C" {
 #endif
 
 /* Agent kinds. */
-#define OR_KIND_SPHERE 0 /* NewtonDamped{2,3}D + MorsePotential            */
-#define OR_KIND_ROD 1    /* RodMechanics<f64,D> + RodInteraction<Morse>      */
+#define OR_KIND_SPHERE 0   /* NewtonDamped{2,3}D + MorsePotential            */
+#define OR_KIND_ROD 1      /* RodMechanics<f64,D> + RodInteraction<Morse>      */
+#define OR_KIND_BROWNIAN 2 /* Brownian{2,3}D + MorsePotential (mechanics.rs:228-374) */
+#define OR_KIND_LANGEVIN 3 /* Langevin{2,3}D + MorsePotential (mechanics.rs:376-475) */
 
 /* Status codes (mirror chili's SimulationError variants). */
 #define OR_OK 0
@@ -51,6 +53,9 @@ typedef struct or_config {
   /* MorsePotential */
   double radius, stiffness, cutoff, strength;
   double dt;
+  /* stochastic mechanics: Brownian / Langevin k_B T, and the seed of the random stream */
+  double kb_temperature;
+  uint64_t rng_seed;
 } or_config;
 
 /* Optional outputs describing the LAST step that was run. */
@@ -71,6 +76,12 @@ typedef struct or_debug {
  * the final state.  Returns OR_OK or an error code. */
 int32_t or_run(const or_config *cfg, int64_t n_agents, double *pos, double *vel,
                int64_t n_steps, or_debug *dbg, double *elapsed_s);
+
+/* The random stream of the stochastic mechanics (shared definition with the GPU path):
+ * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the standard normals drawn from it
+ * for agent `id` at pack step `step`: n values, two per Philox block (Box-Muller). */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+void or_normals(uint64_t seed, uint64_t step, uint64_t id, int32_t n, double *out);
 
 /* Domain helpers (known-answer tests). */
 int32_t or_domain_voxels(const or_config *cfg, int64_t *n_voxels_out, double *dx_out);

@@ -23,6 +23,10 @@ LIB_PATH = os.path.join(HERE, "_build", "libchili_oracle.so")
 
 KIND_SPHERE = 0
 KIND_ROD = 1
+KIND_BROWNIAN = 2
+KIND_LANGEVIN = 3
+KINDS = {"sphere": KIND_SPHERE, "rod": KIND_ROD, "brownian": KIND_BROWNIAN,
+         "langevin": KIND_LANGEVIN}
 
 OK, ECALC, EBOUNDARY, EINDEX, EDECOMPOSE, EINVAL = 0, 1, 2, 3, 4, 5
 
@@ -50,6 +54,8 @@ class OrConfig(C.Structure):
         ("cutoff", C.c_double),
         ("strength", C.c_double),
         ("dt", C.c_double),
+        ("kb_temperature", C.c_double),
+        ("rng_seed", C.c_uint64),
     ]
 
 
@@ -96,6 +102,11 @@ def lib():
         L.or_nearest_point_from_point_to_line.restype = None
         L.or_morse.argtypes = [C.c_int32, dp, dp] + [C.c_double] * 5 + [dp, dp]
         L.or_morse.restype = C.c_int32
+        u32p = C.POINTER(C.c_uint32)
+        L.or_philox4x32_10.argtypes = [u32p, u32p, u32p]
+        L.or_philox4x32_10.restype = None
+        L.or_normals.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, dp]
+        L.or_normals.restype = None
         for name, n in (("or_euler", 4), ("or_adams_bashforth_2", 5), ("or_adams_bashforth_3", 6)):
             getattr(L, name).argtypes = [C.c_double] * n
             getattr(L, name).restype = C.c_double
@@ -111,7 +122,7 @@ def make_config(model) -> OrConfig:
     """OrConfig from a cellular_raza_gb300.workloads.Model-like object (duck typed)."""
     c = OrConfig()
     c.dim = model.dim
-    c.kind = KIND_ROD if model.kind == "rod" else KIND_SPHERE
+    c.kind = KINDS[model.kind]
     c.n_vertices = model.n_vertices
     c.solver_order = model.solver_order
     c.n_subdomains = model.n_subdomains
@@ -136,6 +147,8 @@ def make_config(model) -> OrConfig:
     c.cutoff = model.cutoff
     c.strength = model.strength
     c.dt = model.dt
+    c.kb_temperature = getattr(model, "kb_temperature", 0.0)
+    c.rng_seed = getattr(model, "rng_seed", 0)
     return c
 
 
@@ -174,6 +187,22 @@ def run(model, pos, vel, n_steps, debug=False):
     if rc != OK:
         raise OracleError(rc, dbg.error_agent, dbg.error_step)
     out["pos"], out["vel"], out["elapsed_s"] = pos, vel, el.value
+    return out
+
+
+def philox4x32_10(ctr, key):
+    """One Philox4x32-10 block (four uint32 words) for counter ctr[4] and key key[2]."""
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().or_philox4x32_10(c, k, o)
+    return [int(x) for x in o]
+
+
+def normals(seed, step, agent_id, n):
+    """The n standard normals of the stochastic mechanics for one agent and step."""
+    out = np.zeros(n, np.float64)
+    lib().or_normals(int(seed), int(step), int(agent_id), int(n), _dp(out))
     return out
 
 

@@ -311,3 +311,78 @@ def test_rod_pair_forces_by_hand(oracle):
     fb = (ea * 0.5) + (ob * 0.5)  # B is second: ext (from call 1) then own (call 2)
     assert np.allclose(r["force"][0], fa, rtol=1e-13, atol=1e-15)
     assert np.allclose(r["force"][1], fb, rtol=1e-13, atol=1e-15)
+
+
+# ---- stochastic mechanics (Brownian / Langevin / RodMechanics diffusion) ------------
+
+def test_philox4x32_10_known_answers(oracle):
+    """Philox4x32-10 against the known-answer vectors published with the algorithm
+    (Random123): zero, all-ones and the pi-digit counter/key."""
+    assert oracle.philox4x32_10([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c,
+                                                          0x9b00dbd8]
+    assert oracle.philox4x32_10([0xffffffff] * 4, [0xffffffff] * 2) == [
+        0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert oracle.philox4x32_10([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344],
+                                [0xa4093822, 0x299f31d0]) == [0xd16cfe09, 0x94fdcceb,
+                                                              0x5001e420, 0x24126ea1]
+
+
+def test_normal_stream_statistics(oracle):
+    z = np.concatenate([oracle.normals(11, s, i, 3) for s in range(100) for i in range(300)])
+    n = z.size
+    assert abs(z.mean()) < 4.0 / math.sqrt(n)
+    assert abs(z.var() - 1.0) < 4.0 * math.sqrt(2.0 / n)
+    assert abs(np.mean(z ** 4) - 3.0) < 0.1  # Gaussian kurtosis
+    # deterministic, and distinct across ids, steps and seeds
+    assert np.array_equal(oracle.normals(11, 5, 7, 6), oracle.normals(11, 5, 7, 6))
+    assert not np.array_equal(oracle.normals(11, 5, 7, 6), oracle.normals(11, 5, 8, 6))
+    assert not np.array_equal(oracle.normals(11, 5, 7, 6), oracle.normals(11, 6, 7, 6))
+    assert not np.array_equal(oracle.normals(11, 5, 7, 6), oracle.normals(12, 5, 7, 6))
+
+
+def free_particles(kind, n=3000, dim=3, **kw):
+    """n non-interacting point particles (strength 0) far from the walls."""
+    side = 1000.0
+    rng = np.random.Generator(np.random.PCG64(3))
+    pos = rng.uniform(400.0, 600.0, size=(n, 1, dim))
+    m = W.Model(kind=kind, dim=dim, n_vertices=1, domain_min=(0.0,) * dim,
+                domain_max=(side,) * dim, interaction_range=50.0, strength=0.0, dt=0.01, **kw)
+    return m, pos, np.zeros_like(pos)
+
+
+def test_brownian_free_diffusion_msd(oracle):
+    """Brownian3D without forces: <|dx|^2> per axis = 2 D t (mechanics.rs:228-374)."""
+    m, pos, vel = free_particles("brownian", diffusion=0.5, kb_temperature=1.0, rng_seed=5)
+    out = oracle.run(m, pos, vel, 100)
+    msd = np.mean((out["pos"] - pos) ** 2)
+    expect = 2.0 * 0.5 * 1.0  # 2 D t, t = 100 * 0.01
+    assert abs(msd / expect - 1.0) < 0.06  # ~2 % statistical error at 9,000 coordinates
+    assert np.all(out["vel"] == 0.0)  # Brownian velocity stays zero
+
+
+def test_langevin_equipartition(oracle):
+    """Langevin3D without forces relaxes to <v^2> = k_B T / M per axis
+    (mechanics.rs:376-475)."""
+    m, pos, vel = free_particles("langevin", mass=2.0, damping=2.0, kb_temperature=0.5,
+                                 rng_seed=9)
+    out = oracle.run(m, pos, vel, 600)  # t = 6 = 12 relaxation times 1 / gamma
+    v2 = np.mean(out["vel"] ** 2)
+    assert abs(v2 / (0.5 / 2.0) - 1.0) < 0.08  # Euler bias ~ gamma dt / 2 = 1 %
+
+
+def test_rod_diffusion_random_term(oracle):
+    """RodMechanics with diffusion: each vertex coordinate moves by 2^-2 D sqrt(dt) z per step
+    (bacterial_rods.rs:215-240) on top of the deterministic forces; with springs at rest,
+    no bending and damping 0, one step's displacement has that variance."""
+    n = 2000
+    rng = np.random.Generator(np.random.PCG64(4))
+    cen = rng.uniform(100.0, 900.0, size=(n, 2))
+    pos = np.stack([cen + [-1.5, 0.0], cen + [1.5, 0.0]], axis=1)
+    m = W.Model(kind="rod", dim=2, n_vertices=2, domain_min=(0.0, 0.0),
+                domain_max=(1000.0, 1000.0), interaction_range=12.0, spring_tension=1.0,
+                rigidity=0.0, spring_length=3.0, damping=0.0, diffusion=0.8, radius=0.1,
+                stiffness=0.5, cutoff=0.2, strength=0.0, dt=0.01, rng_seed=21)
+    out = oracle.run(m, pos, np.zeros_like(pos), 1)
+    d = (out["pos"] - pos).ravel()
+    expect = (0.25 * 0.8) ** 2 * 0.01
+    assert abs(d.var() / expect - 1.0) < 0.08
