@@ -28,6 +28,7 @@ EXPORTED = [
     "crg_debug_forces", "crg_debug_neighbor_stats", "crg_profile", "crg_measure_fma_peaks",
     "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc", "crg_autotune",
     "crg_set_sim_stop", "crg_sim_download", "crg_clear_error", "crg_repack", "crg_step_count",
+    "crg_checkpoint_size", "crg_checkpoint_save", "crg_checkpoint_load",
     "crg_server_create", "crg_server_submit", "crg_server_wait", "crg_server_stats",
     "crg_server_destroy",
 ]
@@ -125,6 +126,9 @@ def load(build_if_missing: bool = True):
     L.crg_cell_list_noalloc.argtypes = [C.POINTER(CrgDomain), C.c_int64, vp, vp, vp, vp, vp]
     L.crg_autotune.argtypes = [vp, C.c_int64, i64p, i64p, dp]
     L.crg_set_sim_stop.argtypes = [vp, C.c_int32, C.c_int64]
+    L.crg_checkpoint_size.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.crg_checkpoint_save.argtypes = [vp, C.c_void_p, C.c_int64]
+    L.crg_checkpoint_load.argtypes = [vp, C.c_void_p, C.c_int64]
     L.crg_sim_download.argtypes = [vp, C.c_int32, i64p, dp, dp, u64p]
     L.crg_clear_error.argtypes = [vp, C.POINTER(C.c_int32)]
     L.crg_repack.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32,

@@ -795,6 +795,137 @@ int32_t crg_snapshot(crg_ctx *c, int32_t op) {
   return CRG_OK;
 }
 
+namespace {
+
+struct CkptHeader {
+  char magic[8];
+  int32_t version, n_sims, nc, dim, kind, order;
+  uint32_t n_agents, n_vox;
+  int64_t steps_done;
+};
+constexpr char kCkptMagic[8] = {'C', 'R', 'G', 'C', 'K', 'P', 'T', '1'};
+
+// The checkpoint's device slices, in blob order: per array, its first n_agents entries of
+// each component (arrays are component-major with stride cap).
+struct CkptSlice {
+  char *dev;
+  size_t elem, comps;
+};
+std::vector<CkptSlice> ckpt_slices(crg_ctx *c) {
+  const size_t nc = (size_t)c->nc;
+  std::vector<CkptSlice> v = {{(char *)c->pos, sizeof(double), nc},
+                              {(char *)c->vel, sizeof(double), nc},
+                              {(char *)c->id, sizeof(uint64_t), 1},
+                              {(char *)c->key, sizeof(uint32_t), 1},
+                              {(char *)c->off, sizeof(float), nc}};
+  if (c->order > 1) {
+    v.push_back({(char *)c->hist, sizeof(double), 2 * nc});
+    v.push_back({(char *)c->hmeta, 1, 1});
+  }
+  return v;
+}
+
+size_t ckpt_bytes(crg_ctx *c, uint32_t n_agents) {
+  size_t b = sizeof(CkptHeader) + sizeof(uint32_t) * (c->n_sims + 1) + sizeof(int64_t) * c->n_sims;
+  for (const CkptSlice &s : ckpt_slices(c)) b += s.elem * s.comps * n_agents;
+  return b + sizeof(uint32_t) * ((size_t)c->n_vox + 1) + sizeof(int64_t);
+}
+
+}  // namespace
+
+int32_t crg_checkpoint_size(crg_ctx *c, int64_t *bytes) {
+  if (!c || !bytes) return CRG_EINVAL;
+  *bytes = (int64_t)ckpt_bytes(c, c->n_agents);
+  return CRG_OK;
+}
+
+int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
+  if (!c || !buf || bytes < (int64_t)ckpt_bytes(c, c->n_agents)) return CRG_EINVAL;
+  if (c->err_code != CRG_OK) return c->err_code;
+  char *p = (char *)buf;
+  CkptHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.n_sims = c->n_sims;
+  h.nc = c->nc;
+  h.dim = c->dim;
+  h.kind = c->kind;
+  h.order = c->order;
+  h.n_agents = c->n_agents;
+  h.n_vox = c->n_vox;
+  h.steps_done = c->steps_done;
+  std::memcpy(p, &h, sizeof(h));
+  p += sizeof(h);
+  std::memcpy(p, c->agent_off_h.data(), sizeof(uint32_t) * (c->n_sims + 1));
+  p += sizeof(uint32_t) * (c->n_sims + 1);
+  for (int s = 0; s < c->n_sims; ++s, p += sizeof(int64_t))
+    std::memcpy(p, &c->sims_h[s].stop_step, sizeof(int64_t));
+  cudaStream_t st = c->stream;
+  const size_t n = c->n_agents;
+  for (const CkptSlice &s : ckpt_slices(c))
+    for (size_t k = 0; k < s.comps; ++k, p += s.elem * n)
+      if (n) CUDA_TRY(cudaMemcpyAsync(p, s.dev + s.elem * k * (size_t)c->cap, s.elem * n,
+                                      cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(p, c->start, sizeof(uint32_t) * ((size_t)c->n_vox + 1),
+                           cudaMemcpyDeviceToHost, st));
+  p += sizeof(uint32_t) * ((size_t)c->n_vox + 1);
+  CUDA_TRY(cudaMemcpyAsync(p, c->step_ctr, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CRG_OK;
+}
+
+int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
+  if (!c || !buf || bytes < (int64_t)sizeof(CkptHeader)) return CRG_EINVAL;
+  const char *p = (const char *)buf;
+  CkptHeader h;
+  std::memcpy(&h, p, sizeof(h));
+  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1 || h.n_sims != c->n_sims ||
+      h.nc != c->nc || h.dim != c->dim || h.kind != c->kind || h.order != c->order ||
+      h.n_vox != c->n_vox || bytes < (int64_t)ckpt_bytes(c, h.n_agents))
+    return CRG_EINVAL;
+  p += sizeof(h);
+  std::vector<uint32_t> aoff(c->n_sims + 1);
+  std::memcpy(aoff.data(), p, sizeof(uint32_t) * (c->n_sims + 1));
+  p += sizeof(uint32_t) * (c->n_sims + 1);
+  if (aoff[0] != 0 || aoff[c->n_sims] != h.n_agents) return CRG_EINVAL;
+  for (int s = 0; s < c->n_sims; ++s)
+    if (aoff[s + 1] < aoff[s] || (int64_t)(aoff[s + 1] - aoff[s]) > c->caps[s]) return CRG_EINVAL;
+  std::vector<int64_t> stops(c->n_sims);
+  std::memcpy(stops.data(), p, sizeof(int64_t) * c->n_sims);
+  p += sizeof(int64_t) * c->n_sims;
+  CUDA_TRY(cudaStreamSynchronize(c->stream));
+  invalidate_graph(c);
+  c->n_agents = h.n_agents;
+  c->agent_off_h = aoff;
+  for (int s = 0; s < c->n_sims; ++s) {
+    c->sims_h[s].agent_off = aoff[s];
+    c->sims_h[s].n_agents = aoff[s + 1] - aoff[s];
+    c->sims_h[s].stop_step = stops[s];
+  }
+  c->steps_done = h.steps_done;
+  c->err_code = CRG_OK;
+  c->err_agent = c->err_step = -1;
+  cudaStream_t st = c->stream;
+  CUDA_TRY(cudaMemcpyAsync(c->d_sims, c->sims_h.data(), sizeof(SimDev) * c->n_sims,
+                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c->d_agent_off, c->agent_off_h.data(),
+                           sizeof(uint32_t) * (c->n_sims + 1), cudaMemcpyHostToDevice, st));
+  const size_t n = c->n_agents;
+  for (const CkptSlice &s : ckpt_slices(c))
+    for (size_t k = 0; k < s.comps; ++k, p += s.elem * n)
+      if (n) CUDA_TRY(cudaMemcpyAsync(s.dev + s.elem * k * (size_t)c->cap, p, s.elem * n,
+                                      cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(c->start, p, sizeof(uint32_t) * ((size_t)c->n_vox + 1),
+                           cudaMemcpyHostToDevice, st));
+  p += sizeof(uint32_t) * ((size_t)c->n_vox + 1);
+  CUDA_TRY(cudaMemcpyAsync(c->step_ctr, p, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, st));
+  CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CRG_OK;
+}
+
 int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block,
                      double *ms_per_step) {
   if (!c || steps <= 0) return CRG_EINVAL;

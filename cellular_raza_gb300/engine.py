@@ -5,6 +5,7 @@ This is a thin owner of a ``crg_ctx*``; every call goes through libcrg.so.
 from __future__ import annotations
 
 import ctypes as C
+import struct
 from typing import Dict, List, Optional, Sequence
 
 import numpy as np
@@ -181,6 +182,24 @@ class Simulation:
 
     def snapshot(self, restore: bool = False):
         N.check(self._L.crg_snapshot(self._h, 1 if restore else 0), "crg_snapshot")
+
+    def checkpoint(self) -> bytes:
+        """The handle's whole simulation state as bytes (crg_checkpoint_save)."""
+        n = C.c_int64()
+        N.check(self._L.crg_checkpoint_size(self._h, C.byref(n)), "crg_checkpoint_size")
+        buf = C.create_string_buffer(n.value)
+        N.check(self._L.crg_checkpoint_save(self._h, buf, n.value), "crg_checkpoint_save", self._h)
+        return buf.raw
+
+    def resume(self, blob: bytes):
+        """Restore a checkpoint taken from a handle with the same domains, models and
+        capacities (crg_checkpoint_load); stepping continues bit for bit."""
+        buf = C.create_string_buffer(blob, len(blob))
+        N.check(self._L.crg_checkpoint_load(self._h, buf, len(blob)), "crg_checkpoint_load")
+        # per-simulation agent ranges: the uint32 offsets after the 48-byte header
+        n = len(self.models)
+        off = struct.unpack_from(f"<{n + 1}I", blob, 48)
+        self.counts = [off[s + 1] - off[s] for s in range(n)]
 
     def stream(self) -> int:
         s = C.c_void_p()

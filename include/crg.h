@@ -198,6 +198,20 @@ int32_t crg_last_error(crg_ctx *ctx, int64_t *agent, int64_t *step);
 #define CRG_SNAPSHOT_RESTORE 1
 int32_t crg_snapshot(crg_ctx *ctx, int32_t op);
 
+/* Host checkpoint of the handle's simulation state: positions, velocities, ids, the cell
+ * list in its storage order, FP32 offsets, solver history, the step counter, and per
+ * simulation its agent range and stop step.  crg_checkpoint_size gives the bytes needed;
+ * crg_checkpoint_save writes them to host memory; crg_checkpoint_load, on a handle created
+ * with the same domains, models and capacities (a fresh one, or the same one later),
+ * restores the state so that stepping continues bit for bit as if it had not stopped.
+ * The blob starts with a header that load checks (magic, version, kind, dimension,
+ * vertices, solver order, simulation and voxel counts).  Replaces nothing in the
+ * reference: chili's save points store cells through serde for analysis, and resuming a
+ * run from them is not implemented there (cellular_raza-core/src/lib.rs:14-22). */
+int32_t crg_checkpoint_size(crg_ctx *ctx, int64_t *bytes);
+int32_t crg_checkpoint_save(crg_ctx *ctx, void *buf, int64_t bytes);
+int32_t crg_checkpoint_load(crg_ctx *ctx, const void *buf, int64_t bytes);
+
 /* The CUDA stream (cudaStream_t) every launch of the handle is issued on, for callers that
  * order their own work or events against it. */
 int32_t crg_get_stream(crg_ctx *ctx, void **stream);
