@@ -354,6 +354,191 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
   sphere_update<D>(P, S, i, key, pa, va, acc);
 }
 
+// Largest system the FP64 default runs with agent groups (k_spheres_groups); above it the
+// lane-per-agent kernel has warps enough to fill the SMs.
+constexpr uint32_t kSphereGroupsMax = 38912;
+constexpr int kGrpL = 8;     // lanes per agent
+constexpr int kGrpA = 4;     // agents per warp
+constexpr int kGrpCap = 64;  // survivor list of an agent between evaluations
+
+// ---------------------------------------------------------------------------------------
+// Agent groups (FP64, small systems).  With a few thousand agents the lane-per-agent kernel
+// leaves most SMs without a warp, and a warp per agent wastes the FP64 lanes of the agent's
+// few survivors.  Here a warp carries four agents with eight lanes each:
+//   * each group numbers its agent's candidates consecutively -- the 3^D neighbourhood
+//     boxes in visiting order, each box's agents in cell-list order, itself skipped -- and
+//     scans eight per round through the FP32 prefilter, appending survivors in order to the
+//     agent's list in shared memory;
+//   * the survivors of the four agents are evaluated in FP64 in full 32-lane batches;
+//   * each group's first lane adds its agent's half-forces in list (= candidate) order and,
+//     at the end, updates the agent.
+// Same terms, same order of additions as k_spheres_step: identical bits.
+// ---------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
+  __shared__ uint32_t sB0[4][kGrpA][27], sPre[4][kGrpA][28];
+  __shared__ float sKd[4][kGrpA][27][D];
+  __shared__ uint8_t sTw[4][kGrpA][27];
+  __shared__ uint32_t sPart[4][kGrpA][kGrpCap];
+  __shared__ uint8_t sWt[4][kGrpA][kGrpCap];
+  __shared__ double sH[4][kGrpA][kGrpCap][D];
+  __shared__ uint8_t sOk[4][kGrpA][kGrpCap];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int g = lane / kGrpL, k = lane % kGrpL;
+  const uint32_t agent0 = (blockIdx.x * 4 + w) * kGrpA;
+  const uint32_t i = agent0 + g;
+  const bool valid = i < P.n_agents;
+  const uint32_t ii = valid ? i : 0u;
+  const int64_t cap = P.cap;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
+  const SimDev &S = P.sims[sim];
+  uint32_t key = P.key[ii];
+  if (key - S.voxel_off >= S.n_vox) {
+    if (valid && k == 0) invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const bool live = valid && *P.step_ctr < S.stop_step;
+  if (valid && !live && k == 0) frozen_copy(P, i, key, D);
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  double pa[D];
+  float oa[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    pa[c] = P.pos[c * cap + ii];
+    oa[c] = P.off[c * cap + ii];
+  }
+  const uint32_t sub_v = subdomain_of(S, v);
+  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+    nb[c] = hi - lo[c] + 1;
+  }
+  const int n_box = live ? nb[0] * nb[1] * nb[2] : 0;  // <= 27
+  // ---- the agent's boxes: first agent, count (-> prefix), weight, centre shift --------
+  for (int q = k; q < n_box; q += kGrpL) {
+    const int j2 = lo[2] + q % nb[2];
+    const int j1 = lo[1] + (q / nb[2]) % nb[1];
+    const int j0 = lo[0] + q / (nb[1] * nb[2]);
+    const uint32_t wv = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                 : (uint32_t)j0 * S.nvox[1] + j1;
+    sTw[w][g][q] = ((wv == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
+                    subdomain_of(S, wv) != sub_v) ? 2 : 1;
+    const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};
+#pragma unroll
+    for (int c = 0; c < D; ++c) sKd[w][g][q][c] = (float)dj[c] * S.dxf[c];
+    const uint32_t b0 = P.start[S.voxel_off + wv], b1 = P.start[S.voxel_off + wv + 1];
+    uint32_t cnt = 0;
+    if (b0 > b1 || b1 > P.n_agents)
+      invariant_failed(P.status, kSiteForceRange, S.voxel_off + wv);
+    else
+      cnt = b1 - b0;
+    sB0[w][g][q] = b0;
+    sPre[w][g][q + 1] = cnt;
+  }
+  __syncwarp();
+  if (k == 0) {
+    sPre[w][g][0] = 0;
+    for (int q = 0; q < n_box; ++q) sPre[w][g][q + 1] += sPre[w][g][q];
+  }
+  __syncwarp();
+  const uint32_t total = sPre[w][g][n_box];
+
+  double acc[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) acc[c] = 0.0;
+  uint32_t j_next = 0;  // the group's next candidate
+  while (__any_sync(0xffffffffu, j_next < total)) {
+    // ---- scan rounds until the candidates are done or a list could overflow ----------
+    int n_list = 0;
+    while (true) {
+      const bool can = j_next < total && n_list + kGrpL <= kGrpCap;
+      if (!__any_sync(0xffffffffu, can)) break;
+      const uint32_t j = j_next + k;
+      bool surv = false;
+      uint32_t b = 0;
+      uint8_t wt = 0;
+      if (can && j < total) {
+        int q = 0, qh = n_box;  // last box whose prefix is <= j
+        while (qh - q > 1) {
+          const int m = (q + qh) >> 1;
+          if (sPre[w][g][m] <= j) q = m; else qh = m;
+        }
+        b = sB0[w][g][q] + (j - sPre[w][g][q]);
+        if (b != i) {
+          float d2 = 0.0f;
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            const float z = (oa[c] - P.off[c * cap + b]) - sKd[w][g][q][c];
+            d2 = fmaf(z, z, d2);
+          }
+          surv = !(d2 > thr2);  // NaN falls through to the exact path
+          wt = sTw[w][g][q];
+        }
+      }
+      const uint32_t gm = (__ballot_sync(0xffffffffu, surv) >> (g * kGrpL)) & 0xffu;
+      if (surv) {
+        const int pos = n_list + __popc(gm & ((1u << k) - 1u));
+        sPart[w][g][pos] = b;
+        sWt[w][g][pos] = wt;
+      }
+      if (can) {
+        n_list += __popc(gm);
+        j_next += kGrpL;
+      }
+    }
+    __syncwarp();
+    // ---- FP64 Morse for the listed survivors of the four agents, full batches --------
+    int st[kGrpA + 1];
+    st[0] = 0;
+#pragma unroll
+    for (int gg = 0; gg < kGrpA; ++gg)
+      st[gg + 1] = st[gg] + __shfl_sync(0xffffffffu, n_list, gg * kGrpL);
+    for (int t0 = 0; t0 < st[kGrpA]; t0 += 32) {
+      const int t = t0 + lane;
+      if (t < st[kGrpA]) {
+        int gg = 0;
+#pragma unroll
+        for (int q = 1; q < kGrpA; ++q) gg += (t >= st[q]);
+        const int m = t - st[gg];
+        const uint32_t a = agent0 + gg, b = sPart[w][gg][m];
+        const uint32_t sim_a = (P.n_sims == 1) ? 0u : sim_of_agent(P, a);
+        double z[D], h[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + a], P.pos[c * cap + b]);
+        const bool ok = morse_half_f64<D>(z, P.sims[sim_a], P.sims[sim_a].radius, h);
+        sOk[w][gg][m] = ok ? 1 : 0;
+#pragma unroll
+        for (int c = 0; c < D; ++c) sH[w][gg][m][c] = h[c];
+      }
+    }
+    __syncwarp();
+    // ---- each agent's half-forces in candidate order --------------------------------
+    if (k == 0) {
+      for (int m = 0; m < n_list; ++m) {
+        if (!sOk[w][g][m]) continue;
+        const bool tw = sWt[w][g][m] == 2;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          acc[c] = dadd(acc[c], sH[w][g][m][c]);
+          if (tw) acc[c] = dadd(acc[c], sH[w][g][m][c]);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  if (live && k == 0) {
+    double va[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) va[c] = P.vel[c * cap + i];
+    sphere_update<D>(P, S, i, key, pa, va, acc);
+  }
+}
+
 // The agents the mixed kernel handed over (rctl[0] of them in fix_list): FP64 force and
 // update, exactly as the FP64 path would compute them.
 template <int D>
@@ -589,6 +774,17 @@ constexpr size_t sphere_pass_smem() {
 
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st) {
   if (!P.n_agents) return;
+  // FP64 default: agent groups while there are too few agents to give every SM several
+  // warps of the lane-per-agent form (variant 2), the lane-per-agent kernel above that
+  const bool small = P.n_agents <= kSphereGroupsMax;
+  if (precision == CRG_PREC_F64 && (P.variant == 2 || (P.variant == 0 && small))) {
+    const unsigned grid = (P.n_agents + 4 * kGrpA - 1) / (4 * kGrpA);
+    if (dim == 3)
+      k_spheres_groups<3><<<grid, 128, 0, st>>>(P);
+    else
+      k_spheres_groups<2><<<grid, 128, 0, st>>>(P);
+    return;
+  }
   if (precision == CRG_PREC_F64 && P.variant != 1) {
     const unsigned grid = (P.n_agents + 31) / 32;
     if (dim == 3)

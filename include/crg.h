@@ -240,11 +240,11 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * of the ids array (same layout as crg_download's ids).  Capture must have been enabled
  * with crg_set_option(ctx, CRG_OPT_DEBUG_FORCES, 1) before that step. */
 #define CRG_OPT_DEBUG_FORCES 5
-/* Force kernel: 0 (default) warp-packed FP64 evaluation, one pass per lane and round
- * (rods: lanes refill from a global rod queue, separate update kernel); 1 one thread per
- * agent; 2 (rods) warp-packed with per-lane slot queues; 3 (rods) warp-packed over fixed
- * groups of 32 rods.  All produce identical results; 1 is kept as the simple reference
- * formulation. */
+/* Force kernel: 0 (default) automatic; 1 one thread per agent (the simple reference
+ * formulation).  Rods: 0 = pass list (walk, pass kernel, bend, update), 2 warp-packed with
+ * per-lane slot queues, 3 warp-packed over fixed groups of 32 rods.  FP64 spheres: 0 = warp
+ * per agent up to 38,912 agents, lane per agent above; 2 warp per agent; 3 lane per agent
+ * (warp-packed survivors).  All produce identical results. */
 #define CRG_OPT_KERNEL_VARIANT 6
 /* Rods, default kernel: capacity of the pass list in passes (one pass = one candidate pair
  * half, about 11 per rod in a dense 2D colony).  A step whose list does not fit computes its

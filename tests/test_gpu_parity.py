@@ -257,11 +257,13 @@ def test_rod_passes_without_survivors(gpu):
 
 @pytest.mark.parametrize("n_sub", [1, 5])
 def test_sphere_kernel_variants_bitwise_identical(gpu, n_sub):
-    """Warp-packed and thread-per-agent FP64 sphere kernels: identical bits."""
+    """FP64 sphere kernels -- warp per agent (the default at this size), thread per agent and
+    lane per agent with warp-packed survivors: identical bits."""
     w = W.spheres_3d(seed=62, n=20_000, n_subdomains=n_sub)
     a = E.run(w, 100)
-    b = E.run(w, 100, options={N.OPT_KERNEL_VARIANT: 1})
-    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    for variant in (1, 2, 3):
+        b = E.run(w, 100, options={N.OPT_KERNEL_VARIANT: variant})
+        assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
 
 
 def test_cell_list_order_over_many_steps(gpu, oracle):
