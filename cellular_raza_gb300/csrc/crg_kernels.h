@@ -62,7 +62,7 @@ struct RepackArgs {
 void launch_repack(const RepackArgs &A, cudaStream_t st);
 
 void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st);
-int sort_kernel_count();
+int sort_kernel_count(uint32_t n_vox);  // kernels one launch_sort issues
 void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st);
 void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
                          cudaStream_t st);

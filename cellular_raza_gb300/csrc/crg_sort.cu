@@ -105,6 +105,32 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(uint32_t *__restric
   }
 }
 
+// Whole scan in one block when the voxels fit one tile (small packs): start[j] = exclusive
+// prefix, count[j] = 0, start[n] = total.
+__global__ void __launch_bounds__(kScanThreads) k_scan_single(uint32_t *__restrict__ count,
+                                                              uint32_t n,
+                                                              uint32_t *__restrict__ start) {
+  const uint32_t base = threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < n) ? count[base + k] : 0u;
+    s += v[k];
+  }
+  uint32_t tot;
+  uint32_t ex = block_excl_scan(s, &tot);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) {
+      start[base + k] = ex;
+      count[base + k] = 0u;
+    }
+    ex += v[k];
+  }
+  if (threadIdx.x == 0) start[n] = tot;
+}
+
 // Slot assignment.  Sort key = class << 32 | previous position.
 __global__ void k_scatter(const SortArgs A) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -301,15 +327,19 @@ static inline unsigned grid_for(uint64_t n, unsigned block) {
 
 void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
   const uint32_t nb = (A.n_vox + kScanTile - 1) / kScanTile;
-  k_scan_reduce<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum);
-  k_scan_blocks<<<1, kScanThreads, 0, st>>>(bsum, nb, A.start, A.n_vox);
-  k_scan_final<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum, A.start);
+  if (nb <= 1) {
+    k_scan_single<<<1, kScanThreads, 0, st>>>(A.count, A.n_vox, A.start);
+  } else {
+    k_scan_reduce<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum);
+    k_scan_blocks<<<1, kScanThreads, 0, st>>>(bsum, nb, A.start, A.n_vox);
+    k_scan_final<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum, A.start);
+  }
   if (A.n_agents) k_scatter<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
   k_segsort<<<grid_for(A.n_vox, 256), 256, 0, st>>>(A);
   if (A.n_agents) k_gather<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
 }
 
-int sort_kernel_count() { return 6; }
+int sort_kernel_count(uint32_t n_vox) { return n_vox <= (uint32_t)kScanTile ? 4 : 6; }
 
 void launch_repack(const RepackArgs &A, cudaStream_t st) {
   if (A.last > A.first) k_repack<<<grid_for(A.last - A.first, 256), 256, 0, st>>>(A);
