@@ -149,6 +149,13 @@ __device__ __forceinline__ void stream_normals(uint64_t seed, uint64_t step, uin
   }
 }
 
+// Out of line, for callers whose register budget the unrolled stream would set (rods).
+template <int N>
+__device__ __noinline__ void stream_normals_ool(uint64_t seed, uint64_t step, uint64_t id,
+                                                double *z) {
+  stream_normals<N>(seed, step, id, z);
+}
+
 // num::ToPrimitive::to_usize for f64: truncation toward zero on the open interval
 // (-1, 2^64); everything else (NaN included) has no value.
 __device__ __forceinline__ bool to_usize(double x, uint64_t &out) {

@@ -278,7 +278,7 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   for (int k = 0; k < NC; ++k) rx[k] = 0.0;
   if (S.stochastic) {
     double z[NC];
-    stream_normals<NC>(S.rng_seed, (uint64_t)*P.step_ctr, P.id[i], z);
+    stream_normals_ool<NC>(S.rng_seed, (uint64_t)*P.step_ctr, P.id[i], z);
     const double sd = __dsqrt_rn(dt);
 #pragma unroll
     for (int k = 0; k < NC; ++k)
@@ -1815,11 +1815,10 @@ __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
   for (int c = 0; c < D; ++c) P.bend[(s * D + c) * cap + i] = f[c];
 }
 
-// Mechanics, solver, boundary and next key of every rod from its interaction force: the
-// sum, in pass order, of the M / 2 that k_rods_passq stored for its passes (rows a pass
-// does not touch are +0, which leaves the sum unchanged since it is never -0), or, after a
-// pass list overflow, the force k_rods_queue stored in frc.  Frozen simulations copy their
-// state.
+// Mechanics, solver, boundary and next key of every rod from its interaction force -- the
+// in-order sum of its passes' M / 2 in mbuf, or after a pass list overflow the force
+// k_rods_queue stored in frc -- and its curvature forces in bend.  Frozen simulations copy
+// their state.
 template <int D, int NV>
 __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   constexpr int NC = NV * D;
@@ -1841,6 +1840,8 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) acc[k] = P.frc[k * cap + i];
   } else {
+    // the sum, in pass order, of the M / 2 that k_rods_passq stored for its passes (rows a
+    // pass does not touch are +0, which leaves the sum unchanged since it is never -0)
 #pragma unroll
     for (int k = 0; k < NC; ++k) acc[k] = 0.0;
     const double *mb = P.mbuf + P.pass_off[i];
