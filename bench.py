@@ -483,7 +483,10 @@ def crg_arm(args):
     fma = E.measure_fma_peaks()
     fp64_peak = fma["fp64_tflops"]
     achieved = kernel_flops / (kernel_ms * 1e-3) / 1e12
-    kernel = "k_rods_passq" if w.model.kind == "rod" else "k_spheres_pass"
+    if w.model.kind == "rod":
+        kernel = "k_rods_passq"
+    else:  # FP64 spheres: agent groups up to 38,912 agents, lane per agent above
+        kernel = "k_spheres_groups" if w.n <= 38912 else "k_spheres_pass"
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak if fp64_peak else None,
                 "traffic": committed_traffic(f"{args.workload}_{kernel}"),
