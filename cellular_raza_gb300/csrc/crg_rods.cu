@@ -1,9 +1,8 @@
 // crg_rods.cu -- one chili step for RodMechanics + RodInteraction<MorsePotential> rods.
 //
-// One thread per rod in cell-list order.  For every candidate rod b in the 3^D
-// neighbourhood of rod a's voxel (keyed by centroid, bacterial_rods.rs:550-554) it builds
-// the two matrices RodInteraction::calculate_force_between produces
-// (bacterial_rods.rs:292-336):
+// The physics: for every candidate rod b in the 3^D neighbourhood of rod a's voxel (keyed
+// by centroid, bacterial_rods.rs:550-554) the step builds the two matrices
+// RodInteraction::calculate_force_between produces (bacterial_rods.rs:292-336):
 //   own_a(b): a's vertices against b's segments, force on a's vertices (a.calc(a, b).0)
 //   ext_a(b): b's vertices against a's segments, force distributed on a's vertices
 //             with weights (1 - t, t)                                   (b.calc(b, a).1)
@@ -16,6 +15,15 @@
 // in FP64 as well and are skipped; the rest are evaluated in FP64 in the reference's
 // operation order.  RodMechanics::calculate_increment (bacterial_rods.rs:157-213), the
 // solver, apply_boundary (:489-534) and the centroid voxel key follow.
+//
+// The kernels (all produce identical bits): the default path lists every rod's passes
+// (one pass = own_a(b) or ext_a(b)) in that order (k_rods_walk), evaluates them one pass
+// per lane with the survivors of the warp's 32 passes in full FP64 batches
+// (k_rods_passq), computes the curvature forces per angle (k_rods_bend) and adds up each
+// rod's passes in order before the mechanics and the solver (k_rods_update); k_rods_queue
+// is the same evaluation with one rod per lane (fallback when the pass list overflows).
+// k_rods_step (one thread per rod), k_rods_packed and k_rods_pass are kept as cross-check
+// variants (CRG_OPT_KERNEL_VARIANT).
 #include "crg_internal.cuh"
 #include "crg_kernels.h"
 
