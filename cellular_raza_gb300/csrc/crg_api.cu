@@ -188,6 +188,7 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.dt = m.dt;
   S.order = m.solver_order;
   S.stop_step = INT64_MAX;
+  S.step_base = 0;
   S.radius_f = (float)m.radius;
   S.stiffness_f = (float)m.stiffness;
   S.cutoff_f = (float)m.cutoff;
@@ -617,6 +618,7 @@ int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *p
     c->agent_off_h[s + 1] = c->agent_off_h[s] + (uint32_t)cnt[s];
     c->sims_h[s].agent_off = c->agent_off_h[s];
     c->sims_h[s].n_agents = (uint32_t)cnt[s];
+    c->sims_h[s].step_base = 0;
   }
   invalidate_graph(c);
   c->err_code = CRG_OK;
@@ -826,7 +828,8 @@ std::vector<CkptSlice> ckpt_slices(crg_ctx *c) {
 }
 
 size_t ckpt_bytes(crg_ctx *c, uint32_t n_agents) {
-  size_t b = sizeof(CkptHeader) + sizeof(uint32_t) * (c->n_sims + 1) + sizeof(int64_t) * c->n_sims;
+  size_t b = sizeof(CkptHeader) + sizeof(uint32_t) * (c->n_sims + 1) +
+             2 * sizeof(int64_t) * c->n_sims;
   for (const CkptSlice &s : ckpt_slices(c)) b += s.elem * s.comps * n_agents;
   return b + sizeof(uint32_t) * ((size_t)c->n_vox + 1) + sizeof(int64_t);
 }
@@ -846,7 +849,7 @@ int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
   CkptHeader h;
   std::memset(&h, 0, sizeof(h));
   std::memcpy(h.magic, kCkptMagic, 8);
-  h.version = 1;
+  h.version = 2;
   h.n_sims = c->n_sims;
   h.nc = c->nc;
   h.dim = c->dim;
@@ -859,8 +862,10 @@ int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
   p += sizeof(h);
   std::memcpy(p, c->agent_off_h.data(), sizeof(uint32_t) * (c->n_sims + 1));
   p += sizeof(uint32_t) * (c->n_sims + 1);
-  for (int s = 0; s < c->n_sims; ++s, p += sizeof(int64_t))
+  for (int s = 0; s < c->n_sims; ++s, p += 2 * sizeof(int64_t)) {
     std::memcpy(p, &c->sims_h[s].stop_step, sizeof(int64_t));
+    std::memcpy(p + sizeof(int64_t), &c->sims_h[s].step_base, sizeof(int64_t));
+  }
   cudaStream_t st = c->stream;
   const size_t n = c->n_agents;
   for (const CkptSlice &s : ckpt_slices(c))
@@ -880,7 +885,7 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
   const char *p = (const char *)buf;
   CkptHeader h;
   std::memcpy(&h, p, sizeof(h));
-  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1 || h.n_sims != c->n_sims ||
+  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 2 || h.n_sims != c->n_sims ||
       h.nc != c->nc || h.dim != c->dim || h.kind != c->kind || h.order != c->order ||
       h.n_vox != c->n_vox || bytes < (int64_t)ckpt_bytes(c, h.n_agents))
     return CRG_EINVAL;
@@ -891,9 +896,11 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
   if (aoff[0] != 0 || aoff[c->n_sims] != h.n_agents) return CRG_EINVAL;
   for (int s = 0; s < c->n_sims; ++s)
     if (aoff[s + 1] < aoff[s] || (int64_t)(aoff[s + 1] - aoff[s]) > c->caps[s]) return CRG_EINVAL;
-  std::vector<int64_t> stops(c->n_sims);
-  std::memcpy(stops.data(), p, sizeof(int64_t) * c->n_sims);
-  p += sizeof(int64_t) * c->n_sims;
+  std::vector<int64_t> stops(c->n_sims), bases(c->n_sims);
+  for (int s = 0; s < c->n_sims; ++s, p += 2 * sizeof(int64_t)) {
+    std::memcpy(&stops[s], p, sizeof(int64_t));
+    std::memcpy(&bases[s], p + sizeof(int64_t), sizeof(int64_t));
+  }
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   invalidate_graph(c);
   c->n_agents = h.n_agents;
@@ -902,6 +909,7 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
     c->sims_h[s].agent_off = aoff[s];
     c->sims_h[s].n_agents = aoff[s + 1] - aoff[s];
     c->sims_h[s].stop_step = stops[s];
+    c->sims_h[s].step_base = bases[s];
   }
   c->steps_done = h.steps_done;
   c->err_code = CRG_OK;
@@ -1080,6 +1088,9 @@ int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_
     c->prefilter = src->prefilter;
     c->graph_chunk = src->graph_chunk;
   }
+  // a kept simulation's own step count continues from the source pack (random stream)
+  for (int k = 0; k < n_keep; ++k)
+    c->sims_h[n_new + k].step_base = src->sims_h[keep[k]].step_base + src->steps_done;
   // agent layout: new simulations first (input order), then the kept ones
   c->agent_off_h.assign(n_total + 1, 0);
   for (int s = 0; s < n_total; ++s) {

@@ -55,6 +55,8 @@ struct SimDev {
   int32_t order;    // 1 Euler, 2 AB2, 3 AB3
   int32_t sim_index;
   int64_t stop_step;  // the simulation is frozen once the pack's step counter reaches this
+  int64_t step_base;  // steps the simulation ran before this pack's counter started (repack):
+                      // its own step = pack step + step_base (indexes the random stream)
 };
 
 // Arguments shared by the per-step kernels of a pack.

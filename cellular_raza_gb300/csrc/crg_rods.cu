@@ -286,7 +286,7 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   for (int k = 0; k < NC; ++k) rx[k] = 0.0;
   if (S.stochastic) {
     double z[NC];
-    stream_normals_ool<NC>(S.rng_seed, (uint64_t)*P.step_ctr, P.id[i], z);
+    stream_normals_ool<NC>(S.rng_seed, (uint64_t)(*P.step_ctr + S.step_base), P.id[i], z);
     const double sd = __dsqrt_rn(dt);
 #pragma unroll
     for (int k = 0; k < NC; ++k)

@@ -131,7 +131,7 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
   for (int c = 0; c < D; ++c) rx[c] = rv[c] = 0.0;
   if (S.stochastic) {
     double z[D];
-    stream_normals<D>(S.rng_seed, (uint64_t)*P.step_ctr, P.id[i], z);
+    stream_normals<D>(S.rng_seed, (uint64_t)(*P.step_ctr + S.step_base), P.id[i], z);
     const double sd = __dsqrt_rn(dt);
     const double amp = (S.mech == 1)
                            ? __dsqrt_rn(dmul(2.0, S.diffusion))

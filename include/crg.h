@@ -200,7 +200,7 @@ int32_t crg_snapshot(crg_ctx *ctx, int32_t op);
 
 /* Host checkpoint of the handle's simulation state: positions, velocities, ids, the cell
  * list in its storage order, FP32 offsets, solver history, the step counter, and per
- * simulation its agent range and stop step.  crg_checkpoint_size gives the bytes needed;
+ * simulation its agent range, stop step and own step count.  crg_checkpoint_size gives the bytes needed;
  * crg_checkpoint_save writes them to host memory; crg_checkpoint_load, on a handle created
  * with the same domains, models and capacities (a fresh one, or the same one later),
  * restores the state so that stepping continues bit for bit as if it had not stopped.

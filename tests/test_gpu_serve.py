@@ -117,3 +117,23 @@ def test_repack_keeps_device_state(gpu):
     assert np.array_equal(outs[0], E.run(extra, 25)["pos"])
     assert np.array_equal(outs[1], E.run(ws[3], 50)["pos"])
     assert np.array_equal(outs[2], E.run(ws[1], 50)["pos"])
+
+
+def test_served_rods_and_stochastic_equal_alone(gpu):
+    """Rod requests (pass-list kernels, their own pack class) and Brownian requests (random
+    stream keyed by agent id and step) served while other requests come and go: each result
+    equals its run alone."""
+    ws = [W.rods(n=600 + 300 * k, side=200.0 + 40 * k, seed=120 + k) for k in range(3)]
+    ws += [W.spheres(500 + 400 * k, 100.0 + 20 * k, 130 + k, 3, kind="brownian",
+                     diffusion=0.3, kb_temperature=1.0, rng_seed=7 + k) for k in range(3)]
+    steps = [40, 25, 60, 30, 45, 20]
+    with SV.Server(hbm_budget_bytes=8 << 30, steps_per_tick=8) as srv:
+        tickets = []
+        for w, n in zip(ws, steps):
+            tickets.append(srv.submit(w, n_steps=n))
+            time.sleep(0.01)  # later requests join running packs
+        out = [srv.wait(t) for t in tickets]
+    for w, n, got in zip(ws, steps, out):
+        alone = E.run(w, n)
+        assert np.array_equal(got["pos"], alone["pos"])
+        assert np.array_equal(got["vel"], alone["vel"])
