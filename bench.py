@@ -167,6 +167,16 @@ def cpu_run(w, n_threads, seconds, max_steps):
                       f"({r['elapsed_s']:.1f} s)"}
 
 
+def workload_config(w, n_subdomains, world):
+    """The `config` object both arms print: the workload, its sizes and the step it runs
+    (each arm's sampling and timing details go in its own keys)."""
+    return {"workload": w.name, "agents": w.n, "vertices_per_agent": w.model.n_vertices,
+            "dim": w.model.dim, "sim_steps_per_bench_step": w.n_steps, "solver": "euler",
+            "precision": "f64", "n_subdomains": n_subdomains,
+            "l2": "GPU arm: flushed between timed steps (256 MiB write)",
+            "parallelism": f"replicas x{world}"}
+
+
 def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -193,8 +203,7 @@ def reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded PCG64)", "impl": "reference",
-        "config": {"workload": w.name, "agents": w.n, "sim_steps_per_bench_step": steps,
-                   "n_subdomains": n_threads},
+        "config": workload_config(w, n_threads, 1),
         "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": n_threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
@@ -525,12 +534,7 @@ def crg_arm(args):
             "steps": args.steps, "warmup": max(args.warmup, 3),
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
-            "config": {"workload": w.name, "agents": w.n,
-                       "vertices_per_agent": w.model.n_vertices, "dim": w.model.dim,
-                       "sim_steps_per_bench_step": w.n_steps, "solver": "euler",
-                       "precision": "f64", "n_subdomains": n_cpu,
-                       "l2": "flushed between timed steps (256 MiB write)",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(w, n_cpu, world),
             "e2e": {"value": e2e_value, "unit": "agent-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline,
