@@ -77,3 +77,14 @@ def test_gpu_brownian_diffusion_constant(gpu):
     out = E.run(w)
     msd = np.mean((out["pos"] - pos) ** 2)
     assert abs(msd / (2.0 * D * 2.0) - 1.0) < 0.01  # 6e5 coordinates: ~0.2 % error
+
+
+def test_brownian_mixed_precision_close_to_f64(gpu):
+    """Brownian agents on the mixed-precision path (FP32 pair forces, Kahan sums) draw the
+    same random stream as the FP64 path, so their trajectories stay close."""
+    w = W.spheres(4000, 150.0, 34, 3, kind="brownian", diffusion=0.5, kb_temperature=2.0,
+                  rng_seed=80)
+    a = E.run(w, 50)
+    b = E.run(W.Workload(w.name, w.model.replace(precision="mixed"), w.pos, w.vel, 50), 50)
+    assert rel_err(b["pos"], a["pos"]) < 1e-5
+    assert np.all(b["vel"] == 0.0)
