@@ -196,6 +196,7 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   double dxmax = 0.0;
   for (int i = 0; i < d.dim; ++i) {
     S.dxf[i] = (float)S.dx[i];
+    S.inv_dxf[i] = (float)(1.0 / S.dx[i]);
     if (std::isfinite(S.dx[i])) dxmax = std::max(dxmax, S.dx[i]);
   }
   // FP32 offsets are trusted while |off| <= off_lim.  Every FP32 quantity entering the

@@ -25,6 +25,7 @@ struct SimDev {
   int32_t nvox[3];
   double min[3], max[3], dx[3];
   float dxf[3];
+  float inv_dxf[3];  // (float)(1 / dx): the FP32 voxel-index estimate (voxel_of)
   uint32_t voxel_off, n_vox;
   uint32_t agent_off, n_agents;
   // Subdomain chunking of get_decomp_res/create_subdomains (cartesian_cuboid_n.rs:19-59,
@@ -174,13 +175,27 @@ __device__ __forceinline__ uint32_t subdomain_of(const SimDev &S, uint32_t v) {
 
 // CartesianSubDomain::get_index_of (cartesian_cuboid_n.rs:469-490) + plain-index lookup.
 // Returns 0 ok, 1 conversion failure, 2 index outside the voxel grid.
+//
+// The index is trunc((p - min) / dx) of the FP64 quotient.  An FP32 estimate q of the
+// quotient (one rounding of p - min to FP32, one of 1/dx, one of the product: relative error
+// below 3 * 2^-24) decides it when q lies farther than twice that error from every integer:
+// the FP64 quotient then truncates to the same integer.  Only quotients that close to a
+// voxel face, or outside [0, 2^23), take the FP64 division.
 template <int D>
 __device__ __forceinline__ int voxel_of(const SimDev &S, const double *p, uint32_t &plain) {
   uint64_t idx[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    double n_vox = ddiv(dsub(p[i], S.min[i]), S.dx[i]);
-    if (!to_usize(n_vox, idx[i])) return 1;
+    const double d = dsub(p[i], S.min[i]);
+    const float q = __fmul_rn(__double2float_rn(d), S.inv_dxf[i]);
+    const float fl = floorf(q), fr = q - fl;  // exact for 0 <= q < 2^23
+    const float eps = __fmaf_rn(q, 4.0e-7f, 1.0e-6f);
+    if (q >= 0.0f && q < 8388608.0f && fr > eps && fr < 1.0f - eps) {
+      idx[i] = (uint64_t)fl;
+    } else {
+      const double n_vox = ddiv(d, S.dx[i]);
+      if (!to_usize(n_vox, idx[i])) return 1;
+    }
   }
 #pragma unroll
   for (int i = 0; i < D; ++i)

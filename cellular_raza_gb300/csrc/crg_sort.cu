@@ -458,6 +458,7 @@ extern "C" int32_t crg_cell_list_noalloc(const crg_domain *d, int64_t n, const d
       nv = (uint64_t)d->n_voxels[a];
       S.dx[a] = (d->max[a] - d->min[a]) / (double)nv;
     }
+    S.inv_dxf[a] = (float)(1.0 / S.dx[a]);
     if (nv > kNaMaxVoxels) return CRG_EINVAL;
     total *= nv;
     if (total > kNaMaxVoxels) return CRG_EINVAL;
