@@ -946,9 +946,9 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   if (c->kind == CRG_KIND_ROD) {
     shapes = {{0, 0}, {3, 0}, {1, 64}, {2, 0}};
   } else if (c->precision == CRG_PREC_F64) {
-    shapes = {{0, 0}, {2, 0}, {3, 0}, {1, 64}, {1, 128}, {1, 256}};
+    shapes = {{0, 0}, {2, 0}, {3, 0}, {3, 64}, {1, 64}, {1, 128}, {1, 256}};
   } else {
-    shapes = {{1, 64}, {1, 128}, {1, 256}};
+    shapes = {{1, 64}, {1, 128}, {1, 256}, {3, 0}};
   }
   int32_t r = crg_snapshot(c, CRG_SNAPSHOT_SAVE);
   if (r != CRG_OK) return r;

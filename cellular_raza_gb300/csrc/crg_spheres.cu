@@ -17,6 +17,8 @@
 // error far below the margin folded into filt_thr2) exceeds the cutoff plus margin has an
 // FP64 distance above the cutoff, hence a zero force, and is skipped; everything else is
 // evaluated in FP64.  Skipping a zero changes no sum.
+#include <type_traits>
+
 #include "crg_internal.cuh"
 #include "crg_kernels.h"
 
@@ -37,6 +39,37 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
   s = t;
 }
 
+
+// Mixed path: FP32 Morse half force of agent a (FP64 position pa) from partner b at FP32
+// displacement zf, |zf|^2 = d2 (not NaN).  Whether the pair interacts is decided exactly as
+// on the FP64 path: a pair whose FP32 distance lies within the prefilter margin of the
+// cutoff or of zero is decided from the FP64 distance, so no pair switches on or off
+// relative to FP64.  Shared by the mixed kernels so they produce the same bits.
+template <int D>
+__device__ __forceinline__ bool mixed_half(const PackArgs &P, const SimDev &S, const double *pa,
+                                           uint32_t b, const float *zf, float d2, float *h) {
+  const float dist = sqrtf(d2);
+  bool in;
+  if (fabsf(dist - S.cutoff_f) <= S.band_f || dist <= S.band_f) {
+    double n2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const double z = dsub(pa[c], P.pos[c * P.cap + b]);
+      n2 = (c == 0) ? dmul(z, z) : dadd(n2, dmul(z, z));
+    }
+    const double d64 = __dsqrt_rn(n2);
+    in = !(d64 > S.cutoff || d64 == 0.0);
+  } else {
+    in = !(dist > S.cutoff_f);
+  }
+  if (!in) return false;
+  const float r = S.radius_f + S.radius_f;
+  const float e = expf(-S.stiffness_f * (dist - r));
+  const float force = -2.0f * S.strength_f * S.stiffness_f * e * (1.0f - e);
+#pragma unroll
+  for (int c = 0; c < D; ++c) h[c] = (zf[c] / dist) * force * 0.5f;
+  return true;
+}
 
 // Mixed path, rare case (a NaN displacement: an agent far outside its voxel, NaN
 // positions): agent i's interaction force computed exactly as the FP64 path computes it
@@ -322,29 +355,12 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
               nan_seen = true;
               continue;
             }
-            const float dist = sqrtf(d2);
-            bool in;
-            if (fabsf(dist - S.cutoff_f) <= S.band_f || dist <= S.band_f) {
-              double n2 = 0.0;
+            float h[D];
+            if (mixed_half<D>(P, S, pa, b, zf, d2, h)) {
 #pragma unroll
               for (int c = 0; c < D; ++c) {
-                const double z = dsub(pa[c], P.pos[c * cap + b]);
-                n2 = (c == 0) ? dmul(z, z) : dadd(n2, dmul(z, z));
-              }
-              const double d64 = __dsqrt_rn(n2);
-              in = !(d64 > S.cutoff || d64 == 0.0);
-            } else {
-              in = !(dist > S.cutoff_f);
-            }
-            if (in) {
-              const float r = S.radius_f + S.radius_f;
-              const float e = expf(-S.stiffness_f * (dist - r));
-              const float force = -2.0f * S.strength_f * S.stiffness_f * e * (1.0f - e);
-#pragma unroll
-              for (int c = 0; c < D; ++c) {
-                const float h = (zf[c] / dist) * force * 0.5f;
-                kahan_add(fs[c], fcmp[c], h);
-                if (twice) kahan_add(fs[c], fcmp[c], h);
+                kahan_add(fs[c], fcmp[c], h[c]);
+                if (twice) kahan_add(fs[c], fcmp[c], h[c]);
               }
             }
           }
@@ -571,17 +587,31 @@ __global__ void __launch_bounds__(128) k_spheres_fix(const PackArgs P) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Warp-packed FP64 variant (default for the FP64 path).  Lane l owns agent a_l.  Each round
-// every lane scans the next G positions of its candidate stream (neighbour voxels ascending,
-// cell-list order inside a voxel, itself skipped) through the FP32 prefilter and records the
-// survivors; the warp evaluates all survivors of all lanes in FP64 with every lane busy
-// (half-forces to shared memory); then each lane adds its half-forces in stream order, twice
-// for a partner whose pair weight is 1.  Same terms, same order as k_spheres_step.
+// Warp-packed variant (lane per agent; the FP64 default for large systems).  Lane l owns
+// agent a_l.  Each round every lane scans the next G positions of its candidate stream
+// (neighbour voxels ascending, cell-list order inside a voxel, itself skipped) through the
+// FP32 prefilter and records its survivors (partner, neighbour box).  The warp's survivors,
+// numbered lane by lane, are evaluated in chunks of kSphereCap with every lane busy
+// (half-forces to shared memory); after each chunk every lane adds the half-forces of its
+// own survivors in that chunk in stream order, twice for a partner whose pair weight is 1.
+// FP64: morse_half_f64 and dadd; mixed: mixed_half and compensated FP32 sums.  Same terms,
+// same order of additions as k_spheres_step: identical bits.  Shared memory per warp is
+// bounded by the chunk rather than by the worst case of 32 x G survivors, so an SM holds
+// enough warps to hide the latency of the scan's loads.
 // ---------------------------------------------------------------------------------------
-template <int D, int G>
+constexpr int kSphereG = 32;  // stream positions a lane scans per round (default shape)
+
+template <int D, int G, int PREC>
 __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
-  extern __shared__ double sH[];                      // [G][D][32] half-forces
-  uint32_t *sB = reinterpret_cast<uint32_t *>(sH + G * D * 32);  // [G][32] partner index
+  static_assert(G <= 64, "survivor weights are a 64-bit mask");
+  constexpr bool MIX = PREC != CRG_PREC_F64;
+  constexpr int kSphereCap = 4 * G;  // survivors evaluated per chunk
+  using Mask = typename std::conditional<(G > 32), uint64_t, uint32_t>::type;
+  __shared__ double sH[MIX ? 1 : D][kSphereCap];  // FP64: half-forces of the current chunk
+  __shared__ float sF[MIX ? D : 1][kSphereCap];   // mixed: half-forces of the current chunk
+  __shared__ uint32_t sOk[kSphereCap / 32];       // mixed: bit set = the pair interacts
+  __shared__ uint32_t sB[G][32];                  // survivor k of lane l: partner index
+  __shared__ uint8_t sK[MIX ? G : 1][32];         // mixed: neighbour box, 2 bits per axis
   const int lane = threadIdx.x;
   const uint32_t warp_base = blockIdx.x * 32;
   const uint32_t i = warp_base + lane;
@@ -615,40 +645,52 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
     const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
     nb[c] = hi - lo[c] + 1;
   }
-  const int n_box = nb[0] * nb[1] * nb[2];
   const bool frozen = valid && (*P.step_ctr >= S.stop_step);
   bool done = !valid || frozen;
-  int o_box = 0;
+  int c0 = lo[0], c1 = lo[1], c2 = lo[2];  // next neighbour box; c0 past the end: none left
   uint32_t b_next = 0, b_end = 0;
   bool twice = false;
+  uint32_t kcode = 0;
   float kd[D];
 #pragma unroll
   for (int c = 0; c < D; ++c) kd[c] = 0.f;
   double acc[D];
+  float fs[D], fcmp[D];  // mixed: compensated FP32 sums
+  bool nan_seen = false;
 #pragma unroll
-  for (int c = 0; c < D; ++c) acc[c] = 0.0;
+  for (int c = 0; c < D; ++c) {
+    acc[c] = 0.0;
+    fs[c] = fcmp[c] = 0.0f;
+  }
 
   while (__any_sync(0xffffffffu, !done)) {
     // ---- scan the next G stream positions ------------------------------------------
     int cnt = 0;
-    uint32_t twice_mask = 0;
+    Mask twice_mask = 0;
     int g = 0;
     while (!done && g < G) {
       if (b_next >= b_end) {
-        if (o_box >= n_box) {
+        if (c0 >= lo[0] + nb[0]) {
           done = true;
           break;
         }
-        const int j2 = lo[2] + o_box % nb[2];
-        const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
-        const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
-        ++o_box;
+        const int j0 = c0, j1 = c1, j2 = c2;  // boxes in the order of k_spheres_step's loops
+        if (++c2 >= lo[2] + nb[2]) {
+          c2 = lo[2];
+          if (++c1 >= lo[1] + nb[1]) {
+            c1 = lo[1];
+            ++c0;
+          }
+        }
         const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                     : (uint32_t)j0 * S.nvox[1] + j1;
         twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
+        // centre(a) - centre(b) = -(j - idx) * dx
         kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
         kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
         if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        kcode = (uint32_t)(j0 - idx[0] + 1) | ((uint32_t)(j1 - idx[1] + 1) << 2);
+        if (D == 3) kcode |= (uint32_t)(j2 - idx[D - 1] + 1) << 4;
         b_next = P.start[S.voxel_off + w];
         b_end = P.start[S.voxel_off + w + 1];
         if (b_next > b_end || b_end > P.n_agents) {
@@ -667,12 +709,13 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
         d2 = fmaf(z, z, d2);
       }
       if (d2 > thr2) continue;  // NaN falls through to the exact path
-      sB[cnt * 32 + lane] = b;
-      if (twice) twice_mask |= 1u << cnt;
+      sB[cnt][lane] = b;
+      if (MIX) sK[cnt][lane] = (uint8_t)kcode;
+      if (twice) twice_mask |= (Mask)1 << cnt;
       ++cnt;
     }
 
-    // ---- evaluate every survivor of the warp in FP64 ---------------------------------
+    // ---- number the warp's survivors lane by lane ----------------------------------
     int incl = cnt;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
@@ -682,51 +725,117 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
     const int excl = incl - cnt;
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     __syncwarp();
-    for (int base = 0; base < total; base += 32) {
-      const int j = base + lane;
-      int l = 0;
+    for (int base = 0; base < total; base += kSphereCap) {
+      const int lim = min(total, base + kSphereCap);
+      // ---- evaluate survivors [base, lim) with every lane busy ---------------------
+      for (int jb = base; jb < lim; jb += 32) {
+        const int j = jb + lane;
+        int l = 0;  // owner: the last lane whose first survivor is <= j
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int cand = l + step;
-        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
-        if (cand < 32 && e <= j) l = cand;
-      }
-      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
-      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
-      if (j < total) {
-        const int k = j - ex_l;
-        const uint32_t b = sB[k * 32 + l];
-        const uint32_t a = warp_base + l;
-        const SimDev &So = P.sims[sim_l];
-        double z[D], h[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + a], P.pos[c * cap + b]);
-        if (!morse_half_f64<D>(z, So, So.radius, h)) {
-#pragma unroll
-          for (int c = 0; c < D; ++c) h[c] = 0.0;  // adding +0 leaves the sum unchanged
+        for (int step = 16; step > 0; step >>= 1) {
+          const int cand = l + step;
+          const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
+          if (cand < 32 && e <= j) l = cand;
         }
+        const int ex_l = __shfl_sync(0xffffffffu, excl, l);
+        const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
+        const uint32_t act = __ballot_sync(0xffffffffu, j < lim);
+        bool ok = false;
+        if (j < lim) {
+          const int k = j - ex_l;
+          const uint32_t b = sB[k][l];
+          const uint32_t a = warp_base + l;
+          const SimDev &So = P.sims[sim_l];
+          if (!MIX) {
+            // morse_half_f64, same operations; the warp reconverges after each library call
+            // so a lane that takes a slow path inside one does not leave the batch split
+            double z[D], h[D];
 #pragma unroll
-        for (int c = 0; c < D; ++c) sH[(k * D + c) * 32 + l] = h[c];
-      }
-    }
-    __syncwarp();
-
-    // ---- add this lane's half-forces in stream order ---------------------------------
-    for (int k = 0; k < cnt; ++k) {
-      const bool tw = (twice_mask >> k) & 1u;
+            for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + a], P.pos[c * cap + b]);
+            double n2 = dmul(z[0], z[0]);
 #pragma unroll
-      for (int c = 0; c < D; ++c) {
-        const double h = sH[(k * D + c) * 32 + lane];
-        acc[c] = dadd(acc[c], h);
-        if (tw) acc[c] = dadd(acc[c], h);
+            for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
+            const double dist = __dsqrt_rn(n2);
+            __syncwarp(act);
+            ok = !(dist > So.cutoff || dist == 0.0);
+            const double e = exp(dmul(-So.stiffness, dsub(dist, dadd(So.radius, So.radius))));
+            __syncwarp(act);
+            const double force =
+                dmul(dmul(dmul(dmul(-2.0, So.strength), So.stiffness), e), dsub(1.0, e));
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+              const double q = ddiv(z[c], dist);
+              __syncwarp(act);
+              h[c] = ok ? dmul(dmul(q, force), 0.5) : 0.0;  // adding +0 leaves the sum unchanged
+            }
+#pragma unroll
+            for (int c = 0; c < D; ++c) sH[c][j - base] = h[c];
+          } else {
+            // the scan's FP32 displacement, recomputed with the same operations
+            const uint32_t code = sK[k][l];
+            float zf[D], hf[D];
+            float d2 = 0.0f;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+              const float kdc = (float)((int)((code >> (2 * c)) & 3u) - 1) * So.dxf[c];
+              zf[c] = (P.off[c * cap + a] - P.off[c * cap + b]) - kdc;
+              d2 = fmaf(zf[c], zf[c], d2);
+            }
+            double pa_l[D];
+#pragma unroll
+            for (int c = 0; c < D; ++c) pa_l[c] = P.pos[c * cap + a];
+            // a NaN displacement reaches the owner as a NaN half-force (its agent goes to
+            // the fix-up); a pair out of range is left out of the sum altogether
+            const bool nan = d2 != d2;
+            ok = nan || mixed_half<D>(P, So, pa_l, b, zf, d2, hf);
+            __syncwarp(act);
+#pragma unroll
+            for (int c = 0; c < D; ++c) sF[c][j - base] = nan ? d2 : hf[c];
+          }
+        }
+        if (MIX) {
+          const uint32_t okm = __ballot_sync(0xffffffffu, ok);
+          if (lane == 0) sOk[(jb - base) >> 5] = okm;
+        }
       }
+      __syncwarp();
+      // ---- each lane adds its own survivors of the chunk in stream order -----------
+      const int f0 = max(excl, base), f1 = min(incl, lim);
+      for (int j = f0; j < f1; ++j) {
+        const bool tw = (twice_mask >> (j - excl)) & 1u;  // j - excl < G
+        if (!MIX) {
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            const double h = sH[c][j - base];
+            acc[c] = dadd(acc[c], h);
+            if (tw) acc[c] = dadd(acc[c], h);
+          }
+        } else {
+          if (!((sOk[(j - base) >> 5] >> ((j - base) & 31)) & 1u)) continue;
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            const float h = sF[c][j - base];
+            nan_seen |= h != h;
+            kahan_add(fs[c], fcmp[c], h);
+            if (tw) kahan_add(fs[c], fcmp[c], h);
+          }
+        }
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
   if (!valid) return;
   if (frozen) {
     frozen_copy(P, i, key, D);
     return;
+  }
+  if (MIX) {
+    if (nan_seen) {  // k_spheres_fix computes this agent's force and update in FP64
+      P.fix_list[atomicAdd(&P.rctl[0], 1u)] = i;
+      return;
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = (double)fs[c] - (double)fcmp[c];
   }
   sphere_update<D>(P, S, i, key, pa, va, acc);
 }
@@ -773,12 +882,6 @@ __global__ void k_sphere_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_i
 
 }  // namespace
 
-constexpr int kSphereG = 32;
-template <int D>
-constexpr size_t sphere_pass_smem() {
-  return sizeof(double) * kSphereG * D * 32 + sizeof(uint32_t) * kSphereG * 32;
-}
-
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st) {
   if (!P.n_agents) return;
   // FP64 default: agent groups while there are too few agents to give every SM several
@@ -793,16 +896,37 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
     return;
   }
   if (precision == CRG_PREC_F64 && P.variant != 1) {
+    // block (autotuned shape): 64 scans 64 stream positions per round into 256-survivor
+    // chunks, any other value 32 into 128.  Default: 64 above 2^21 agents, where its fuller
+    // folds outweigh the lower occupancy (larger shared memory per warp); 32 below.
     const unsigned grid = (P.n_agents + 31) / 32;
-    if (dim == 3)
-      k_spheres_pass<3, kSphereG><<<grid, 32, sphere_pass_smem<3>(), st>>>(P);
-    else
-      k_spheres_pass<2, kSphereG><<<grid, 32, sphere_pass_smem<2>(), st>>>(P);
+    if (block == 64 || (block == 0 && P.n_agents > (1u << 21))) {
+      if (dim == 3)
+        k_spheres_pass<3, 64, CRG_PREC_F64><<<grid, 32, 0, st>>>(P);
+      else
+        k_spheres_pass<2, 64, CRG_PREC_F64><<<grid, 32, 0, st>>>(P);
+    } else {
+      if (dim == 3)
+        k_spheres_pass<3, kSphereG, CRG_PREC_F64><<<grid, 32, 0, st>>>(P);
+      else
+        k_spheres_pass<2, kSphereG, CRG_PREC_F64><<<grid, 32, 0, st>>>(P);
+    }
+    return;
+  }
+  if (precision != CRG_PREC_F64) cudaMemsetAsync(P.rctl, 0, sizeof(uint32_t), st);
+  if (precision != CRG_PREC_F64 && P.variant == 3) {  // warp-packed mixed kernel
+    const unsigned grid = (P.n_agents + 31) / 32;
+    if (dim == 3) {
+      k_spheres_pass<3, kSphereG, CRG_PREC_MIXED><<<grid, 32, 0, st>>>(P);
+      k_spheres_fix<3><<<32, 128, 0, st>>>(P);
+    } else {
+      k_spheres_pass<2, kSphereG, CRG_PREC_MIXED><<<grid, 32, 0, st>>>(P);
+      k_spheres_fix<2><<<32, 128, 0, st>>>(P);
+    }
     return;
   }
   if (block <= 0 || block > 256) block = 128;
   const unsigned grid = (P.n_agents + block - 1) / block;
-  if (precision != CRG_PREC_F64) cudaMemsetAsync(P.rctl, 0, sizeof(uint32_t), st);
   if (dim == 3) {
     if (precision == CRG_PREC_F64) {
       k_spheres_step<3, CRG_PREC_F64><<<grid, block, 0, st>>>(P);

@@ -23,6 +23,7 @@ def main():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--n-subdomains", type=int, default=16)
     p.add_argument("--precision", default=None, choices=[None, "f64", "mixed"])
+    p.add_argument("--variant", type=int, default=0, help="CRG_OPT_KERNEL_VARIANT")
     a = p.parse_args()
     kw = {"n_subdomains": a.n_subdomains}
     if a.n:
@@ -32,6 +33,7 @@ def main():
     w = getattr(W, a.workload)(seed=2024, **kw)
     with E.Simulation.single(w.model, w.n) as sim:
         sim.set_option(N.OPT_GRAPH_CHUNK, 0)
+        sim.set_option(N.OPT_KERNEL_VARIANT, a.variant)
         sim.upload(w.pos, w.vel)
         t = time.perf_counter()
         sim.step(a.steps)

@@ -244,7 +244,9 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * formulation).  Rods: 0 = pass list (walk, pass kernel, bend, update), 2 warp-packed with
  * per-lane slot queues, 3 warp-packed over fixed groups of 32 rods.  FP64 spheres: 0 = warp
  * per agent up to 38,912 agents, lane per agent above; 2 warp per agent; 3 lane per agent
- * (warp-packed survivors).  All produce identical results. */
+ * (warp-packed survivors; CRG_OPT_BLOCK 64 scans 64 candidates per lane and round instead
+ * of 32).  Mixed spheres: 3 lane per agent (warp-packed survivors), else one thread per
+ * agent.  All variants of one precision produce identical results. */
 #define CRG_OPT_KERNEL_VARIANT 6
 /* Rods, default kernel: capacity of the pass list in passes (one pass = one candidate pair
  * half, about 11 per rod in a dense 2D colony).  A step whose list does not fit computes its

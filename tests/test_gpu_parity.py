@@ -163,6 +163,29 @@ def test_mixed_precision_error(gpu):
     assert float(err.max()) <= 1e-5
 
 
+@pytest.mark.parametrize("dim,n_sub", [(3, 1), (3, 5), (2, 4)])
+def test_mixed_kernel_variants_bitwise_identical(gpu, dim, n_sub):
+    """Mixed-precision sphere kernels -- thread per agent and lane per agent with warp-packed
+    survivors -- add the same FP32 terms in the same order: identical bits, single
+    simulations and a batch of several."""
+    w = W.spheres(20_000, 300.0 if dim == 3 else 2000.0, 63, dim, n_subdomains=n_sub,
+                  precision="mixed")
+    a = E.run(w, 60, options={N.OPT_KERNEL_VARIANT: 1})
+    b = E.run(w, 60, options={N.OPT_KERNEL_VARIANT: 3})
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    ws = W.ensemble(seed=64, n_sims=3, n_lo=500, n_hi=5000, precision="mixed", n_steps=30)
+    outs = []
+    for variant in (1, 3):
+        sim = E.Simulation([x.model for x in ws], [x.n for x in ws])
+        sim.set_option(N.OPT_KERNEL_VARIANT, variant)
+        sim.upload(np.concatenate([x.pos for x in ws]), np.concatenate([x.vel for x in ws]),
+                   counts=[x.n for x in ws])
+        sim.step(30)
+        outs.append(sim.download(order="id"))
+        sim.close()
+    assert np.array_equal(outs[0]["pos"], outs[1]["pos"])
+
+
 def test_boundary_error_reported(gpu):
     w = W.spheres(10, 100.0, seed=1, dim=3, dt=1.0, damping=0.0, strength=0.0)
     vel = np.zeros_like(w.vel)
@@ -261,8 +284,9 @@ def test_sphere_kernel_variants_bitwise_identical(gpu, n_sub):
     lane per agent with warp-packed survivors: identical bits."""
     w = W.spheres_3d(seed=62, n=20_000, n_subdomains=n_sub)
     a = E.run(w, 100)
-    for variant in (1, 2, 3):
-        b = E.run(w, 100, options={N.OPT_KERNEL_VARIANT: variant})
+    for opts in ({N.OPT_KERNEL_VARIANT: 1}, {N.OPT_KERNEL_VARIANT: 2},
+                 {N.OPT_KERNEL_VARIANT: 3}, {N.OPT_KERNEL_VARIANT: 3, N.OPT_BLOCK: 64}):
+        b = E.run(w, 100, options=opts)
         assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
 
 
