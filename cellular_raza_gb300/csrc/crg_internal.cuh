@@ -286,24 +286,50 @@ __device__ __forceinline__ void invariant_failed(int32_t *status, int32_t site, 
   }
 }
 
+// x * 0.5 with the IEEE result of the FP64 multiply (round to nearest even), computed on
+// the bit pattern with integer instructions.
+__device__ __forceinline__ double half_exact(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long sign = u & 0x8000000000000000ull, mag = u ^ sign;
+  const unsigned long long e = mag >> 52;
+  // lowest binade and subnormals: the value is mag * 2^-1074, so halving is a shift of mag
+  // rounded to nearest, ties to even (the result is subnormal or zero)
+  unsigned long long q = mag >> 1;
+  q += (mag & q & 1ull);
+  unsigned long long h = sign | q;
+  if (e >= 2) h = u - (1ull << 52);  // normal result: exponent - 1, exact
+  if (e == 0x7ffull) h = u;          // infinities and NaN are their own half
+  return __longlong_as_double((long long)h);
+}
+
+// dist > cutoff || dist == 0.0 for a distance taken as the square root of a sum of squares
+// (+0, positive, +inf or NaN; NaN carries on as in the reference), compared on the bit
+// patterns with integer instructions.  cutoff_bits: the cutoff's bits, INT64_MAX for a NaN
+// cutoff (never exceeded), -1 for a cutoff <= 0 (always exceeded).
+__device__ __forceinline__ bool beyond_cutoff(double dist, long long cutoff_bits) {
+  const long long db = __double_as_longlong(dist);
+  const unsigned long long mag = (unsigned long long)db & 0x7fffffffffffffffull;
+  return mag <= 0x7ff0000000000000ull && (mag == 0ull || db > cutoff_bits);
+}
+
 // calculate_morse_interaction (cellular_raza-building-blocks/src/cell_building_blocks/
 // interaction.rs:151-182) in FP64, returning the own-perspective force already scaled by
 // one half (chili adds f.xa(1/2), update_mechanics.rs:98,194-199).  Each operation is
-// separately rounded in the reference's order.  Returns false for a zero force
-// (dist > cutoff or dist == 0).
+// separately rounded in the reference's order; the pair-independent terms (radius + radius,
+// -stiffness, -2 strength stiffness) come precomputed per simulation with the same
+// roundings, and the halving is done on the bit pattern (half_exact).  Returns false for a
+// zero force (dist > cutoff or dist == 0).
 template <int D>
-__device__ __forceinline__ bool morse_half_f64(const double *z, const SimDev &S,
-                                               double ext_radius, double *h) {
+__device__ __forceinline__ bool morse_half_f64(const double *z, const SimDev &S, double *h) {
   double n2 = dmul(z[0], z[0]);
 #pragma unroll
   for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
-  double dist = __dsqrt_rn(n2);
-  if (dist > S.cutoff || dist == 0.0) return false;
-  double r = dadd(S.radius, ext_radius);
-  double e = exp(dmul(-S.stiffness, dsub(dist, r)));
-  double force = dmul(dmul(dmul(dmul(-2.0, S.strength), S.stiffness), e), dsub(1.0, e));
+  const double dist = __dsqrt_rn(n2);
+  if (beyond_cutoff(dist, S.cutoff_bits)) return false;
+  const double e = exp(dmul(S.mrs_nstiff, dsub(dist, S.mrs_r)));
+  const double force = dmul(dmul(S.mrs_k, e), dsub(1.0, e));
 #pragma unroll
-  for (int c = 0; c < D; ++c) h[c] = dmul(dmul(ddiv(z[c], dist), force), 0.5);
+  for (int c = 0; c < D; ++c) h[c] = half_exact(dmul(ddiv(z[c], dist), force));
   return true;
 }
 

@@ -964,22 +964,6 @@ __device__ __forceinline__ void eval_fold_pass(const PackArgs &P, double *sRes, 
   __syncwarp();
 }
 
-// x * 0.5 with the IEEE result of the FP64 multiply (round to nearest even), computed on
-// the bit pattern with integer instructions.
-__device__ __forceinline__ double half_exact(double x) {
-  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-  const unsigned long long sign = u & 0x8000000000000000ull, mag = u ^ sign;
-  const unsigned long long e = mag >> 52;
-  // lowest binade and subnormals: the value is mag * 2^-1074, so halving is a shift of mag
-  // rounded to nearest, ties to even (the result is subnormal or zero)
-  unsigned long long q = mag >> 1;
-  q += (mag & q & 1ull);
-  unsigned long long h = sign | q;
-  if (e >= 2) h = u - (1ull << 52);  // normal result: exponent - 1, exact
-  if (e == 0x7ffull) h = u;          // infinities and NaN are their own half
-  return __longlong_as_double((long long)h);
-}
-
 // 0.0 + x, exactly: x itself except that -0.0 becomes +0.0.
 __device__ __forceinline__ double plus_zero(double x) {
   return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;

@@ -40,6 +40,33 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 }
 
 
+// morse_half_f64 evaluated by a batch of lanes `act` together (every lane of act calls it):
+// the same operations in the same order, so the same bits, with the warp reconverged after
+// the square root, the exp and each division.  Without that, a lane that takes a slow path
+// inside one of these library calls can leave the batch split into groups for the rest of
+// the evaluation, and every later FP64 instruction runs with a fraction of its lanes.
+// Returns whether the pair interacts (h = +0 when it does not).
+template <int D>
+__device__ __forceinline__ bool morse_half_f64_batch(const double *z, const SimDev &S, double *h,
+                                                     unsigned act) {
+  double n2 = dmul(z[0], z[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
+  const double dist = __dsqrt_rn(n2);
+  __syncwarp(act);
+  const bool ok = !beyond_cutoff(dist, S.cutoff_bits);
+  const double e = exp(dmul(S.mrs_nstiff, dsub(dist, S.mrs_r)));
+  __syncwarp(act);
+  const double force = dmul(dmul(S.mrs_k, e), dsub(1.0, e));
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const double q = ddiv(z[c], dist);
+    __syncwarp(act);
+    h[c] = ok ? half_exact(dmul(q, force)) : 0.0;
+  }
+  return ok;
+}
+
 // Mixed path: FP32 Morse half force of agent a (FP64 position pa) from partner b at FP32
 // displacement zf, |zf|^2 = d2 (not NaN).  Whether the pair interacts is decided exactly as
 // on the FP64 path: a pair whose FP32 distance lies within the prefilter margin of the
@@ -105,7 +132,7 @@ __device__ Vec3 agent_force_f64(const PackArgs &P, const SimDev &S, uint32_t i, 
           double z[D], h[D];
 #pragma unroll
           for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
-          if (morse_half_f64<D>(z, S, S.radius, h)) {
+          if (morse_half_f64<D>(z, S, h)) {
 #pragma unroll
             for (int c = 0; c < D; ++c) {
               r.x[c] = dadd(r.x[c], h[c]);
@@ -336,7 +363,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
             double z[D], h[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
-            if (morse_half_f64<D>(z, S, S.radius, h)) {
+            if (morse_half_f64<D>(z, S, h)) {
 #pragma unroll
               for (int c = 0; c < D; ++c) {
                 acc[c] = dadd(acc[c], h[c]);
@@ -533,7 +560,9 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
         double z[D], h[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + a], P.pos[c * cap + b]);
-        const bool ok = morse_half_f64<D>(z, P.sims[sim_a], P.sims[sim_a].radius, h);
+        // no reconvergence points here: this kernel runs with few warps per SM, where
+        // overlapping the three divisions matters more than full lanes
+        const bool ok = morse_half_f64<D>(z, P.sims[sim_a], h);
         sOk[w][gg][m] = ok ? 1 : 0;
 #pragma unroll
         for (int c = 0; c < D; ++c) sH[w][gg][m][c] = h[c];
@@ -747,27 +776,10 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
           const uint32_t a = warp_base + l;
           const SimDev &So = P.sims[sim_l];
           if (!MIX) {
-            // morse_half_f64, same operations; the warp reconverges after each library call
-            // so a lane that takes a slow path inside one does not leave the batch split
             double z[D], h[D];
 #pragma unroll
             for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + a], P.pos[c * cap + b]);
-            double n2 = dmul(z[0], z[0]);
-#pragma unroll
-            for (int c = 1; c < D; ++c) n2 = dadd(n2, dmul(z[c], z[c]));
-            const double dist = __dsqrt_rn(n2);
-            __syncwarp(act);
-            ok = !(dist > So.cutoff || dist == 0.0);
-            const double e = exp(dmul(-So.stiffness, dsub(dist, dadd(So.radius, So.radius))));
-            __syncwarp(act);
-            const double force =
-                dmul(dmul(dmul(dmul(-2.0, So.strength), So.stiffness), e), dsub(1.0, e));
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-              const double q = ddiv(z[c], dist);
-              __syncwarp(act);
-              h[c] = ok ? dmul(dmul(q, force), 0.5) : 0.0;  // adding +0 leaves the sum unchanged
-            }
+            morse_half_f64_batch<D>(z, So, h, act);  // +0 when out of range: adds nothing
 #pragma unroll
             for (int c = 0; c < D; ++c) sH[c][j - base] = h[c];
           } else {
@@ -872,7 +884,7 @@ __global__ void k_sphere_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_i
           h += x ^ (x >> 31);
           double z[D], hf[D];
           for (int c = 0; c < D; ++c) z[c] = dsub(P.pos[c * cap + i], P.pos[c * cap + b]);
-          if (morse_half_f64<D>(z, S, S.radius, hf)) ++ni;
+          if (morse_half_f64<D>(z, S, hf)) ++ni;
         }
       }
   n_cand[i] = nc;
