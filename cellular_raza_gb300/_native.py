@@ -20,6 +20,9 @@ WEIGHTS_CHILI, WEIGHTS_PHYSICAL = 0, 1
 OPT_PREFILTER, OPT_GRAPH_CHUNK, OPT_BLOCK, OPT_PROFILE, OPT_DEBUG_FORCES = 1, 2, 3, 4, 5
 OPT_KERNEL_VARIANT = 6
 OPT_PASS_LIST = 7
+# CellIdentifier::Division(voxel, counter) = ID_DIVISION | voxel << 32 | counter
+ID_DIVISION = 1 << 63
+NO_PARENT = (1 << 64) - 1
 
 # Every symbol include/crg.h declares (checked by tests/test_abi.py).
 EXPORTED = [
@@ -29,6 +32,7 @@ EXPORTED = [
     "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc", "crg_autotune",
     "crg_set_sim_stop", "crg_sim_download", "crg_clear_error", "crg_repack", "crg_step_count",
     "crg_checkpoint_size", "crg_checkpoint_save", "crg_checkpoint_load",
+    "crg_set_spring_lengths", "crg_download_cycle",
     "crg_server_create", "crg_server_submit", "crg_server_wait", "crg_server_stats",
     "crg_server_destroy",
 ]
@@ -68,6 +72,11 @@ class CrgModel(C.Structure):
         ("dt", C.c_double),
         ("kb_temperature", C.c_double),
         ("rng_seed", C.c_uint64),
+        ("cycle", C.c_int32),
+        ("growth_rate", C.c_double),
+        ("division_length", C.c_double),
+        ("sense_range", C.c_double),
+        ("sense_saturation", C.c_double),
     ]
 
 
@@ -135,6 +144,8 @@ def load(build_if_missing: bool = True):
                              C.POINTER(CrgDomain), C.POINTER(CrgModel), i64p, i64p, dp, dp,
                              C.POINTER(vp)]
     L.crg_step_count.argtypes = [vp, i64p]
+    L.crg_set_spring_lengths.argtypes = [vp, dp]
+    L.crg_download_cycle.argtypes = [vp, dp, dp, u64p]
     L.crg_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
     L.crg_server_submit.argtypes = [vp, C.POINTER(CrgDomain), C.POINTER(CrgModel), C.c_int64,
                                     dp, dp, C.c_int64, u64p]

@@ -53,6 +53,14 @@ struct crg_ctx {
   uint32_t *rctl = nullptr;
   uint32_t *fix_list = nullptr;  // mixed spheres: agents for the FP64 fix-up kernel
   double *bend = nullptr;        // rods: curvature forces between the bend and update kernels
+  // cell cycle (rods, single simulation): per-agent state (current / next), neighbour
+  // counts, division flags and their scan, voxel id counters, pre-sort ranks
+  int cycle = 0;
+  double *slen = nullptr, *nslen = nullptr, *grate = nullptr, *ngrate = nullptr;
+  uint64_t *parent = nullptr, *nparent = nullptr, *vctr = nullptr;
+  uint32_t *nsense = nullptr, *dflag = nullptr, *dpre = nullptr, *dbsum = nullptr;
+  uint32_t *srank = nullptr;
+  uint32_t *h_ndiv = nullptr;  // pinned
   double *frc = nullptr;
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
@@ -176,6 +184,11 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.rng_seed = m.rng_seed;
   S.stochastic = (m.kind == CRG_KIND_BROWNIAN || m.kind == CRG_KIND_LANGEVIN ||
                   (m.kind == CRG_KIND_ROD && m.diffusion != 0.0)) ? 1 : 0;
+  S.cycle = m.cycle ? 1 : 0;
+  S.cyc_growth = m.growth_rate;
+  S.cyc_div_len = m.division_length;
+  S.cyc_sense = m.sense_range;
+  S.cyc_sat = m.sense_saturation;
   S.mrs_r = m.radius + m.radius;
   S.mrs_k = (-2.0 * m.strength) * m.stiffness;
   S.mrs_nstiff = -m.stiffness;
@@ -203,7 +216,10 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   // prefilter distance is then within a few ulps of off_lim (offset roundings, the corner
   // shift, the differences), so its absolute error is bounded by 16 * off_lim * 2^-24 per
   // axis.  The margin below is more than 100 times that bound.
-  double ext = (m.kind == CRG_KIND_ROD) ? 4.0 * (m.n_vertices - 1) * std::fabs(m.spring_length) : 0.0;
+  // a growing rod reaches the division length before it divides
+  const double longest = m.cycle ? std::max(std::fabs(m.spring_length), std::fabs(m.division_length))
+                                 : std::fabs(m.spring_length);
+  double ext = (m.kind == CRG_KIND_ROD) ? 4.0 * (m.n_vertices - 1) * longest : 0.0;
   double off_lim = 4.0 * dxmax + ext + 1.0;
   double err = 16.0 * off_lim * std::ldexp(1.0, -24) * std::sqrt((double)d.dim);
   double margin = 128.0 * err + 1e-4 * std::fabs(m.cutoff) + 1e-6;
@@ -227,6 +243,10 @@ int32_t check_model(const crg_model &m) {
   if (m.kind == CRG_KIND_SPHERE && m.diffusion != 0.0) return CRG_EINVAL;
   if (m.kind == CRG_KIND_BROWNIAN && !(m.kb_temperature != 0.0)) return CRG_EINVAL;
   if (!(m.dt > 0.0)) return CRG_EINVAL;
+  if (m.cycle) {
+    if (m.kind != CRG_KIND_ROD) return CRG_ENOTSUP;
+    if (!(m.sense_saturation != 0.0)) return CRG_EINVAL;  // the growth law divides by it
+  }
   return CRG_OK;
 }
 
@@ -276,11 +296,13 @@ void free_all(crg_ctx *c) {
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
                   c->step_ctr, c->dbg_force, c->frc, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
-                  c->staging, c->snap};
+                  c->staging, c->snap, c->slen, c->nslen, c->grate, c->ngrate, c->parent,
+                  c->nparent, c->vctr, c->nsense, c->dflag, c->dpre, c->dbsum, c->srank};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   free_pass_list(c);
   if (c->h_status) cudaFreeHost(c->h_status);
+  if (c->h_ndiv) cudaFreeHost(c->h_ndiv);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -327,7 +349,24 @@ int32_t allocate(crg_ctx *c) {
     A(nhmeta, cap);
   }
   if (c->n_sims > 1) A(d_sim_of_voxel, c->n_vox);
+  if (c->cycle) {
+    A(slen, cap);
+    A(nslen, cap);
+    A(grate, cap);
+    A(ngrate, cap);
+    A(parent, cap);
+    A(nparent, cap);
+    A(nsense, cap);
+    A(dflag, cap + 1);
+    A(dpre, cap + 1);
+    A(dbsum, cap / 4096 + 2);
+    A(srank, cap);
+    A(vctr, c->n_vox);
+  }
 #undef A
+  if (c->cycle) {
+    CUDA_TRY(cudaMallocHost((void **)&c->h_ndiv, 2 * sizeof(uint32_t)));
+  }
   CUDA_TRY(cudaMallocHost((void **)&c->h_status, 8 * sizeof(int32_t)));
   CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), c->stream));
@@ -356,6 +395,11 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
   c->nc = c->nv * c->dim;
   c->precision = m0.precision;
   c->order = m0.solver_order;
+  c->cycle = m0.cycle ? 1 : 0;
+  if (c->cycle && n_sims > 1) {  // the cell cycle runs on single-simulation handles
+    delete c;
+    return CRG_ENOTSUP;
+  }
   c->n_sims = n_sims;
   c->sims_h.resize(n_sims);
   c->doms.assign(domains, domains + n_sims);
@@ -440,6 +484,19 @@ PackArgs pack_args(crg_ctx *c) {
   P.pass_cap = c->pass_cap;
   P.prefilter = c->prefilter;
   P.variant = c->variant;
+  if (c->cycle) {
+    P.slen = c->slen;
+    P.grate = c->grate;
+    P.parent = c->parent;
+    P.nslen = c->nslen;
+    P.ngrate = c->ngrate;
+    P.nparent = c->nparent;
+    P.nsense = c->nsense;
+    P.dflag = c->dflag;
+    P.dpre = c->dpre;
+    P.vctr = c->vctr;
+    P.srank = c->srank;
+  }
   return P;
 }
 
@@ -473,6 +530,14 @@ SortArgs sort_args(crg_ctx *c, int initial) {
   A.tmp = c->tmp;
   A.status = c->status;
   A.step_ctr = initial ? nullptr : c->step_ctr;
+  if (c->cycle) {
+    A.slen = c->slen;
+    A.grate = c->grate;
+    A.parent = c->parent;
+    A.nslen = c->nslen;
+    A.ngrate = c->ngrate;
+    A.nparent = c->nparent;
+  }
   return A;
 }
 
@@ -555,6 +620,65 @@ void invalidate_graph(crg_ctx *c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   c->gexec = nullptr;
   c->gexec_steps = 0;
+}
+
+// Cell-cycle handles run one step at a time: divisions change the agent count that every
+// launch is sized by.  Per step: neighbour counts (k_rods_sense), forces and the update
+// (growth, division flags), the scan of the flags, a read of the division count, the
+// divisions (k_rods_divide) and the sort of the grown list.  A step whose divisions would
+// exceed the handle's capacity stops before dividing with CRG_ENOMEM.
+int32_t step_cycle(crg_ctx *c, int64_t n_steps) {
+  cudaStream_t st = c->stream;
+  int64_t done = 0;
+  for (; done < n_steps; ++done) {
+    const uint32_t n = c->n_agents;
+    PackArgs P = pack_args(c);
+    crg::launch_rods_sense(c->dim, c->nv, P, st);
+    launch_force(c);
+    crg::launch_scan(c->dflag, n, c->dpre, c->dbsum, st);
+    if (cudaMemcpyAsync(c->h_ndiv, c->dpre + n, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                        st) != cudaSuccess) {
+      c->err_code = CRG_ECUDA;
+      c->err_step = c->steps_done + done;
+      break;
+    }
+    if (read_status(c) != CRG_OK) break;
+    const uint32_t n_div = c->h_ndiv[0];
+    if ((int64_t)n + (int64_t)n_div > c->cap) {
+      c->err_code = CRG_ENOMEM;
+      c->err_agent = -1;
+      c->err_step = c->steps_done + done + 1;
+      break;
+    }
+    if (n_div) crg::launch_rods_divide(c->dim, c->nv, P, n_div, st);
+    SortArgs A = sort_args(c, 0);
+    A.n_agents = n + n_div;
+    A.srank = n_div ? c->srank : nullptr;
+    crg::launch_sort(A, c->bsum, st);
+    if (n_div) {
+      c->n_agents = n + n_div;
+      c->agent_off_h[1] = c->n_agents;
+      c->sims_h[0].n_agents = c->n_agents;
+      if (cudaMemcpyAsync(c->d_sims, c->sims_h.data(), sizeof(SimDev), cudaMemcpyHostToDevice,
+                          st) != cudaSuccess ||
+          cudaMemcpyAsync(c->d_agent_off, c->agent_off_h.data(), 2 * sizeof(uint32_t),
+                          cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        c->err_code = CRG_ECUDA;
+        c->err_step = c->steps_done + done + 1;
+        ++done;
+        break;
+      }
+    }
+    if (cudaGetLastError() != cudaSuccess) {
+      c->err_code = CRG_ECUDA;
+      c->err_step = c->steps_done + done + 1;
+      ++done;
+      break;
+    }
+  }
+  if (c->err_code == CRG_OK) read_status(c);
+  c->steps_done += done;
+  return c->err_code;
 }
 
 }  // namespace
@@ -654,9 +778,18 @@ int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *p
     CUDA_TRY(cudaMemsetAsync(c->nhmeta, 0, (size_t)c->cap, st));
     CUDA_TRY(cudaMemsetAsync(c->nhist, 0, sizeof(double) * (size_t)c->cap * c->nc * 2, st));
   }
+  if (c->cycle && n > 0) {  // every rod starts at the model's spring length, no parent
+    std::vector<double> sl((size_t)n, c->mods[0].spring_length);
+    std::vector<double> gr((size_t)n, c->mods[0].growth_rate);
+    CUDA_TRY(cudaMemcpyAsync(c->nslen, sl.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c->ngrate, gr.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(c->nparent, 0xff, sizeof(uint64_t) * n, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+  }
   SortArgs A = sort_args(c, 1);
   crg::launch_init_keys(A, c->nv, st);
   crg::launch_sort(A, c->bsum, st);
+  if (c->cycle) crg::launch_cycle_init(pack_args(c), st);
   CUDA_TRY(cudaGetLastError());
   int32_t r = read_status(c);
   if (r != CRG_OK) {
@@ -673,6 +806,7 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
     c->steps_done += n_steps;
     return CRG_OK;
   }
+  if (c->cycle) return step_cycle(c, n_steps);
   cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   if (c->profile) {
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
@@ -755,6 +889,7 @@ int32_t crg_download(crg_ctx *c, double *pos, double *vel, uint64_t *ids, uint32
 
 int32_t crg_snapshot(crg_ctx *c, int32_t op) {
   if (!c || (op != CRG_SNAPSHOT_SAVE && op != CRG_SNAPSHOT_RESTORE)) return CRG_EINVAL;
+  if (c->cycle) return CRG_ENOTSUP;  // the cycle state is not part of snapshots
   const size_t cap = (size_t)c->cap, nc = (size_t)c->nc;
   struct Part {
     void *p;
@@ -839,11 +974,13 @@ size_t ckpt_bytes(crg_ctx *c, uint32_t n_agents) {
 
 int32_t crg_checkpoint_size(crg_ctx *c, int64_t *bytes) {
   if (!c || !bytes) return CRG_EINVAL;
+  if (c->cycle) return CRG_ENOTSUP;  // the cycle state is not part of checkpoints
   *bytes = (int64_t)ckpt_bytes(c, c->n_agents);
   return CRG_OK;
 }
 
 int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
+  if (c && c->cycle) return CRG_ENOTSUP;
   if (!c || !buf || bytes < (int64_t)ckpt_bytes(c, c->n_agents)) return CRG_EINVAL;
   if (c->err_code != CRG_OK) return c->err_code;
   char *p = (char *)buf;
@@ -882,6 +1019,7 @@ int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
 }
 
 int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
+  if (c && c->cycle) return CRG_ENOTSUP;
   if (!c || !buf || bytes < (int64_t)sizeof(CkptHeader)) return CRG_EINVAL;
   const char *p = (const char *)buf;
   CkptHeader h;
@@ -938,6 +1076,7 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
 int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block,
                      double *ms_per_step) {
   if (!c || steps <= 0) return CRG_EINVAL;
+  if (c->cycle) return CRG_ENOTSUP;  // trials restore snapshots, which hold no cycle state
   if (c->err_code != CRG_OK) return c->err_code;
   struct Shape {
     int variant, block;
@@ -1054,6 +1193,9 @@ int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_
   if (!out || n_keep < 0 || n_new < 0 || n_keep + n_new < 1) return CRG_EINVAL;
   if (n_keep > 0 && (!src || !keep)) return CRG_EINVAL;
   if (n_new > 0 && (!new_domains || !new_models || !new_caps || !new_counts)) return CRG_EINVAL;
+  if (n_keep > 0 && src->cycle) return CRG_ENOTSUP;  // packs hold no cell cycle
+  for (int32_t k = 0; k < n_new; ++k)
+    if (new_models[k].cycle) return CRG_ENOTSUP;
   *out = nullptr;
   const int n_total = n_keep + n_new;
   std::vector<crg_domain> doms;
@@ -1196,6 +1338,39 @@ int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_
   r = read_status(c);
   if (r != CRG_OK) return fail(r);
   *out = c;
+  return CRG_OK;
+}
+
+int32_t crg_set_spring_lengths(crg_ctx *c, const double *spring_length) {
+  if (!c || !spring_length) return CRG_EINVAL;
+  if (!c->cycle) return CRG_ENOTSUP;
+  // the slot table of the upload's sort (tmp) is overwritten by the first step
+  if (c->steps_done != 0 || c->err_code != CRG_OK) return CRG_EINVAL;
+  const uint32_t n = c->n_agents;
+  if (n == 0) return CRG_OK;
+  cudaStream_t st = c->stream;
+  CUDA_TRY(cudaMemcpyAsync(c->staging, spring_length, sizeof(double) * n,
+                           cudaMemcpyHostToDevice, st));
+  crg::launch_cycle_permute(c->slen, c->staging, c->tmp, n, st);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return CRG_OK;
+}
+
+int32_t crg_download_cycle(crg_ctx *c, double *spring_length, double *growth_rate,
+                           uint64_t *parent) {
+  if (!c) return CRG_EINVAL;
+  if (!c->cycle) return CRG_ENOTSUP;
+  const uint32_t n = c->n_agents;
+  if (n == 0) return CRG_OK;
+  cudaStream_t st = c->stream;
+  if (spring_length)
+    CUDA_TRY(cudaMemcpyAsync(spring_length, c->slen, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  if (growth_rate)
+    CUDA_TRY(cudaMemcpyAsync(growth_rate, c->grate, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  if (parent)
+    CUDA_TRY(cudaMemcpyAsync(parent, c->parent, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
   return CRG_OK;
 }
 

@@ -58,6 +58,9 @@ struct SimDev {
   int64_t stop_step;  // the simulation is frozen once the pack's step counter reaches this
   int64_t step_base;  // steps the simulation ran before this pack's counter started (repack):
                       // its own step = pack step + step_base (indexes the random stream)
+  // cell cycle (rods): base growth rate, division length, sensing range and saturation
+  int32_t cycle;
+  double cyc_growth, cyc_div_len, cyc_sense, cyc_sat;
 };
 
 // Arguments shared by the per-step kernels of a pack.
@@ -104,6 +107,19 @@ struct PackArgs {
                        // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
   int32_t variant;    // force kernel: 0 warp-packed (default), 1 thread per agent
+  // cell cycle (rods; all null when off)
+  const double *slen;       // [cap] spring length of each rod (current order)
+  const double *grate;      // [cap] growth rate of each rod (current order)
+  const uint64_t *parent;   // [cap] identifier the rod divided from (CRG_NO_PARENT if none)
+  double *nslen, *ngrate;   // [cap] next spring length and growth rate (pre-step order;
+                            // daughters of this step at n_agents + their rank)
+  uint64_t *nparent;        // [cap]
+  uint32_t *nsense;         // [cap] neighbour count of this step (k_rods_sense)
+  uint32_t *dflag;          // [cap + 1] 1 where the rod divides this step (update kernel);
+                            // the exclusive scan of it (dpre) numbers the daughters
+  const uint32_t *dpre;     // [cap + 1]
+  uint64_t *vctr;           // [n_vox] Voxel::id_counter
+  uint32_t *srank;          // [cap] position in chili's pre-sort order, daughters included
 };
 
 // ---- IEEE FP64 helpers that are never contracted into fused multiply-adds ----------
@@ -259,6 +275,12 @@ __device__ __forceinline__ void frozen_copy(const PackArgs &P, uint32_t i, uint3
   if (P.hist) {
     for (int c = 0; c < 2 * nc; ++c) P.nhist[c * cap + i] = P.hist[c * cap + i];
     P.nhmeta[i] = P.hmeta[i];
+  }
+  if (P.dflag) {  // cell cycle: a frozen rod keeps its state and does not divide
+    P.nslen[i] = P.slen[i];
+    P.ngrate[i] = P.grate[i];
+    P.nparent[i] = P.parent[i];
+    P.dflag[i] = 0u;
   }
   P.nkey[i] = key;
   P.nid[i] = P.id[i];

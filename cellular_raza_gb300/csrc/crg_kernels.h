@@ -38,6 +38,14 @@ struct SortArgs {
   uint64_t *tmp;    // [cap]
   int32_t *status;
   int64_t *step_ctr;
+  // cell cycle (null when off): per-agent state moved with the agents, and the rank of
+  // each agent in chili's pre-sort order when divisions inserted daughters (else the
+  // agent's index is its rank)
+  double *slen, *grate;
+  uint64_t *parent;
+  const double *nslen, *ngrate;
+  const uint64_t *nparent;
+  const uint32_t *srank;
 };
 
 // Copy of kept simulations from one pack into the "next" arrays of another (crg_repack).
@@ -62,6 +70,10 @@ struct RepackArgs {
 void launch_repack(const RepackArgs &A, cudaStream_t st);
 
 void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st);
+// Exclusive prefix sum of count[0..n) into start[0..n] (start[n] = total); zeroes count.
+// bsum: n / 4096 + 2 entries.
+void launch_scan(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
+                 cudaStream_t st);
 int sort_kernel_count(uint32_t n_vox);  // kernels one launch_sort issues
 void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st);
 void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
@@ -75,6 +87,16 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
                       cudaStream_t st, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr);
 int prepare_rods(int dim, int nv);  // 0 on success
+// Cell cycle of rods: neighbour counts of this step (before the update kernel), and after
+// the update and the scan of its division flags, the divisions (n_div > 0) plus the voxel
+// counters.
+void launch_rods_sense(int dim, int nv, const PackArgs &P, cudaStream_t st);
+void launch_rods_divide(int dim, int nv, const PackArgs &P, uint32_t n_div, cudaStream_t st);
+// Voxel counters from the first cell list; per-agent values from upload order to the cell
+// list through the upload sort's slot table (tmp).
+void launch_cycle_init(const PackArgs &P, cudaStream_t st);
+void launch_cycle_permute(double *dst, const double *src, const uint64_t *tmp, uint32_t n,
+                          cudaStream_t st);
 // Diagnostics over the current cell list.
 void launch_neighbor_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand,
                            uint32_t *n_inter, uint64_t *hash, cudaStream_t st);

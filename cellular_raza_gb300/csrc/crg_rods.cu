@@ -220,11 +220,66 @@ __device__ __forceinline__ void bend_force(const SimDev &S, const double *c1, co
   }
 }
 
+// CartesianSubDomainRods::apply_boundary (bacterial_rods.rs:489-534) on a rod's updated
+// vertices, then its next voxel key from the centroid row_sum / nrows (:550-554); writes
+// the next state at `slot` and counts the key.  `key`: the voxel the rod stays in when the
+// new index falls outside the grid; `id`: the identifier a BoundaryError reports.
+template <int D, int NV>
+__device__ __forceinline__ void rod_finish(const PackArgs &P, const SimDev &S, uint32_t slot,
+                                           uint32_t key, uint64_t id, double *np, double *nvl) {
+  constexpr int NC = NV * D;
+  const int64_t cap = P.cap;
+  bool inside = true;
+#pragma unroll
+  for (int s = 0; s < NV; ++s)
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      double &p = np[s * D + c];
+      double &u = nvl[s * D + c];
+      if (p < S.min[c]) {
+        p = dsub(dmul(S.min[c], 2.0), p);
+        u = fabs(u);
+      }
+      if (p > S.max[c]) {
+        p = dsub(dmul(S.max[c], 2.0), p);
+        u = -fabs(u);
+      }
+    }
+#pragma unroll
+  for (int k = 0; k < NC; ++k)
+    if (np[k] < S.min[k % D] || np[k] > S.max[k % D]) inside = false;
+  if (!inside) set_status(P.status, CRG_EBOUNDARY, id, *P.step_ctr + 1, S.sim_index);
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    P.npos[k * cap + slot] = np[k];
+    P.nvel[k * cap + slot] = nvl[k];
+  }
+  double cen[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) s = dadd(s, np[q * D + c]);
+    cen[c] = ddiv(s, (double)NV);
+  }
+  uint32_t plain;
+  uint32_t nk = key;
+  if (voxel_of<D>(S, cen, plain) == 0) nk = S.voxel_off + plain;
+  if (nk - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteNextKey, slot);
+    nk = key;
+  }
+  P.nkey[slot] = nk;
+  atomicAdd(&P.count[nk], 1u);
+}
+
 // BEND: the curvature forces were computed by k_rods_bend (P.bend), else they are computed
-// here.  Same values, same order of additions either way.
-template <int D, int NV, bool BEND = false>
+// here.  Same values, same order of additions either way.  CYC: cell cycle off (0), on (1)
+// or decided by P.dflag at run time (-1).
+template <int D, int NV, bool BEND = false, int CYC = -1>
 __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, uint32_t i,
                                            uint32_t key, const double *pa, const double *acc) {
+  const bool cyc = (CYC < 0) ? (P.dflag != nullptr) : (CYC == 1);
   constexpr int NC = NV * D;
   const int64_t cap = P.cap;
   if (P.dbg_force) {
@@ -234,6 +289,7 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   double va[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) va[k] = P.vel[k * cap + i];
+  const double l0 = cyc ? P.slen[i] : S.spring_length;  // RodMechanics::spring_length
   double tf[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) tf[k] = acc[k];
@@ -250,7 +306,7 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         const double dir = ddiv(dist[s][c], nrm);
-        const double fi = dmul(dmul(-dir, S.spring_tension), dsub(nrm, S.spring_length));
+        const double fi = dmul(dmul(-dir, S.spring_tension), dsub(nrm, l0));
         tf[s * D + c] = dadd(tf[s * D + c], dmul(fi, 0.5));
         tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], dmul(-fi, 0.5));
       }
@@ -322,51 +378,37 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
     P.nhmeta[i] = 1;
   }
 
-  // CartesianSubDomainRods::apply_boundary (bacterial_rods.rs:489-534).
-  bool inside = true;
-#pragma unroll
-  for (int s = 0; s < NV; ++s)
-#pragma unroll
-    for (int c = 0; c < D; ++c) {
-      double &p = np[s * D + c];
-      double &u = nvl[s * D + c];
-      if (p < S.min[c]) {
-        p = dsub(dmul(S.min[c], 2.0), p);
-        u = fabs(u);
-      }
-      if (p > S.max[c]) {
-        p = dsub(dmul(S.max[c], 2.0), p);
-        u = -fabs(u);
-      }
+  // Cell cycle (bacterial_rods/src/main.rs:66-98), run after local_mechanics_update as the
+  // macro orders the local functions (run_sim.rs:258-283): react_to_neighbors sets the
+  // growth rate from this step's neighbour count, update_cycle grows the spring length and
+  // flags a division.  A dividing rod leaves reflection and voxel key to k_rods_divide:
+  // chili divides (update_cell_cycle_4) before it applies the boundary.
+  if (cyc) {
+    const uint32_t nn = P.nsense[i];
+    double g = S.cyc_growth;
+    if (nn > 0u) {
+      const double x = ddiv(dmul(S.cyc_growth, dsub(S.cyc_sat, (double)nn)), S.cyc_sat);
+      g = (x > 0.0) ? x : 0.0;  // f64::max(x, 0.0): 0 for NaN and negative rates
     }
+    const double l1 = dadd(l0, dmul(g, dt));
+    P.ngrate[i] = g;
+    P.nslen[i] = l1;
+    P.nparent[i] = P.parent[i];
+    const bool divides = l1 > S.cyc_div_len;
+    P.dflag[i] = divides ? 1u : 0u;
+    if (divides) {
 #pragma unroll
-  for (int k = 0; k < NC; ++k)
-    if (np[k] < S.min[k % D] || np[k] > S.max[k % D]) inside = false;
-  if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1, S.sim_index);
-#pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    P.npos[k * cap + i] = np[k];
-    P.nvel[k * cap + i] = nvl[k];
+      for (int k = 0; k < NC; ++k) {
+        P.npos[k * cap + i] = np[k];
+        P.nvel[k * cap + i] = nvl[k];
+      }
+      P.nkey[i] = key;
+      P.nid[i] = P.id[i];
+      return;
+    }
   }
-  // Next key from the centroid row_sum / nrows (bacterial_rods.rs:550-554).
-  double cen[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    double s = 0.0;
-#pragma unroll
-    for (int q = 0; q < NV; ++q) s = dadd(s, np[q * D + c]);
-    cen[c] = ddiv(s, (double)NV);
-  }
-  uint32_t plain;
-  uint32_t nk = key;
-  if (voxel_of<D>(S, cen, plain) == 0) nk = S.voxel_off + plain;
-  if (nk - S.voxel_off >= S.n_vox) {
-    invariant_failed(P.status, kSiteNextKey, i);
-    nk = key;
-  }
-  P.nkey[i] = nk;
+  rod_finish<D, NV>(P, S, i, key, P.id[i], np, nvl);
   P.nid[i] = P.id[i];
-  atomicAdd(&P.count[nk], 1u);
 }
 
 template <int D, int NV, int B>
@@ -1811,7 +1853,7 @@ __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
 // in-order sum of its passes' M / 2 in mbuf, or after a pass list overflow the force
 // k_rods_queue stored in frc -- and its curvature forces in bend.  Frozen simulations copy
 // their state.
-template <int D, int NV>
+template <int D, int NV, int CYC>
 __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   constexpr int NC = NV * D;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1844,7 +1886,7 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
       for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], mb[k * pcap + p]);
     }
   }
-  rod_update<D, NV, true>(P, S, i, key, pa, acc);
+  rod_update<D, NV, true, CYC>(P, S, i, key, pa, acc);
 }
 
 // Candidate rods of the current cell list, a hash of their ids and the number of in-range
@@ -1896,6 +1938,247 @@ __global__ void k_rod_stats(const PackArgs P, uint32_t *n_cand, uint32_t *n_inte
   hash[i] = h;
 }
 
+// ---------------------------------------------------------------------------------------
+// Cell cycle of rods (single-simulation handles).
+// ---------------------------------------------------------------------------------------
+
+// NeighborSensing::accumulate_information of the bacterial-rods agent (bacterial_rods/src/
+// main.rs:49-64) over the partners chili lets a rod meet as "own" in one step
+// (update_mechanics.rs:105, 201-202; remote partners through the positions received in
+// step 2): every other rod of the 3^D neighbourhood, once.  The count is a sum of
+// integers, so the visiting order does not matter.  One thread per rod, FP64 distances as
+// nalgebra's norm() forms them; a partner whose bounding box lies farther than the range
+// (plus a relative 1e-9 for the roundings) from the rod's on some axis is skipped, since no
+// vertex pair of it can then be closer than the range.
+template <int D, int NV>
+__global__ void k_rods_sense(const PackArgs P) {
+  constexpr int NC = NV * D;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n_agents) return;
+  const SimDev &S = P.sims[0];
+  const int64_t cap = P.cap;
+  const uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteForceKey, i);
+    P.nsense[i] = 0u;
+    return;
+  }
+  int idx[D];
+  unravel<D>(S, key - S.voxel_off, idx);
+  double pa[NC], lo_a[D], hi_a[D];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo_a[c] = hi_a[c] = pa[c];
+#pragma unroll
+    for (int q = 1; q < NV; ++q) {
+      lo_a[c] = fmin(lo_a[c], pa[q * D + c]);
+      hi_a[c] = fmax(hi_a[c], pa[q * D + c]);
+    }
+  }
+  const double r = S.cyc_sense;
+  const double thr = dadd(r, dmul(fabs(r), 1e-9));
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+  }
+  uint32_t cnt = 0;
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        if (b0 > b1 || b1 > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b1 = b0;
+        }
+        for (uint32_t b = b0; b < b1; ++b) {
+          if (b == i) continue;
+          double pb[NC];
+#pragma unroll
+          for (int k = 0; k < NC; ++k) pb[k] = P.pos[k * cap + b];
+          bool far = false;
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            double lb = pb[c], hb = pb[c];
+#pragma unroll
+            for (int q = 1; q < NV; ++q) {
+              lb = fmin(lb, pb[q * D + c]);
+              hb = fmax(hb, pb[q * D + c]);
+            }
+            far |= dsub(lb, hi_a[c]) > thr || dsub(lo_a[c], hb) > thr;
+          }
+          if (far) continue;
+#pragma unroll
+          for (int u = 0; u < NV; ++u)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) {
+              double n2 = 0.0;
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const double d = dsub(pa[u * D + c], pb[q * D + c]);
+                n2 = (c == 0) ? dmul(d, d) : dadd(n2, dmul(d, d));
+              }
+              if (__dsqrt_rn(n2) < r) ++cnt;
+            }
+        }
+      }
+  P.nsense[i] = cnt;
+}
+
+// Voxel::update_cell_cycle_4 (chili/update_cycle.rs:10-69) for the rods the update kernel
+// flagged, then SubDomainBox::apply_boundary and the next voxel keys of both halves.
+// dpre is the exclusive scan of the flags over the cell list, so inside voxel v (cell-list
+// range [start[v], start[v+1])) the dividing rods are numbered r = dpre[i] - dpre[start[v]]
+// of m = dpre[start[v+1]] - dpre[start[v]] in storage order, as chili visits them:
+//   * the parent is renamed Division(v, counter + r + 1) and its daughter, appended to the
+//     voxel after every other rod of it, becomes Division(v, counter + m + r + 1);
+//   * in chili's pre-sort order (voxels ascending, each voxel's Vec) rod i sits at
+//     i + dpre[start[v]] and the daughter at start[v+1] + dpre[i]: the sort ranks them so.
+// The daughter's state goes to n_agents + dpre[i] of the next-state arrays, with a fresh
+// solver history (default aux storage).  RodMechanics::divide (bacterial_rods.rs:586-663):
+// both halves get (1/2 - R / (n spring_length)) spring_length; the first keeps the first
+// vertex, the second the last, and the vertices are spread along the old polyline at
+// steps of (length - 2 R) / (n - 1) / 2; float sums start at -0.0 as Rust's Sum for f64.
+template <int D, int NV>
+__global__ void k_rods_divide(const PackArgs P) {
+  constexpr int NC = NV * D;
+  const uint32_t n = P.n_agents;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SimDev &S = P.sims[0];
+  const int64_t cap = P.cap;
+  const uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) {
+    invariant_failed(P.status, kSiteForceKey, i);
+    P.srank[i] = i;
+    return;
+  }
+  const uint32_t d_lo = P.dpre[P.start[key]];
+  const uint32_t di = P.dpre[i];
+  P.srank[i] = i + d_lo;
+  if (P.dpre[i + 1] == di) return;  // not dividing: k_rods_update finished it
+  const uint32_t m = P.dpre[P.start[key + 1]] - d_lo;
+  const uint32_t r = di - d_lo;
+  const uint32_t j = n + di;
+  P.srank[j] = P.start[key + 1] + di;
+  const uint64_t c0 = P.vctr[key];
+  const uint64_t plain = key - S.voxel_off;
+  const uint64_t old = P.id[i];
+  const uint64_t pid = CRG_ID_DIVISION | (plain << 32) | ((c0 + r + 1) & 0xffffffffull);
+  const uint64_t did = CRG_ID_DIVISION | (plain << 32) | ((c0 + m + r + 1) & 0xffffffffull);
+
+  double pos[NC], v1[NC], v2[NC], c1[NC], c2[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    pos[k] = P.npos[k * cap + i];
+    v1[k] = v2[k] = P.nvel[k * cap + i];
+    c1[k] = c2[k] = pos[k];
+  }
+  const double slen = P.nslen[i];
+  const double radius = S.radius;
+  const double div_factor = dsub(0.5, ddiv(radius, dmul((double)NV, slen)));
+  const double nsl = dmul(div_factor, slen);
+  double seg[NV - 1];
+#pragma unroll
+  for (int q = 0; q + 1 < NV; ++q) {
+    double n2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const double d = dsub(pos[q * D + c], pos[(q + 1) * D + c]);
+      n2 = (c == 0) ? dmul(d, d) : dadd(n2, dmul(d, d));
+    }
+    seg[q] = __dsqrt_rn(n2);
+  }
+  double total = -0.0;
+#pragma unroll
+  for (int q = 0; q + 1 < NV; ++q) total = dadd(total, seg[q]);
+  const double seglen = ddiv(ddiv(dsub(total, dmul(2.0, radius)), (double)(NV - 1)), 2.0);
+  bool ok = true;
+  for (int nvx = 0; nvx < NV; ++nvx) {
+    const double target = dmul((double)nvx, seglen);
+    int k = -1;
+    double pk = 0.0, acc = -0.0;
+    for (int q = 0; q < NV - 1; ++q) {  // sums of the first q segments
+      if (acc <= target) {
+        k = q;
+        pk = acc;
+      }
+      acc = dadd(acc, seg[q]);
+    }
+    int mm = -1;
+    double rm = 0.0;
+    acc = -0.0;
+    for (int q = 0; q < NV; ++q) {  // sums of the last q segments, last first
+      if (acc <= target) {
+        mm = q;
+        rm = acc;
+      }
+      if (q < NV - 1) acc = dadd(acc, seg[NV - 2 - q]);
+    }
+    if (k < 0 || mm < 0 || NV - mm - 2 < 0) {
+      ok = false;
+      break;
+    }
+    const double qf = ddiv(dsub(target, pk), seg[k]);
+    const double pf = ddiv(dsub(target, rm), seg[NV - mm - 2]);
+    const double omq = dsub(1.0, qf), omp = dsub(1.0, pf);
+    for (int c = 0; c < D; ++c) {
+      c1[nvx * D + c] = dadd(dmul(pos[k * D + c], omq), dmul(pos[(k + 1) * D + c], qf));
+      c2[(NV - nvx - 1) * D + c] =
+          dadd(dmul(pos[(NV - mm - 1) * D + c], omp), dmul(pos[(NV - mm - 2) * D + c], pf));
+    }
+  }
+  if (!ok) {  // DivisionError: the step reports it; both halves stay copies of the parent
+    set_status(P.status, CRG_ECALC, old, *P.step_ctr + 1, S.sim_index);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) c1[k] = c2[k] = pos[k];
+  }
+  P.nid[i] = pid;
+  P.nid[j] = did;
+  P.nparent[i] = old;
+  P.nparent[j] = old;
+  P.nslen[i] = nsl;
+  P.nslen[j] = nsl;
+  P.ngrate[j] = P.ngrate[i];
+  if (P.nhist) {
+    for (int k = 0; k < 2 * NC; ++k) P.nhist[k * cap + j] = 0.0;
+    P.nhmeta[j] = 0;
+  }
+  // the voxel the daughter was appended to: its move class in the sort
+  const_cast<uint32_t *>(P.key)[j] = key;
+  rod_finish<D, NV>(P, S, i, key, pid, c1, v1);
+  rod_finish<D, NV>(P, S, j, key, did, c2, v2);
+}
+
+// Voxel::id_counter after insert_initial_cells (chili/datastructures.rs:278-299): one per
+// agent inserted into the voxel.
+__global__ void k_cycle_init(const PackArgs P) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= P.n_vox) return;
+  P.vctr[v] = (uint64_t)(P.start[v + 1] - P.start[v]);
+}
+
+// Per-agent values given in upload order moved to the cell list: slot s holds the agent
+// the upload's sort took from input index tmp[s] (its low 31 bits).
+__global__ void k_cycle_permute(double *dst, const double *src, const uint64_t *tmp,
+                                uint32_t n) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  dst[s] = src[(uint32_t)(tmp[s] & 0x7fffffffull)];
+}
+
+// Voxel::id_counter after the divisions of the step: + 2 per division in the voxel.
+__global__ void k_cycle_counters(const PackArgs P) {
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= P.n_vox) return;
+  P.vctr[v] += 2ull * (uint64_t)(P.dpre[P.start[v + 1]] - P.dpre[P.start[v]]);
+}
+
 // Resident warps of k_rods_queue / k_rods_passq on the current device, [D - 2][NV]
 // (set by prepare_rods).
 unsigned g_queue_warps[2][9] = {};
@@ -1944,7 +2227,10 @@ void launch_t(const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0, cud
     const uint64_t nb = ((uint64_t)P.n_agents * (NV - 2) + 127) / 128;
     k_rods_bend<D, NV><<<(unsigned)nb, 128, 0, st>>>(P);
   }
-  k_rods_update<D, NV><<<rblocks, 128, 0, st>>>(P);
+  if (P.dflag)
+    k_rods_update<D, NV, 1><<<rblocks, 128, 0, st>>>(P);
+  else
+    k_rods_update<D, NV, 0><<<rblocks, 128, 0, st>>>(P);
 }
 
 template <int D, int NV>
@@ -2033,6 +2319,55 @@ void launch_stats_d(int nv, const PackArgs &P, uint32_t *n_cand, uint32_t *n_int
     case 8: k_rod_stats<D, 8><<<grid, 128, 0, st>>>(P, n_cand, n_inter, hash); break;
     default: break;
   }
+}
+
+template <int D>
+void launch_cycle_d(int nv, const PackArgs &P, bool divide, cudaStream_t st) {
+  const unsigned grid = (P.n_agents + 127) / 128;
+#define CRG_CYCLE_CASE(NVV)                                        \
+  case NVV:                                                        \
+    if (divide)                                                    \
+      k_rods_divide<D, NVV><<<grid, 128, 0, st>>>(P);              \
+    else                                                           \
+      k_rods_sense<D, NVV><<<grid, 128, 0, st>>>(P);               \
+    break;
+  switch (nv) {
+    CRG_CYCLE_CASE(2)
+    CRG_CYCLE_CASE(3)
+    CRG_CYCLE_CASE(4)
+    CRG_CYCLE_CASE(5)
+    CRG_CYCLE_CASE(6)
+    CRG_CYCLE_CASE(7)
+    CRG_CYCLE_CASE(8)
+    default: break;
+  }
+#undef CRG_CYCLE_CASE
+}
+
+void launch_rods_sense(int dim, int nv, const PackArgs &P, cudaStream_t st) {
+  if (!P.n_agents) return;
+  if (dim == 3)
+    launch_cycle_d<3>(nv, P, false, st);
+  else
+    launch_cycle_d<2>(nv, P, false, st);
+}
+
+void launch_rods_divide(int dim, int nv, const PackArgs &P, uint32_t n_div, cudaStream_t st) {
+  if (!P.n_agents || !n_div) return;
+  if (dim == 3)
+    launch_cycle_d<3>(nv, P, true, st);
+  else
+    launch_cycle_d<2>(nv, P, true, st);
+  k_cycle_counters<<<(P.n_vox + 255) / 256, 256, 0, st>>>(P);
+}
+
+void launch_cycle_init(const PackArgs &P, cudaStream_t st) {
+  k_cycle_init<<<(P.n_vox + 255) / 256, 256, 0, st>>>(P);
+}
+
+void launch_cycle_permute(double *dst, const double *src, const uint64_t *tmp, uint32_t n,
+                          cudaStream_t st) {
+  if (n) k_cycle_permute<<<(n + 255) / 256, 256, 0, st>>>(dst, src, tmp, n);
 }
 
 void launch_rod_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,

@@ -131,7 +131,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_single(uint32_t *__restri
   if (threadIdx.x == 0) start[n] = tot;
 }
 
-// Slot assignment.  Sort key = class << 32 | previous position.
+// Slot assignment.  Sort key = class << 62 | rank << 31 | index, where the rank is the
+// agent's previous position (with divisions: its position in chili's pre-sort order, the
+// daughters of a voxel following its other agents) and the index locates its state.
 __global__ void k_scatter(const SortArgs A) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.n_agents) return;
@@ -154,7 +156,8 @@ __global__ void k_scatter(const SortArgs A) {
     invariant_failed(A.status, kSiteScatterSlot, i);
     return;
   }
-  A.tmp[slot] = ((uint64_t)cls << 32) | (uint64_t)i;
+  const uint32_t rank = A.srank ? A.srank[i] : i;
+  A.tmp[slot] = ((uint64_t)cls << 62) | ((uint64_t)rank << 31) | (uint64_t)i;
 }
 
 // One thread per voxel: order the voxel's segment and reset its histogram counter.
@@ -186,7 +189,7 @@ __global__ void k_gather(const SortArgs A) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && A.step_ctr) *A.step_ctr += 1;
   if (s >= A.n_agents) return;
-  uint32_t src = (uint32_t)(A.tmp[s] & 0xffffffffull);
+  uint32_t src = (uint32_t)(A.tmp[s] & 0x7fffffffull);
   if (src >= A.n_agents) {
     invariant_failed(A.status, kSiteGatherSrc, s);
     src = s;
@@ -227,6 +230,11 @@ __global__ void k_gather(const SortArgs A) {
   if (A.hist) {
     for (int c = 0; c < 2 * nc; ++c) A.hist[c * cap + s] = A.nhist[c * cap + src];
     A.hmeta[s] = A.nhmeta[src];
+  }
+  if (A.slen) {
+    A.slen[s] = A.nslen[src];
+    A.grate[s] = A.ngrate[src];
+    A.parent[s] = A.nparent[src];
   }
 }
 
@@ -325,15 +333,20 @@ static inline unsigned grid_for(uint64_t n, unsigned block) {
   return (unsigned)((n + block - 1) / block);
 }
 
-void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
-  const uint32_t nb = (A.n_vox + kScanTile - 1) / kScanTile;
+void launch_scan(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
+                 cudaStream_t st) {
+  const uint32_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb <= 1) {
-    k_scan_single<<<1, kScanThreads, 0, st>>>(A.count, A.n_vox, A.start);
+    k_scan_single<<<1, kScanThreads, 0, st>>>(count, n, start);
   } else {
-    k_scan_reduce<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum);
-    k_scan_blocks<<<1, kScanThreads, 0, st>>>(bsum, nb, A.start, A.n_vox);
-    k_scan_final<<<nb, kScanThreads, 0, st>>>(A.count, A.n_vox, bsum, A.start);
+    k_scan_reduce<<<nb, kScanThreads, 0, st>>>(count, n, bsum);
+    k_scan_blocks<<<1, kScanThreads, 0, st>>>(bsum, nb, start, n);
+    k_scan_final<<<nb, kScanThreads, 0, st>>>(count, n, bsum, start);
   }
+}
+
+void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
+  launch_scan(A.count, A.n_vox, A.start, bsum, st);
   if (A.n_agents) k_scatter<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
   k_segsort<<<grid_for(A.n_vox, 256), 256, 0, st>>>(A);
   if (A.n_agents) k_gather<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
@@ -424,7 +437,7 @@ __global__ void k_noalloc_keys(const crg::SimDev S, uint32_t n, const double *__
 __global__ void k_noalloc_order(const uint64_t *__restrict__ tmp, uint32_t n,
                                 uint32_t *__restrict__ order) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) order[s] = (uint32_t)(tmp[s] & 0xffffffffull);
+  if (s < n) order[s] = (uint32_t)(tmp[s] & 0x7fffffffull);  // the index field of the sort key
 }
 
 }  // namespace

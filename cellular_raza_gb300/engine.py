@@ -42,6 +42,9 @@ def to_c(model: Model):
               "radius", "stiffness", "cutoff", "strength", "dt", "kb_temperature"):
         setattr(m, f, float(getattr(model, f)))
     m.rng_seed = int(model.rng_seed)
+    m.cycle = 1 if getattr(model, "cycle", False) else 0
+    for f in ("growth_rate", "division_length", "sense_range", "sense_saturation"):
+        setattr(m, f, float(getattr(model, f, 0.0)))
     return d, m
 
 
@@ -124,10 +127,22 @@ class Simulation:
         self._L.crg_agent_count(self._h, C.byref(n))
         return n.value
 
+    def set_spring_lengths(self, spring_length: np.ndarray):
+        """Cell cycle: per-rod spring lengths in the order of the last upload (before the
+        first step)."""
+        sl = np.ascontiguousarray(spring_length, dtype=np.float64)
+        if sl.shape != (self.n_agents,):
+            raise ValueError("one spring length per uploaded rod")
+        N.check(self._L.crg_set_spring_lengths(self._h, _dp(sl)), "crg_set_spring_lengths",
+                self._h)
+
     def download(self, order: str = "list") -> Dict[str, np.ndarray]:
         """Current state.  order="list": cell-list order; "id": per simulation sorted by id
-        (ids 0..n-1 when upload was given no ids)."""
+        (ids 0..n-1 when upload was given no ids).  Cell-cycle handles add spring_length,
+        growth_rate and parent."""
         n = self.n_agents
+        if len(self.models) == 1:
+            self.counts = [n]  # divisions change the count
         shape = (n, self.nv, self.dim)
         pos = np.empty(shape)
         vel = np.empty(shape)
@@ -138,6 +153,14 @@ class Simulation:
                                   vox.ctypes.data_as(C.POINTER(C.c_uint32)))
         N.check(rc, "crg_download", self._h)
         out = {"pos": pos, "vel": vel, "ids": ids, "voxel": vox}
+        if getattr(self.models[0], "cycle", False):
+            out["spring_length"] = np.empty(n)
+            out["growth_rate"] = np.empty(n)
+            out["parent"] = np.empty(n, np.uint64)
+            rc = self._L.crg_download_cycle(self._h, _dp(out["spring_length"]),
+                                            _dp(out["growth_rate"]),
+                                            out["parent"].ctypes.data_as(C.POINTER(C.c_uint64)))
+            N.check(rc, "crg_download_cycle", self._h)
         if order == "id":
             out = self._by_id(out)
         return out
@@ -229,13 +252,19 @@ def measure_fma_peaks():
 
 
 def run(workload, n_steps: Optional[int] = None, options: Optional[Dict[int, int]] = None,
-        order: str = "id") -> Dict[str, np.ndarray]:
+        order: str = "id", capacity: Optional[int] = None) -> Dict[str, np.ndarray]:
     """Upload a workload, run it and return the final state (ordered by id by default).
-    ``options`` maps CRG_OPT_* values to settings."""
+    ``options`` maps CRG_OPT_* values to settings.  A cell-cycle workload gets room for 16
+    times its agents unless ``capacity`` says otherwise."""
     steps = workload.n_steps if n_steps is None else n_steps
-    with Simulation.single(workload.model, workload.n) as sim:
+    cycle = getattr(workload.model, "cycle", False)
+    if capacity is None:
+        capacity = 16 * workload.n if cycle else workload.n
+    with Simulation.single(workload.model, capacity) as sim:
         for k, v in (options or {}).items():
             sim.set_option(k, v)
         sim.upload(workload.pos, workload.vel)
+        if cycle and getattr(workload, "spring_length", None) is not None:
+            sim.set_spring_lengths(workload.spring_length)
         sim.step(steps)
         return sim.download(order=order)

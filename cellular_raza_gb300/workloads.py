@@ -57,6 +57,13 @@ class Model:
     cutoff: float = 15.0
     strength: float = 0.5
     dt: float = 0.01
+    # Cell cycle of the bacterial-rods agent (rods only): growth limited by neighbour
+    # sensing, division past division_length
+    cycle: bool = False
+    growth_rate: float = 0.0
+    division_length: float = 0.0
+    sense_range: float = 0.0
+    sense_saturation: float = 8.0
 
     @property
     def nc(self) -> int:
@@ -73,6 +80,7 @@ class Workload:
     pos: np.ndarray  # [n][nv][dim]
     vel: np.ndarray
     n_steps: int
+    spring_length: Optional[np.ndarray] = None  # cell cycle: per-rod initial spring lengths
 
     @property
     def n(self) -> int:
@@ -146,6 +154,36 @@ def rods_2d(seed: int = 0, n: int = 100_000, n_subdomains: int = 1, **kw) -> Wor
     w = rods(n, side, seed, n_subdomains=n_subdomains, **kw)
     w.name, w.n_steps = "rods_2d", 500
     return w
+
+
+def rod_colony(n: int = 200, side: float = 300.0, seed: int = 0, dim: int = 2,
+               n_vertices: int = 5, growth_rate: float = 2.0, **model_kw) -> Workload:
+    """A growing colony with the bacterial-rods example's agent (cellular_raza-examples/
+    bacterial_rods/src/main.rs:114-150, units dropped): RodMechanics (tension 10, rigidity 1,
+    damping 1.5), RodInteraction(Morse radius 3, stiffness 0.5, strength 0.1, cutoff 5),
+    division past spring length 6, neighbour sensing of vertex pairs closer than 2 x radius
+    with saturation 8.  dt is 0.01 rather than the example's 0.1: forward Euler on the
+    spring chain is stable only while omega^2 dt < damping (omega^2 up to ~4 x tension).
+    Spring lengths start uniform in [1.5, 5.5] (the vertices spaced accordingly) and the
+    base growth rate is raised from 0.1 so that divisions start within tens of steps."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    slen = rng.uniform(1.5, 5.5, size=n)
+    centres = rng.uniform(0.2 * side, 0.8 * side, size=(n, dim))
+    theta = rng.uniform(0.0, 2.0 * math.pi, size=n)
+    direction = np.zeros((n, dim))
+    direction[:, 0] = np.cos(theta)
+    direction[:, 1] = np.sin(theta)
+    k = np.arange(n_vertices) - (n_vertices - 1) / 2.0
+    pos = centres[:, None, :] + k[None, :, None] * slen[:, None, None] * direction[:, None, :]
+    vel = np.zeros_like(pos)
+    kw = dict(kind="rod", dim=dim, n_vertices=n_vertices, domain_min=(0.0,) * dim,
+              domain_max=(side,) * dim, interaction_range=20.0, spring_tension=10.0,
+              rigidity=1.0, spring_length=3.0, damping=1.5, diffusion=0.0, radius=3.0,
+              stiffness=0.5, cutoff=5.0, strength=0.1, dt=0.01, cycle=True,
+              growth_rate=growth_rate, division_length=6.0, sense_range=6.0,
+              sense_saturation=8.0)
+    kw.update(model_kw)
+    return Workload("rod_colony", Model(**kw), pos, vel, 200, slen)
 
 
 def ensemble(seed: int = 0, n_sims: int = 1024, n_lo: int = 256, n_hi: int = 65536,

@@ -95,7 +95,23 @@ typedef struct crg_model {
   double dt;
   double kb_temperature; /* Brownian / Langevin k_B T */
   uint64_t rng_seed;     /* seed of the stochastic mechanics' random stream */
+  /* Cell cycle (rods, single-simulation handles; 0 = off): the bacterial-rods agent's
+   * Cycle + NeighborSensing (cellular_raza-examples/bacterial_rods/src/main.rs:48-112).
+   * Each step every rod counts the vertex pairs it shares with the agents it meets that
+   * are closer than sense_range (n); its growth rate becomes growth_rate * (sense_saturation
+   * - n) / sense_saturation, at least 0, when n > 0, else growth_rate; its spring length
+   * grows by rate * dt, and past division_length it divides (RodMechanics::divide with the
+   * Morse radius, bacterial_rods.rs:586-663).  Agent counts then change from step to step. */
+  int32_t cycle;
+  double growth_rate, division_length, sense_range, sense_saturation;
 } crg_model;
+
+/* Identifiers of agents made or renamed by a division: chili's CellIdentifier::Division(
+ * voxel plain index, voxel counter) (cellular_raza-concepts/src/cell.rs:18-25, chili/
+ * update_cycle.rs:30-64), encoded as CRG_ID_DIVISION | voxel << 32 | counter.  Initial
+ * agents keep the ids given to crg_upload and have parent CRG_NO_PARENT. */
+#define CRG_ID_DIVISION (1ull << 63)
+#define CRG_NO_PARENT (~0ull)
 
 typedef struct crg_ctx crg_ctx;
 
@@ -185,6 +201,16 @@ int32_t crg_server_destroy(crg_server *srv);
 
 /* Number of agents currently held (total over simulations of a batch). */
 int32_t crg_agent_count(crg_ctx *ctx, int64_t *n);
+
+/* Cell cycle: per-rod spring lengths in the order of the arrays given to the last
+ * crg_upload (call after it and before stepping; default: the model's spring_length). */
+int32_t crg_set_spring_lengths(crg_ctx *ctx, const double *spring_length);
+
+/* Cell cycle: per-agent spring length, growth rate and parent identifier, in the order
+ * of crg_download.  Any pointer may be NULL.  A step whose divisions would take the agent
+ * count past the handle's capacity stops with CRG_ENOMEM; a DivisionError is CRG_ECALC. */
+int32_t crg_download_cycle(crg_ctx *ctx, double *spring_length, double *growth_rate,
+                           uint64_t *parent);
 
 /* First error seen on the device: code, agent id and 1-based step (or -1). */
 int32_t crg_last_error(crg_ctx *ctx, int64_t *agent, int64_t *step);

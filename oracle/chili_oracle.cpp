@@ -317,6 +317,10 @@ struct Sim {
     uint64_t id;
     double pos[NC];
     double vel[NC];
+    // cell cycle (rods): RodMechanics::spring_length, the agent's growth_rate and the
+    // identifier of the agent it divided from
+    double slen = 0.0, grate = 0.0;
+    uint64_t parent = OR_NO_PARENT;
   };
   // AuxStorageMechanics (chili/aux_storage.rs:41-130) with RingBuffer<_, order-1>.
   struct Aux {
@@ -324,6 +328,8 @@ struct Sim {
     double hx[2][NC];
     double hv[2][NC];
     int first = 0, size = 0;
+    uint32_t nsense = 0;   // AuxStorageInteraction's NeighborSensing accumulator
+    bool divide = false;   // CycleEvent::Division pending
   };
   struct Entry {
     Cell c;
@@ -333,6 +339,12 @@ struct Sim {
     uint64_t plain;
     std::vector<uint64_t> nbrs;
     std::vector<Entry> cells;
+    uint64_t id_counter = 0;  // Voxel::id_counter (chili/datastructures.rs:42)
+  };
+  // Cell cycle parameters (or_cycle).
+  struct CycleP {
+    bool on = false;
+    double growth = 0.0, div_len = 0.0, sense = 0.0, sat = 0.0;
   };
   // PosInformation / ForceInformation / SendCell (chili/update_mechanics.rs:19-61).
   struct PosInfo {
@@ -357,6 +369,7 @@ struct Sim {
 
   Domain dom;
   Params prm;
+  CycleP cyc;
   std::vector<uint32_t> sub_of;  // voxel plain -> subdomain
   std::vector<Box> boxes;
   int S = 1;
@@ -371,6 +384,7 @@ struct Sim {
   std::vector<double> dbg_force;  // indexed by id
   int64_t step_base = 0;          // steps run by earlier calls (random stream index)
   int64_t n_agents = 0;
+  const double *slen_in = nullptr;  // cell cycle: initial spring lengths (input order)
 
   static void zero(double *x) {
     for (int k = 0; k < NC; ++k) x[k] = 0.0;
@@ -422,6 +436,21 @@ struct Sim {
     got_error.store(1);
   }
 
+  // neighbor_sensing_single (update_mechanics.rs:578-591) with the bacterial-rods agent's
+  // NeighborSensing::accumulate_information (bacterial_rods/src/main.rs:49-64): every pair
+  // of an own vertex and an ext vertex closer than the sensing range counts once.
+  void sense(Aux &a, const double *own, const double *ext) const {
+    if (!cyc.on) return;
+    for (int i = 0; i < NV; ++i)
+      for (int j = 0; j < NV; ++j) {
+        double d[D];
+        for (int c = 0; c < D; ++c) d[c] = own[i * D + c] - ext[j * D + c];
+        double n2 = d[0] * d[0];
+        for (int c = 1; c < D; ++c) n2 = n2 + d[c] * d[c];
+        if (std::sqrt(n2) < cyc.sense) a.nsense += 1;
+      }
+  }
+
   // Voxel::calculate_force_between_cells_external (update_mechanics.rs:65-108).
   // Returns false when the voxel holds no cells (force is None).
   bool force_external(Voxel &vox, const double *ext_pos, double ext_info, double *force) {
@@ -431,6 +460,7 @@ struct Sim {
       double f1[NC], f2[NC];
       calc(e.c.pos, ext_pos, ext_info, f1, f2);
       add_half(e.a.force, f1);
+      sense(e.a, e.c.pos, ext_pos);  // update_mechanics.rs:105
       if (some) {
         for (int k = 0; k < NC; ++k) force[k] = f2[k] * one_half + force[k];
       } else {
@@ -461,6 +491,8 @@ struct Sim {
           calc(e2.c.pos, c1.pos, i1, g2, g1);
           add_half(e1.a.force, g1);
           add_half(e2.a.force, g2);
+          sense(e1.a, c1.pos, e2.c.pos);  // update_mechanics.rs:201-202
+          sense(e2.a, e2.c.pos, c1.pos);
         }
         for (uint64_t nb : vox.nbrs) {
           Voxel *nv = voxel_local(b, nb);
@@ -573,7 +605,7 @@ struct Sim {
           double fi[D];
           for (int c2 = 0; c2 < D; ++c2) {
             double dir = dist[i][c2] / nrm;
-            fi[c2] = -dir * prm.spring_tension * (nrm - prm.spring_length);
+            fi[c2] = -dir * prm.spring_tension * (nrm - c.slen);
           }
           for (int c2 = 0; c2 < D; ++c2) tf[i * D + c2] += fi[c2] * one_half;
           for (int c2 = 0; c2 < D; ++c2) tf[(i + 1) * D + c2] += -fi[c2] * one_half;
@@ -707,11 +739,142 @@ struct Sim {
     if (!(NV == 1 && prm.kind == OR_KIND_BROWNIAN)) std::memcpy(e.c.vel, nv, sizeof(nv));
   }
 
+  // The local cell functions in the macro's order (run_sim.rs:258-283):
+  // local_mechanics_update, local_interaction_react_to_neighbors, local_cycle_update.
   void update_local(int s, bool last, int64_t step) {
     Box &b = boxes[s];
     int64_t dummy = 0;
     for (Voxel &v : b.voxels)
-      for (Entry &e : v.cells) mechanics_update(e, step, (last && want_debug) ? &dummy : nullptr);
+      for (Entry &e : v.cells) {
+        mechanics_update(e, step, (last && want_debug) ? &dummy : nullptr);
+        if (cyc.on) {
+          react(e);
+          cycle_update(e);
+        }
+      }
+  }
+
+  // NeighborSensing::react_to_neighbors + clear_accumulator (bacterial_rods/src/
+  // main.rs:66-78): rate * (K - n) / K, at least 0, for n > 0 neighbours, else the base
+  // rate.  f64::max(x, 0.0) is written x > 0 ? x : 0 (it returns 0 for NaN as Rust's does;
+  // the two may differ only in the sign of a zero rate, which adds nothing to the length).
+  void react(Entry &e) const {
+    const uint32_t n = e.a.nsense;
+    if (n > 0) {
+      const double v = cyc.growth * (cyc.sat - (double)n) / cyc.sat;
+      e.c.grate = (v > 0.0) ? v : 0.0;
+    } else {
+      e.c.grate = cyc.growth;
+    }
+    e.a.nsense = 0;
+  }
+
+  // local_cycle_update (chili/update_cycle.rs:111-131) with the agent's Cycle::update_cycle
+  // (bacterial_rods/src/main.rs:87-98): grow, and divide past the threshold length.
+  void cycle_update(Entry &e) const {
+    e.c.slen = e.c.slen + e.c.grate * prm.dt;
+    if (e.c.slen > cyc.div_len) e.a.divide = true;
+  }
+
+  static uint64_t division_id(uint64_t plain, uint64_t counter) {
+    return OR_ID_DIVISION | (plain << 32) | (counter & 0xffffffffull);
+  }
+
+  // RodMechanics::divide (bacterial_rods.rs:586-663): c1 keeps the first vertex and c2 the
+  // last; both get div_factor * spring_length; the vertices are re-spread along the old
+  // polyline.  Float sums start at -0.0 as Rust's Sum for f64 does.  Returns false for a
+  // DivisionError (no segment index satisfies the search, or the index leaves the range).
+  bool divide(Cell &c1, Cell &c2) const {
+    if constexpr (NV < 2) {
+      return false;
+    } else {
+      const double two = 1.0 + 1.0, one_half = 1.0 / two;
+      const double radius = prm.radius;
+      double pos[NC];
+      std::memcpy(pos, c1.pos, sizeof(pos));
+      c2 = c1;
+      const double div_factor = one_half - radius / ((double)NV * c1.slen);
+      const double nsl = div_factor * c1.slen;
+      c1.slen = nsl;
+      c2.slen = nsl;
+      double seg[NV - 1];
+      for (int q = 0; q + 1 < NV; ++q) {
+        double d[D];
+        for (int c = 0; c < D; ++c) d[c] = pos[q * D + c] - pos[(q + 1) * D + c];
+        double n2 = d[0] * d[0];
+        for (int c = 1; c < D; ++c) n2 = n2 + d[c] * d[c];
+        seg[q] = std::sqrt(n2);
+      }
+      double total = -0.0;
+      for (int q = 0; q + 1 < NV; ++q) total = total + seg[q];
+      const double seglen = (total - two * radius) / (double)(NV - 1) / two;
+      for (int nvx = 0; nvx < NV; ++nvx) {
+        const double target = (double)nvx * seglen;
+        int k = -1;
+        double pk = 0.0, acc = -0.0;
+        for (int n = 0; n < NV - 1; ++n) {  // sum of the first n segments
+          if (acc <= target) {
+            k = n;
+            pk = acc;
+          }
+          acc = acc + seg[n];
+        }
+        if (k < 0) return false;
+        const double q = (target - pk) / seg[k];
+        for (int c = 0; c < D; ++c)
+          c1.pos[nvx * D + c] = pos[k * D + c] * (1.0 - q) + pos[(k + 1) * D + c] * q;
+        int m = -1;
+        double rm = 0.0;
+        acc = -0.0;
+        for (int n = 0; n < NV; ++n) {  // sum of the last n segments, last first
+          if (acc <= target) {
+            m = n;
+            rm = acc;
+          }
+          if (n < NV - 1) acc = acc + seg[NV - 2 - n];
+        }
+        if (m < 0 || NV - m - 2 < 0) return false;
+        const double p = (target - rm) / seg[NV - m - 2];
+        for (int c = 0; c < D; ++c)
+          c2.pos[(NV - nvx - 1) * D + c] =
+              pos[(NV - m - 1) * D + c] * (1.0 - p) + pos[(NV - m - 2) * D + c] * p;
+      }
+      return true;
+    }
+  }
+
+  // SubDomainBox::update_cell_cycle_4 -> Voxel::update_cell_cycle_4 (chili/update_cycle.rs:
+  // 10-69): per voxel, dividing agents in storage order get the identifier Division(voxel,
+  // ++counter) and their daughters are collected; the daughters are appended to the voxel
+  // with Division(voxel, ++counter) each and a fresh AuxStorage (no solver history).
+  void cycle4(int s) {
+    Box &b = boxes[s];
+    for (Voxel &v : b.voxels) {
+      std::vector<Entry> born;
+      for (Entry &e : v.cells) {
+        if (!e.a.divide) continue;
+        e.a.divide = false;
+        Cell c2;
+        const uint64_t old = e.c.id;
+        if (!divide(e.c, c2)) {
+          set_error(b, OR_ECALC, (int64_t)old);
+          return;
+        }
+        v.id_counter += 1;
+        e.c.id = division_id(v.plain, v.id_counter);
+        e.c.parent = old;
+        Entry ne;
+        ne.c = c2;
+        ne.c.parent = old;
+        zero(ne.a.force);
+        born.push_back(ne);
+      }
+      for (Entry &ne : born) {
+        v.id_counter += 1;
+        ne.c.id = division_id(v.plain, v.id_counter);
+        v.cells.push_back(ne);
+      }
+    }
   }
 
   // SubDomainMechanics::apply_boundary (cartesian_cuboid_n.rs:594-631; rods:
@@ -884,6 +1047,8 @@ struct Sim {
       c.id = (uint64_t)i;
       std::memcpy(c.pos, pos + i * NC, sizeof(c.pos));
       std::memcpy(c.vel, vel + i * NC, sizeof(c.vel));
+      c.slen = slen_in ? slen_in[i] : prm.spring_length;
+      c.grate = cyc.growth;
       double kp[D];
       key_point(c, kp);
       uint64_t p;
@@ -918,6 +1083,7 @@ struct Sim {
         e.c = c;
         zero(e.a.force);
         v->cells.push_back(e);
+        v->id_counter += 1;  // insert_initial_cells (datastructures.rs:296)
       }
     }
     mb_pos.assign(S, std::vector<std::vector<PosInfo>>(S));
@@ -937,6 +1103,7 @@ struct Sim {
       if (bar) bar->arrive_and_wait();
       if (b.error == OR_OK) step3(s);
       if (b.error == OR_OK) update_local(s, last, step_base + step - 1);
+      if (b.error == OR_OK && cyc.on) cycle4(s);
       if (b.error == OR_OK) boundary(s);
       if (b.error == OR_OK) sort1(s);
       if (bar) bar->arrive_and_wait();
@@ -1014,6 +1181,29 @@ struct Sim {
     if (dbg && dbg->force_last)
       std::memcpy(dbg->force_last, dbg_force.data(), sizeof(double) * dbg_force.size());
   }
+
+  // Storage-order export of a cell-cycle run; false when the output arrays are too short.
+  bool export_cycle(or_cycle &o) {
+    int64_t n = 0;
+    for (Box &b : boxes)
+      for (Voxel &v : b.voxels) n += (int64_t)v.cells.size();
+    o.n_out = n;
+    if (n > o.cap_out) return false;
+    int64_t k = 0;
+    for (Box &b : boxes)
+      for (Voxel &v : b.voxels)
+        for (Entry &e : v.cells) {
+          if (o.ids_out) o.ids_out[k] = e.c.id;
+          if (o.parent_out) o.parent_out[k] = e.c.parent;
+          if (o.pos_out) std::memcpy(o.pos_out + k * NC, e.c.pos, sizeof(e.c.pos));
+          if (o.vel_out) std::memcpy(o.vel_out + k * NC, e.c.vel, sizeof(e.c.vel));
+          if (o.spring_length_out) o.spring_length_out[k] = e.c.slen;
+          if (o.growth_rate_out) o.growth_rate_out[k] = e.c.grate;
+          if (o.voxel_out) o.voxel_out[k] = (uint32_t)v.plain;
+          ++k;
+        }
+    return true;
+  }
 };
 
 template <int D, int NV>
@@ -1036,9 +1226,56 @@ int32_t run_t(const or_config &cfg, const Domain &dom, int64_t n, double *pos, d
   return r;
 }
 
+template <int D, int NV>
+int32_t run_cycle_t(const or_config &cfg, const Domain &dom, or_cycle &cy, int64_t n,
+                    const double *pos, const double *vel, int64_t n_steps) {
+  auto sim = std::make_unique<Sim<D, NV>>();
+  sim->dom = dom;
+  sim->prm = Params{cfg.mass,      cfg.damping,   cfg.spring_tension, cfg.rigidity,
+                    cfg.spring_length, cfg.radius, cfg.stiffness, cfg.cutoff,
+                    cfg.strength,  cfg.dt,        cfg.solver_order, cfg.kind,
+                    cfg.diffusion, cfg.kb_temperature, cfg.rng_seed};
+  sim->cap = cfg.solver_order - 1;
+  sim->cyc.on = true;
+  sim->cyc.growth = cy.growth_rate;
+  sim->cyc.div_len = cy.division_length;
+  sim->cyc.sense = cy.sense_range;
+  sim->cyc.sat = cy.sense_saturation;
+  sim->slen_in = cy.spring_length_in;
+  int r = sim->setup(cfg, n, pos, vel);
+  if (r) return r;
+  or_debug dbg;
+  std::memset(&dbg, 0, sizeof(dbg));
+  r = sim->run(n_steps, &dbg);
+  cy.error_agent = dbg.error_agent;
+  cy.error_step = dbg.error_step;
+  if (!sim->export_cycle(cy) && r == OR_OK) r = OR_EINVAL;
+  return r;
+}
+
 }  // namespace oracle_impl
 
 using namespace oracle_impl;
+
+int32_t oracle_cycle_rods2(const or_config &cfg, const Domain &dom, or_cycle &cy, int64_t n,
+                           const double *pos, const double *vel, int64_t n_steps);
+int32_t oracle_cycle_rods3(const or_config &cfg, const Domain &dom, or_cycle &cy, int64_t n,
+                           const double *pos, const double *vel, int64_t n_steps);
+
+#define ORACLE_CYCLE_DEF(NAME, D)                                                         \
+  int32_t NAME(const or_config &cfg, const Domain &dom, or_cycle &cy, int64_t n,           \
+               const double *pos, const double *vel, int64_t n_steps) {                   \
+    switch (cfg.n_vertices) {                                                             \
+      case 2: return run_cycle_t<D, 2>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      case 3: return run_cycle_t<D, 3>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      case 4: return run_cycle_t<D, 4>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      case 5: return run_cycle_t<D, 5>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      case 6: return run_cycle_t<D, 6>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      case 7: return run_cycle_t<D, 7>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      case 8: return run_cycle_t<D, 8>(cfg, dom, cy, n, pos, vel, n_steps);               \
+      default: return OR_EINVAL;                                                          \
+    }                                                                                     \
+  }
 
 // The rod instantiations are compiled in separate units (ORACLE_PART 2 and 3) so the
 // oracle builds in parallel.
@@ -1064,9 +1301,11 @@ int32_t oracle_run_rods3(const or_config &cfg, const Domain &dom, int64_t n, dou
 
 #if ORACLE_PART == 2 || ORACLE_PART == -1
 ORACLE_RODS_DEF(oracle_run_rods2, 2)
+ORACLE_CYCLE_DEF(oracle_cycle_rods2, 2)
 #endif
 #if ORACLE_PART == 3 || ORACLE_PART == -1
 ORACLE_RODS_DEF(oracle_run_rods3, 3)
+ORACLE_CYCLE_DEF(oracle_cycle_rods3, 3)
 #endif
 
 #if ORACLE_PART == 0 || ORACLE_PART == -1
@@ -1094,6 +1333,22 @@ int32_t or_run(const or_config *cfg, int64_t n_agents, double *pos, double *vel,
     return oracle_run_rods3(*cfg, dom, n_agents, pos, vel, n_steps, dbg, elapsed_s);
   }
   return OR_EINVAL;
+}
+
+int32_t or_run_cycle(const or_config *cfg, or_cycle *cyc, int64_t n_agents,
+                     const double *pos, const double *vel, int64_t n_steps) {
+  if (!cfg || !cyc || n_agents < 0 || n_steps < 0 || (n_agents > 0 && (!pos || !vel)))
+    return OR_EINVAL;
+  if (cfg->kind != OR_KIND_ROD || cfg->solver_order < 1 || cfg->solver_order > 3 ||
+      cfg->n_subdomains < 1 || !(cyc->sense_saturation != 0.0))
+    return OR_EINVAL;
+  cyc->n_out = 0;
+  cyc->error_agent = cyc->error_step = -1;
+  Domain dom;
+  int r = make_domain(*cfg, dom);
+  if (r) return r;
+  if (cfg->dim == 2) return oracle_cycle_rods2(*cfg, dom, *cyc, n_agents, pos, vel, n_steps);
+  return oracle_cycle_rods3(*cfg, dom, *cyc, n_agents, pos, vel, n_steps);
 }
 
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {

@@ -77,6 +77,34 @@ typedef struct or_debug {
 int32_t or_run(const or_config *cfg, int64_t n_agents, double *pos, double *vel,
                int64_t n_steps, or_debug *dbg, double *elapsed_s);
 
+/* Cell cycle of the bacterial-rods agent (cellular_raza-examples/bacterial_rods/src/
+ * main.rs:48-112): NeighborSensing counts vertex pairs of an agent and every partner it
+ * meets that are closer than sense_range; react_to_neighbors sets the growth rate to
+ * growth_rate * (sense_saturation - n) / sense_saturation (at least 0) when n > 0, else
+ * growth_rate; Cycle::update_cycle grows the spring length by rate * dt and divides past
+ * division_length with RodMechanics::divide (bacterial_rods.rs:586-663).  Daughters and
+ * dividing parents get CellIdentifier::Division(voxel, counter), encoded as
+ * OR_ID_DIVISION | voxel << 32 | counter; the parent of an initial agent is OR_NO_PARENT. */
+#define OR_ID_DIVISION (1ull << 63)
+#define OR_NO_PARENT (~0ull)
+
+typedef struct or_cycle {
+  double growth_rate, division_length, sense_range, sense_saturation;
+  const double *spring_length_in; /* [n] initial spring lengths (NULL: cfg->spring_length) */
+  int64_t cap_out;                /* room in the output arrays (agents) */
+  int64_t n_out;                  /* agents after the run (also set when cap_out is short) */
+  uint64_t *ids_out, *parent_out; /* [cap_out], chili's storage order */
+  double *pos_out, *vel_out;      /* [cap_out][nv][dim] */
+  double *spring_length_out, *growth_rate_out; /* [cap_out] */
+  uint32_t *voxel_out;            /* [cap_out] */
+  int64_t error_agent, error_step;
+} or_cycle;
+
+/* Runs n_steps chili steps of rods with the cell cycle (aspects Mechanics, Interaction,
+ * Cycle, NeighborSensing).  Outputs in storage order; OR_EINVAL when cap_out is short. */
+int32_t or_run_cycle(const or_config *cfg, or_cycle *cyc, int64_t n_agents,
+                     const double *pos, const double *vel, int64_t n_steps);
+
 /* The random stream of the stochastic mechanics (shared definition with the GPU path):
  * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the standard normals drawn from it
  * for agent `id` at pack step `step`: n values, two per Philox block (Box-Muller). */

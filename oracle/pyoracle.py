@@ -82,6 +82,31 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+ID_DIVISION = 1 << 63
+NO_PARENT = (1 << 64) - 1
+
+
+class OrCycle(C.Structure):
+    _fields_ = [
+        ("growth_rate", C.c_double),
+        ("division_length", C.c_double),
+        ("sense_range", C.c_double),
+        ("sense_saturation", C.c_double),
+        ("spring_length_in", C.POINTER(C.c_double)),
+        ("cap_out", C.c_int64),
+        ("n_out", C.c_int64),
+        ("ids_out", C.POINTER(C.c_uint64)),
+        ("parent_out", C.POINTER(C.c_uint64)),
+        ("pos_out", C.POINTER(C.c_double)),
+        ("vel_out", C.POINTER(C.c_double)),
+        ("spring_length_out", C.POINTER(C.c_double)),
+        ("growth_rate_out", C.POINTER(C.c_double)),
+        ("voxel_out", C.POINTER(C.c_uint32)),
+        ("error_agent", C.c_int64),
+        ("error_step", C.c_int64),
+    ]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -92,6 +117,9 @@ def lib():
         L.or_run.argtypes = [C.POINTER(OrConfig), C.c_int64, dp, dp, C.c_int64,
                              C.POINTER(OrDebug), dp]
         L.or_run.restype = C.c_int32
+        L.or_run_cycle.argtypes = [C.POINTER(OrConfig), C.POINTER(OrCycle), C.c_int64, dp, dp,
+                                   C.c_int64]
+        L.or_run_cycle.restype = C.c_int32
         L.or_domain_voxels.argtypes = [C.POINTER(OrConfig), C.POINTER(C.c_int64), dp]
         L.or_get_decomp_res.argtypes = [C.c_uint64, C.c_uint64] + [C.POINTER(C.c_uint64)] * 3
         L.or_subdomain_map.argtypes = [C.POINTER(OrConfig), C.POINTER(C.c_uint32)]
@@ -188,6 +216,48 @@ def run(model, pos, vel, n_steps, debug=False):
         raise OracleError(rc, dbg.error_agent, dbg.error_step)
     out["pos"], out["vel"], out["elapsed_s"] = pos, vel, el.value
     return out
+
+
+def run_cycle(model, pos, vel, n_steps, spring_length=None):
+    """Run n_steps chili steps of rods with the bacterial-rods cell cycle (growth limited by
+    neighbour sensing, division past model.division_length).  Returns the agents in chili's
+    storage order: ids, parent, pos, vel, spring_length, growth_rate, voxel."""
+    L = lib()
+    cfg = make_config(model)
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    vel = np.ascontiguousarray(vel, dtype=np.float64)
+    n = pos.shape[0]
+    cy = OrCycle()
+    cy.growth_rate = model.growth_rate
+    cy.division_length = model.division_length
+    cy.sense_range = model.sense_range
+    cy.sense_saturation = model.sense_saturation
+    sl = None
+    if spring_length is not None:
+        sl = np.ascontiguousarray(spring_length, dtype=np.float64)
+        cy.spring_length_in = _dp(sl)
+    cap = max(2 * n, 64)
+    while True:
+        out = {"ids": np.zeros(cap, np.uint64), "parent": np.zeros(cap, np.uint64),
+               "pos": np.zeros((cap,) + pos.shape[1:]), "vel": np.zeros((cap,) + pos.shape[1:]),
+               "spring_length": np.zeros(cap), "growth_rate": np.zeros(cap),
+               "voxel": np.zeros(cap, np.uint32)}
+        cy.cap_out = cap
+        cy.ids_out = out["ids"].ctypes.data_as(C.POINTER(C.c_uint64))
+        cy.parent_out = out["parent"].ctypes.data_as(C.POINTER(C.c_uint64))
+        cy.pos_out = _dp(out["pos"])
+        cy.vel_out = _dp(out["vel"])
+        cy.spring_length_out = _dp(out["spring_length"])
+        cy.growth_rate_out = _dp(out["growth_rate"])
+        cy.voxel_out = out["voxel"].ctypes.data_as(C.POINTER(C.c_uint32))
+        rc = L.or_run_cycle(C.byref(cfg), C.byref(cy), n, _dp(pos), _dp(vel), int(n_steps))
+        if rc == EINVAL and cy.n_out > cap:
+            cap = int(cy.n_out)
+            continue
+        if rc != OK:
+            raise OracleError(rc, cy.error_agent, cy.error_step)
+        m = int(cy.n_out)
+        return {k: v[:m] for k, v in out.items()}
 
 
 def philox4x32_10(ctr, key):
