@@ -37,7 +37,8 @@ def check(got, ref):
     assert rel(got["growth_rate"], ref["growth_rate"]) <= TOL
 
 
-@pytest.mark.parametrize("dim,n_sub,order", [(2, 1, 1), (2, 4, 1), (3, 2, 1), (2, 3, 2)])
+@pytest.mark.parametrize("dim,n_sub,order", [(2, 1, 1), (2, 4, 1), (3, 2, 1), (2, 3, 2),
+                                             (3, 2, 3)])
 def test_colony_matches_oracle(gpu, oracle, dim, n_sub, order):
     w = W.rod_colony(n=150, side=300.0 if dim == 2 else 120.0, seed=3, dim=dim,
                      n_subdomains=n_sub, solver_order=order)
