@@ -76,6 +76,29 @@ def test_colony_grows_and_ids_are_unique(oracle, dim, n_sub):
     n = len(out["ids"])
     assert n > 120
     assert len(set(out["ids"].tolist())) == n
+    n_vox = int(np.prod(oracle.domain_voxels(w.model)[0][:dim]))
+
+    def names_a_voxel(x):
+        return (x >> np.uint64(63) == 1) & ((x >> np.uint64(32)) & np.uint64(0x7fffffff) < n_vox)
+
     div = out["ids"] >> np.uint64(63) == 1
-    assert np.all(out["parent"][div] != np.uint64((1 << 64) - 1))
+    assert np.all(names_a_voxel(out["ids"][div]))
+    assert np.all(out["ids"][~div] < 120)
+    par = out["parent"][div]
+    assert np.all((par < 120) | names_a_voxel(par))
+    assert np.all(out["parent"][~div] == np.uint64((1 << 64) - 1))
     assert np.all(out["spring_length"] > 0.0)
+
+
+@pytest.mark.parametrize("order", [1, 3])
+def test_cycle_without_growth_equals_plain_rods(oracle, order):
+    """Growth 0 and every spring length at the model's: no division, so the cycle run moves
+    the rods exactly as the plain rod step does (same storage order, same bits)."""
+    w = W.rod_colony(n=120, seed=8, growth_rate=0.0, n_subdomains=3, solver_order=order)
+    cyc = oracle.run_cycle(w.model, w.pos, w.vel, 150)
+    plain = oracle.run(w.model.replace(cycle=False), w.pos, w.vel, 150, debug=True)
+    assert np.array_equal(cyc["ids"], plain["order"])
+    ids = cyc["ids"].astype(np.int64)
+    assert np.array_equal(cyc["pos"], plain["pos"][ids])
+    assert np.array_equal(cyc["vel"], plain["vel"][ids])
+    assert np.all(cyc["parent"] == np.uint64((1 << 64) - 1))
