@@ -349,6 +349,36 @@ def extra_ensemble(torch):
             "speedup": batched / sequential}
 
 
+def extra_cycle(n_rods=2000, steps=600):
+    """A growing colony of the bacterial-rods agent (cell cycle: neighbour sensing, growth
+    limited by the neighbour count, division), 2,000 rods at the density of
+    workloads.rod_colony's 150-rod colony, 600 steps.  Cycle handles run one step per launch
+    sequence (each step reads its division count back); the wall time around the calls
+    covers that.  Agent-steps sum the agent count of every step."""
+    import math
+    import time
+
+    from cellular_raza_gb300 import engine as E
+    from cellular_raza_gb300 import workloads as W
+
+    w = W.rod_colony(n=n_rods, side=300.0 * math.sqrt(n_rods / 150.0), seed=2024,
+                     n_subdomains=N_SUBDOMAINS)
+    with E.Simulation.single(w.model, 8 * w.n) as sim:
+        sim.upload(w.pos, w.vel)
+        sim.set_spring_lengths(w.spring_length)
+        agent_steps = 0
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            agent_steps += sim.n_agents
+            sim.step(1)
+        dt = time.perf_counter() - t0
+        n_end = sim.n_agents
+    return {"workload": "rod_colony", "agents_start": w.n, "agents_end": n_end,
+            "steps": steps, "dim": w.model.dim, "vertices_per_agent": w.model.n_vertices,
+            "agent_steps_per_s": agent_steps / dt, "ms_per_step": dt * 1e3 / steps,
+            "timing": "wall clock around the crg_step calls"}
+
+
 def extra_served(n_requests=160, rate_hz=8.0):
     """Poisson stream of simulation requests (N log-uniform [128, 262144], steps uniform
     [100, 2000], 2D/3D and FP64/mixed 50/50) through the request server (continuous batching,
@@ -520,7 +550,8 @@ def crg_arm(args):
     if world == 1 and not args.no_extras:
         for name, fn in (("mixed_large", lambda: extra_mixed_large(torch)),
                          ("ensemble", lambda: extra_ensemble(torch)),
-                         ("served", extra_served)):
+                         ("served", extra_served),
+                         ("cell_cycle", extra_cycle)):
             try:
                 extras[name] = fn()
             except Exception as e:  # reported, not fatal for the headline line
@@ -546,6 +577,7 @@ def crg_arm(args):
             "mixed_large": extras.get("mixed_large"),
             "ensemble": extras.get("ensemble"),
             "served": extras.get("served"),
+            "cell_cycle": extras.get("cell_cycle"),
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
