@@ -535,7 +535,10 @@ def crg_arm(args):
                 "force_stage_ms_per_step": force_ms, "force_stage_flop_per_step": flops,
                 "force_stage_tflops": flops / (force_ms * 1e-3) / 1e12,
                 "sort_ms_per_step": sort_ms}
-    # the sort kernels are HBM-bound: algorithmic bytes per step
+    # the sort kernels are HBM-bound.  Algorithmic bytes per agent and step: pos and vel
+    # read and written (2 x 2 x 8 x nc), ids read and written (2 x 8), old and new key,
+    # count and slot (4 x 4), FP32 offsets written (4 x nc), the 64-bit slot entry written,
+    # sorted and read (8 x 3)
     nc = w.model.nc
     sort_bytes = w.n * (2 * 2 * 8 * nc + 2 * 8 + 4 * 4 + 4 * nc + 8 * 3)
     hbm = peaks.get("hbm_gbs")
