@@ -41,7 +41,7 @@ extern "C" {
 #define CRG_ENOMEM 6      /* device allocation failed / admission budget exceeded */
 #define CRG_ECUDA 7       /* CUDA runtime error */
 #define CRG_ETIMEDOUT 8   /* bounded device-side wait expired */
-#define CRG_ENOTSUP 9     /* feature outside what this build supports */
+#define CRG_ENOTSUP 9     /* feature outside what this library supports */
 #define CRG_EINTERNAL 10  /* a device-side invariant check failed; the access was skipped
                              (crg_last_error: agent = index, step = check site) */
 
