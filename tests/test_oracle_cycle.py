@@ -102,3 +102,31 @@ def test_cycle_without_growth_equals_plain_rods(oracle, order):
     assert np.array_equal(cyc["pos"], plain["pos"][ids])
     assert np.array_equal(cyc["vel"], plain["vel"][ids])
     assert np.all(cyc["parent"] == np.uint64((1 << 64) - 1))
+
+
+def test_two_divisions_in_one_voxel(oracle):
+    """Two rods of one voxel (plain index 1, two initial agents: counter 2) divide in the same
+    step.  chili renames the parents first, in storage order (Division(1, 3), (1, 4)), then
+    appends the daughters (Division(1, 5), (1, 6)) in the same order
+    (chili/update_cycle.rs:30-64)."""
+    m = colony_model()
+    x = 10.0 + 6.5 * np.arange(5)
+    a = np.stack([x, np.full(5, 55.0)], axis=1)
+    b = np.stack([x, np.full(5, 90.0)], axis=1)
+    pos = np.stack([a, b])
+    out = oracle.run_cycle(m, pos, np.zeros_like(pos), 1, spring_length=np.array([6.5, 6.5]))
+    v = 1 << 32
+    assert list(out["ids"]) == [DIV | v | 3, DIV | v | 4, DIV | v | 5, DIV | v | 6]
+    assert list(out["parent"]) == [0, 1, 0, 1]
+    assert list(out["voxel"]) == [1, 1, 1, 1]
+
+
+def test_division_error_for_a_rod_shorter_than_two_radii(oracle):
+    """RodMechanics::divide finds no segment when (length - 2 R) < 0: a DivisionError, which
+    ends the run with an error (CalcError here)."""
+    m = colony_model(division_length=1.0)
+    x = 10.0 + 1.2 * np.arange(5)  # length 4.8 < 2 R = 6
+    pos = np.stack([x, np.full(5, 50.0)], axis=1)[None]
+    with pytest.raises(oracle.OracleError) as e:
+        oracle.run_cycle(m, pos, np.zeros_like(pos), 1, spring_length=np.array([1.2]))
+    assert e.value.code == oracle.ECALC
