@@ -26,7 +26,7 @@ NO_PARENT = (1 << 64) - 1
 
 # Every symbol include/crg.h declares (checked by tests/test_abi.py).
 EXPORTED = [
-    "crg_create", "crg_create_batch", "crg_upload", "crg_step", "crg_download",
+    "crg_create", "crg_create_batch", "crg_upload", "crg_step", "crg_forces", "crg_download",
     "crg_agent_count", "crg_last_error", "crg_destroy", "crg_strerror", "crg_set_option",
     "crg_debug_forces", "crg_debug_neighbor_stats", "crg_profile", "crg_measure_fma_peaks",
     "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc", "crg_autotune",
@@ -119,6 +119,7 @@ def load(build_if_missing: bool = True):
                                    C.POINTER(vp)]
     L.crg_upload.argtypes = [vp, C.c_int64, i64p, dp, dp, u64p]
     L.crg_step.argtypes = [vp, C.c_int64]
+    L.crg_forces.argtypes = [vp, C.c_int64, dp, dp]
     L.crg_download.argtypes = [vp, dp, dp, u64p, u32p]
     L.crg_agent_count.argtypes = [vp, i64p]
     L.crg_last_error.argtypes = [vp, i64p, i64p]

@@ -62,6 +62,7 @@ struct crg_ctx {
   uint32_t *srank = nullptr;
   uint32_t *h_ndiv = nullptr;  // pinned
   double *frc = nullptr;
+  double *fbuf = nullptr;  // crg_forces: the interaction force of every slot
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
   uint32_t snap_agents = 0;
@@ -295,7 +296,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
+                  c->step_ctr, c->dbg_force, c->frc, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
                   c->staging, c->snap, c->slen, c->nslen, c->grate, c->ngrate, c->parent,
                   c->nparent, c->vctr, c->nsense, c->dflag, c->dpre, c->dbsum, c->srank};
   for (void *p : ptrs)
@@ -625,8 +626,9 @@ void invalidate_graph(crg_ctx *c) {
 // Cell-cycle handles run one step at a time: divisions change the agent count that every
 // launch is sized by.  Per step: neighbour counts (k_rods_sense), forces and the update
 // (growth, division flags), the scan of the flags, a read of the division count, the
-// divisions (k_rods_divide) and the sort of the grown list.  A step whose divisions would
-// exceed the handle's capacity stops before dividing with CRG_ENOMEM.
+// divisions (k_rods_divide), the voxel counters and the sort of the grown list.  A step
+// whose divisions would exceed the handle's capacity stops before dividing with CRG_ENOMEM;
+// a step that fails stops before its sort, so the handle keeps the previous step's state.
 int32_t step_cycle(crg_ctx *c, int64_t n_steps) {
   cudaStream_t st = c->stream;
   int64_t done = 0;
@@ -650,7 +652,12 @@ int32_t step_cycle(crg_ctx *c, int64_t n_steps) {
       c->err_step = c->steps_done + done + 1;
       break;
     }
-    if (n_div) crg::launch_rods_divide(c->dim, c->nv, P, n_div, st);
+    if (n_div) {
+      crg::launch_rods_divide(c->dim, c->nv, P, n_div, st);
+      // a DivisionError stops the step before anything of it is committed
+      if (read_status(c) != CRG_OK) break;
+      crg::launch_cycle_counters(P, st);
+    }
     SortArgs A = sort_args(c, 0);
     A.n_agents = n + n_div;
     A.srank = n_div ? c->srank : nullptr;
@@ -721,9 +728,10 @@ int32_t crg_destroy(crg_ctx *c) {
   return CRG_OK;
 }
 
-int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *pos,
-                   const double *vel, const uint64_t *ids) {
-  if (!c || n < 0 || (n > 0 && (!pos || !vel))) return CRG_EINVAL;
+// crg_upload; vel = nullptr gives every agent zero velocity.
+static int32_t upload_impl(crg_ctx *c, int64_t n, const int64_t *counts, const double *pos,
+                           const double *vel, const uint64_t *ids) {
+  if (!c || n < 0 || (n > 0 && !pos)) return CRG_EINVAL;
   std::vector<int64_t> cnt(c->n_sims);
   if (c->n_sims == 1) {
     cnt[0] = counts ? counts[0] : n;
@@ -761,8 +769,12 @@ int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *p
   if (n > 0) {
     CUDA_TRY(cudaMemcpyAsync(c->staging, pos, bytes, cudaMemcpyHostToDevice, st));
     crg::launch_transpose_in(c->staging, c->npos, (uint32_t)n, c->nc, c->cap, st);
-    CUDA_TRY(cudaMemcpyAsync(c->staging, vel, bytes, cudaMemcpyHostToDevice, st));
-    crg::launch_transpose_in(c->staging, c->nvel, (uint32_t)n, c->nc, c->cap, st);
+    if (vel) {
+      CUDA_TRY(cudaMemcpyAsync(c->staging, vel, bytes, cudaMemcpyHostToDevice, st));
+      crg::launch_transpose_in(c->staging, c->nvel, (uint32_t)n, c->nc, c->cap, st);
+    } else {
+      CUDA_TRY(cudaMemsetAsync(c->nvel, 0, sizeof(double) * (size_t)c->cap * c->nc, st));
+    }
     if (ids) {
       CUDA_TRY(cudaMemcpyAsync(c->nid, ids, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
     } else {
@@ -797,6 +809,47 @@ int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *p
     return r;
   }
   return CRG_OK;
+}
+
+int32_t crg_upload(crg_ctx *c, int64_t n, const int64_t *counts, const double *pos,
+                   const double *vel, const uint64_t *ids) {
+  if (n > 0 && !vel) return CRG_EINVAL;
+  return upload_impl(c, n, counts, pos, vel, ids);
+}
+
+int32_t crg_forces(crg_ctx *c, int64_t n, const double *pos, double *force) {
+  if (!c || n < 0 || (n > 0 && (!pos || !force))) return CRG_EINVAL;
+  if (c->n_sims != 1 || c->cycle) return CRG_ENOTSUP;
+  int32_t r = upload_impl(c, n, nullptr, pos, nullptr, nullptr);
+  if (r != CRG_OK || n == 0) return r;
+  if (!c->fbuf && (r = dalloc(&c->fbuf, (size_t)c->cap * c->nc)) != CRG_OK) return r;
+  cudaStream_t st = c->stream;
+  // One force evaluation of the uploaded cell list.  The kernels also compute the state a
+  // step would reach from these forces; it stays in the "next" arrays and is dropped, and a
+  // BoundaryError raised by it concerns a step that is not taken.
+  crg::PackArgs P = pack_args(c);
+  P.dbg_force = c->fbuf;
+  if (c->kind == CRG_KIND_SPHERE)
+    crg::launch_spheres_step(c->dim, c->precision, P, c->block, st);
+  else
+    crg::launch_rods_step(c->dim, c->nv, c->precision, P, c->block, st);
+  CUDA_TRY(cudaGetLastError());
+  r = read_status(c);
+  if (r == CRG_EBOUNDARY) {
+    c->err_code = CRG_OK;
+    c->err_agent = c->err_step = -1;
+    c->err_sim = -1;
+    r = CRG_OK;
+  }
+  if (r != CRG_OK) return r;
+  CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, st));
+  // the histogram of the dropped next keys
+  CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), st));
+  crg::launch_unsort_out(c->fbuf, c->tmp, c->staging, (uint32_t)n, c->nc, c->cap, c->status, st);
+  CUDA_TRY(cudaMemcpyAsync(force, c->staging, sizeof(double) * (size_t)n * c->nc,
+                           cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaGetLastError());
+  return read_status(c);
 }
 
 int32_t crg_step(crg_ctx *c, int64_t n_steps) {
@@ -856,6 +909,11 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
   if (c->profile)
     for (auto &e : ev) cudaEventDestroy(e);
   c->steps_done += n_steps - std::max<int64_t>(left, 0);
+  // The failing step of a simulation is not committed and its later steps leave it frozen
+  // (sim_frozen, failed_sim): a single simulation holds the state after its last good step.
+  if (c->n_sims == 1 && c->err_code != CRG_OK && c->err_code != CRG_ECUDA &&
+      c->err_code != CRG_EINTERNAL && c->err_step >= 1)
+    c->steps_done = std::min(c->steps_done, c->err_step - 1);
   return c->err_code;
 }
 
@@ -1182,6 +1240,11 @@ int32_t crg_clear_error(crg_ctx *c, int32_t *sim) {
   c->err_agent = c->err_step = -1;
   c->err_sim = -1;
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, c->stream));
+  // a cell-cycle step stops before its sort, leaving the voxel histogram filled
+  CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), c->stream));
+  if (c->n_sims == 1)  // the frozen steps advanced the device counter past the kept state
+    CUDA_TRY(cudaMemcpyAsync(c->step_ctr, &c->steps_done, sizeof(int64_t),
+                             cudaMemcpyHostToDevice, c->stream));
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   return code;
 }

@@ -122,6 +122,18 @@ struct PackArgs {
   uint32_t *srank;          // [cap] position in chili's pre-sort order, daughters included
 };
 
+// Records e on st: as an external event node while st is being captured into a graph (so the
+// graph records it each time it runs), as a plain record otherwise (the external flag is for
+// capture only).
+inline void record_event(cudaEvent_t e, cudaStream_t st) {
+  if (!e) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+  else
+    cudaEventRecord(e, st);
+}
+
 // ---- IEEE FP64 helpers that are never contracted into fused multiply-adds ----------
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
@@ -253,7 +265,9 @@ __device__ __forceinline__ uint32_t sim_of_agent(const PackArgs &P, uint32_t i) 
 
 // status word: [0] code, [1] agent id lo, [2] agent id hi, [3] step (or check site),
 // [4] simulation index within the pack, [5] largest pass list a rod step asked for since
-// the status was last cleared (read by the host to size the pass list)
+// the status was last cleared (read by the host to size the pass list), [6] the failed
+// simulation as of the end of the previous step (0 none, s + 1 simulation s, -1 all), which
+// the force and update kernels read instead of [0] because [0] can change during them
 __device__ __forceinline__ void set_status(int32_t *status, int32_t code, uint64_t agent,
                                            int64_t step, int32_t sim = 0) {
   if (atomicCAS(&status[0], 0, code) == 0) {
@@ -262,6 +276,25 @@ __device__ __forceinline__ void set_status(int32_t *status, int32_t code, uint64
     status[3] = (int32_t)step;
     status[4] = sim;
   }
+}
+
+// A simulation is frozen (carried through a step unchanged) once its requested number of
+// steps is done or once one of its earlier steps failed: chili stops a simulation at its
+// first error (chili/errors.rs:73-122), so no later step may change its state.
+__device__ __forceinline__ bool sim_frozen(const PackArgs &P, const SimDev &S) {
+  const int32_t failed = P.status[6];
+  return *P.step_ctr >= S.stop_step || failed == -1 || failed == S.sim_index + 1;
+}
+
+// The simulation whose step failed in the force or update kernels (a code other than
+// CRG_EINTERNAL in status[0], its index in status[4]), or -1.  Read by the sort kernels that
+// follow those kernels: the failing step is not committed for that simulation, so the
+// handle keeps the state after the last step that succeeded.  Only invariant checks of the
+// sort kernels themselves write the status during a sort, and they write CRG_EINTERNAL
+// into a clear word only, so every sort kernel of a step reads the same answer.
+__device__ __forceinline__ int32_t failed_sim(const int32_t *status) {
+  const int32_t code = status[0];
+  return (code != 0 && code != CRG_EINTERNAL) ? status[4] : -1;
 }
 
 // A frozen simulation (its requested number of steps is done) is carried through the step

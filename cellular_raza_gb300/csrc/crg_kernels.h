@@ -80,6 +80,10 @@ void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int
                          cudaStream_t st);
 void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
                           cudaStream_t st);
+// Cell-list values [nc][cap] -> agent-major rows in the order of the upload that built the
+// cell list (through the insertion sort's slot table tmp).
+void launch_unsort_out(const double *src, const uint64_t *tmp, double *dst, uint32_t n, int nc,
+                       int64_t cap, int32_t *status, cudaStream_t st);
 
 // Force + integrator + boundary + next voxel key (+ histogram) for one step.
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st);
@@ -88,10 +92,11 @@ void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int blo
                       cudaStream_t st, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr);
 int prepare_rods(int dim, int nv);  // 0 on success
 // Cell cycle of rods: neighbour counts of this step (before the update kernel), and after
-// the update and the scan of its division flags, the divisions (n_div > 0) plus the voxel
-// counters.
+// the update and the scan of its division flags, the divisions (n_div > 0), then the voxel
+// counters (launched once the divisions are known to have succeeded).
 void launch_rods_sense(int dim, int nv, const PackArgs &P, cudaStream_t st);
 void launch_rods_divide(int dim, int nv, const PackArgs &P, uint32_t n_div, cudaStream_t st);
+void launch_cycle_counters(const PackArgs &P, cudaStream_t st);
 // Voxel counters from the first cell list; per-agent values from upload order to the cell
 // list through the upload sort's slot table (tmp).
 void launch_cycle_init(const PackArgs &P, cudaStream_t st);

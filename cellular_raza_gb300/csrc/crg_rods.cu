@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
   }
-  if (*P.step_ctr >= S.stop_step) {  // frozen simulation
+  if (sim_frozen(P, S)) {  // frozen simulation
     frozen_copy(P, i, key, NC);
     return;
   }
@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(W * 32) k_rods_packed(const PackArgs P) {
   }
   const int n_box = nb[0] * nb[1] * nb[2];
   // enumeration cursor
-  const bool frozen = valid && (*P.step_ctr >= S.stop_step);
+  const bool frozen = valid && sim_frozen(P, S);
   bool done = !valid || frozen;
   int stage = 0;  // 0: next voxel, 1: next candidate, 2: inside a pass
   int o_box = 0;
@@ -1326,7 +1326,7 @@ __global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
   }
   const int n_box = nb[0] * nb[1] * nb[2];
   // cursor
-  const bool frozen = valid && (*P.step_ctr >= S.stop_step);
+  const bool frozen = valid && sim_frozen(P, S);
   bool done = !valid || frozen;
   int o_box = 0;
   uint32_t b_next = 0, b_end = 0, cur_b = 0;
@@ -1448,7 +1448,6 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
   FoldScratch &F = *reinterpret_cast<FoldScratch *>(sAcc + NC * 32);
   const int lane = threadIdx.x;
   const int64_t cap = P.cap;
-  const int64_t step = *P.step_ctr;
   const float inf = __int_as_float(0x7f800000);
   // the rod of this lane and its candidate cursor
   bool have = false, drained = false;
@@ -1543,7 +1542,7 @@ __global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
           i = t;
           sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
           S = P.sims + sim;
-          if (step < S->stop_step) {  // frozen rods are copied by the update kernel
+          if (!sim_frozen(P, *S)) {  // frozen rods are copied by the update kernel
             uint32_t key = P.key[i];
             if (key - S->voxel_off >= S->n_vox) {
               invariant_failed(P.status, kSiteForceKey, i);
@@ -1635,7 +1634,7 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
   const int64_t cap = P.cap;
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
   const SimDev &S = P.sims[sim];
-  const bool live = valid && *P.step_ctr < S.stop_step;  // frozen rods have no passes
+  const bool live = valid && !sim_frozen(P, S);  // frozen rods have no passes
   uint32_t key = P.key[ii];
   if (key - S.voxel_off >= S.n_vox) {
     if (live) invariant_failed(P.status, kSiteForceKey, i);
@@ -1832,7 +1831,7 @@ __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
   const uint32_t i = (uint32_t)(g - (uint64_t)s * n);
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
   const SimDev &S = P.sims[sim];
-  if (*P.step_ctr >= S.stop_step) return;  // frozen: copied by k_rods_update
+  if (sim_frozen(P, S)) return;  // frozen: copied by k_rods_update
   const int64_t cap = P.cap;
   double x[3][D], c1[D], c2[D], f[D];
 #pragma unroll
@@ -1863,7 +1862,7 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   const SimDev &S = P.sims[sim];
   uint32_t key = P.key[i];
   if (key - S.voxel_off >= S.n_vox) key = S.voxel_off;  // recorded by the force kernel
-  if (*P.step_ctr >= S.stop_step) {
+  if (sim_frozen(P, S)) {
     frozen_copy(P, i, key, NC);
     return;
   }
@@ -2358,6 +2357,9 @@ void launch_rods_divide(int dim, int nv, const PackArgs &P, uint32_t n_div, cuda
     launch_cycle_d<3>(nv, P, true, st);
   else
     launch_cycle_d<2>(nv, P, true, st);
+}
+
+void launch_cycle_counters(const PackArgs &P, cudaStream_t st) {
   k_cycle_counters<<<(P.n_vox + 255) / 256, 256, 0, st>>>(P);
 }
 

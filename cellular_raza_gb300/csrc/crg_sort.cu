@@ -53,13 +53,39 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, uint32_t *total)
   return res;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const uint32_t *__restrict__ count,
-                                                              uint32_t n, uint32_t *bsum) {
+// Voxel range [lo, hi) of the simulation whose current step failed (failed_sim), empty if
+// none or if `status` is null (scans that are not a cell-list re-sort).  Its agents keep
+// their voxels, so its histogram entries are the voxel sizes of the current cell list.
+struct FailedRange {
+  uint32_t lo = 0, hi = 0;
+  __device__ FailedRange(const int32_t *status, const SimDev *sims) {
+    const int32_t f = status ? failed_sim(status) : -1;
+    if (f >= 0) {
+      lo = sims[f].voxel_off;
+      hi = lo + sims[f].n_vox;
+    }
+  }
+  __device__ bool has(uint32_t v) const { return v - lo < hi - lo; }
+};
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(uint32_t *__restrict__ count,
+                                                              uint32_t n, uint32_t *bsum,
+                                                              const int32_t *status,
+                                                              const SimDev *sims,
+                                                              const uint32_t *old_start) {
+  const FailedRange fr(status, sims);
   const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   uint32_t s = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k)
-    if (base + k < n) s += count[base + k];
+    if (base + k < n) {
+      uint32_t c = count[base + k];
+      if (fr.has(base + k)) {  // k_scan_final reads the corrected entry
+        c = old_start[base + k + 1] - old_start[base + k];
+        count[base + k] = c;
+      }
+      s += c;
+    }
   uint32_t tot;
   block_excl_scan(s, &tot);
   if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
@@ -107,15 +133,20 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(uint32_t *__restric
 
 // Whole scan in one block when the voxels fit one tile (small packs): start[j] = exclusive
 // prefix, count[j] = 0, start[n] = total.
+// The voxel sizes of a failed simulation are read from `start` before the first barrier of
+// the scan, and start is written after it.
 __global__ void __launch_bounds__(kScanThreads) k_scan_single(uint32_t *__restrict__ count,
-                                                              uint32_t n,
-                                                              uint32_t *__restrict__ start) {
+                                                              uint32_t n, uint32_t *start,
+                                                              const int32_t *status,
+                                                              const SimDev *sims) {
+  const FailedRange fr(status, sims);
   const uint32_t base = threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   uint32_t s = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     v[k] = (base + k < n) ? count[base + k] : 0u;
+    if (base + k < n && fr.has(base + k)) v[k] = start[base + k + 1] - start[base + k];
     s += v[k];
   }
   uint32_t tot;
@@ -134,12 +165,20 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_single(uint32_t *__restri
 // Slot assignment.  Sort key = class << 62 | rank << 31 | index, where the rank is the
 // agent's previous position (with divisions: its position in chili's pre-sort order, the
 // daughters of a voxel following its other agents) and the index locates its state.
+// The agents of a simulation whose step failed keep their voxel and their place (class 0,
+// rank = current position), so their slots are their current positions.
 __global__ void k_scatter(const SortArgs A) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= A.n_agents) return;
-  const uint32_t k = A.nkey[i];
+  const int32_t f = A.initial ? -1 : failed_sim(A.status);
+  const bool keep = f >= 0 && i - A.sims[f].agent_off < A.sims[f].n_agents;
+  uint32_t k = A.nkey[i];
+  if (keep) {
+    k = A.key[i];
+    A.nkey[i] = k;
+  }
   uint32_t cls = 0;
-  if (!A.initial) {
+  if (!A.initial && !keep) {
     const uint32_t old = A.key[i];
     if (k != old) {
       const uint32_t s = (A.n_sims == 1) ? 0u : A.sim_of_voxel ? A.sim_of_voxel[k] : 0u;
@@ -156,30 +195,97 @@ __global__ void k_scatter(const SortArgs A) {
     invariant_failed(A.status, kSiteScatterSlot, i);
     return;
   }
-  const uint32_t rank = A.srank ? A.srank[i] : i;
+  const uint32_t rank = (A.srank && !keep) ? A.srank[i] : i;
   A.tmp[slot] = ((uint64_t)cls << 62) | ((uint64_t)rank << 31) | (uint64_t)i;
 }
 
-// One thread per voxel: order the voxel's segment and reset its histogram counter.
-__global__ void k_segsort(const SortArgs A) {
-  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= A.n_vox) return;
-  const uint32_t s0 = A.start[v], s1 = A.start[v + 1];
-  A.count[v] = 0u;
-  if (s0 > s1 || s1 > A.n_agents) {
-    invariant_failed(A.status, kSiteSegRange, v);
-    return;
-  }
-  if (s1 - s0 < 2) return;
-  uint64_t *t = A.tmp;
-  for (uint32_t a = s0 + 1; a < s1; ++a) {
-    uint64_t x = t[a];
-    uint32_t b = a;
-    while (b > s0 && t[b - 1] > x) {
-      t[b] = t[b - 1];
-      --b;
+constexpr int kSegThreads = 256;  // voxels per block of k_segsort
+constexpr uint32_t kSegShort = 32;    // segments up to this length: one thread, insertion sort
+constexpr uint32_t kSegSmem = 2048;   // longer ones up to this length: in shared memory
+
+// Sorts t[0..m) ascending in place with all threads of the block (every thread calls it).
+// A bitonic network over the next power of two p >= m in the form whose compare-exchanges
+// all put the smaller key first: per merge size k, each element of the first half of a run
+// of k against its mirror in the second half, then half-cleaners at distances k/4 .. 1.
+// Positions m..p-1 stand for +infinity: a real key only ever moves to a lower position by a
+// swap with a larger one, so it never reaches them, and pairs that touch them never swap.
+// O(m log^2 m) work, (log2 p)(log2 p + 1)/2 barriers.  Keys are distinct (they hold the
+// agent index).
+__device__ void block_bitonic(uint64_t *t, uint32_t m) {
+  uint32_t p = 1;
+  while (p < m) p <<= 1;
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t x = threadIdx.x; x < (p >> 1); x += blockDim.x) {
+        const uint32_t blk = x / j, off = x - blk * j;
+        uint32_t a, b;
+        if (j == (k >> 1)) {  // mirror stage of a merge of two runs of k / 2
+          a = blk * k + off;
+          b = blk * k + k - 1 - off;
+        } else {  // half-cleaner over blocks of 2 j
+          a = blk * 2 * j + off;
+          b = a + j;
+        }
+        if (b < m) {
+          const uint64_t ta = t[a], tb = t[b];
+          if (tb < ta) {
+            t[a] = tb;
+            t[b] = ta;
+          }
+        }
+      }
+      __syncthreads();
     }
-    t[b] = x;
+  }
+}
+
+// One thread per voxel: order the voxel's segment of slot keys and reset its histogram
+// counter.  Segments hold ~2 agents in the configured workloads and are insertion-sorted by
+// their thread; a longer one (a coarse grid, a dense cluster) goes to a list in shared
+// memory and is sorted by the whole block afterwards, in shared memory up to kSegSmem
+// entries and in place in global memory beyond, so a voxel with 2^20 agents costs
+// O(m log^2 m) rather than O(m^2).
+__global__ void __launch_bounds__(kSegThreads) k_segsort(const SortArgs A) {
+  __shared__ uint32_t sLong[kSegThreads];
+  __shared__ uint32_t nLong;
+  __shared__ uint64_t sBuf[kSegSmem];
+  if (threadIdx.x == 0) nLong = 0;
+  __syncthreads();
+  const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < A.n_vox) {
+    const uint32_t s0 = A.start[v], s1 = A.start[v + 1];
+    A.count[v] = 0u;
+    if (s0 > s1 || s1 > A.n_agents) {
+      invariant_failed(A.status, kSiteSegRange, v);
+    } else if (s1 - s0 > kSegShort) {
+      sLong[atomicAdd(&nLong, 1u)] = v;
+    } else if (s1 - s0 >= 2) {
+      uint64_t *t = A.tmp;
+      for (uint32_t a = s0 + 1; a < s1; ++a) {
+        uint64_t x = t[a];
+        uint32_t b = a;
+        while (b > s0 && t[b - 1] > x) {
+          t[b] = t[b - 1];
+          --b;
+        }
+        t[b] = x;
+      }
+    }
+  }
+  __syncthreads();
+  const uint32_t n_long = nLong;
+  for (uint32_t q = 0; q < n_long; ++q) {
+    const uint32_t w = sLong[q];
+    const uint32_t s0 = A.start[w], m = A.start[w + 1] - s0;  // checked above
+    if (m <= kSegSmem) {
+      for (uint32_t x = threadIdx.x; x < m; x += blockDim.x) sBuf[x] = A.tmp[s0 + x];
+      __syncthreads();
+      block_bitonic(sBuf, m);
+      for (uint32_t x = threadIdx.x; x < m; x += blockDim.x) A.tmp[s0 + x] = sBuf[x];
+      __syncthreads();
+    } else {
+      block_bitonic(A.tmp + s0, m);
+    }
   }
 }
 
@@ -187,8 +293,16 @@ __global__ void k_segsort(const SortArgs A) {
 // offsets from the voxel corner.
 __global__ void k_gather(const SortArgs A) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0 && A.step_ctr) *A.step_ctr += 1;
+  if (s == 0 && A.step_ctr) {
+    *A.step_ctr += 1;
+    // the failed simulation as the next step's force kernels see it (sim_frozen)
+    const int32_t code = A.status[0];
+    A.status[6] = code == 0 ? 0 : code == CRG_EINTERNAL ? -1 : A.status[4] + 1;
+  }
   if (s >= A.n_agents) return;
+  // a simulation whose step failed keeps its current state (its slots are its positions)
+  const int32_t f = A.initial ? -1 : failed_sim(A.status);
+  if (f >= 0 && s - A.sims[f].agent_off < A.sims[f].n_agents) return;
   uint32_t src = (uint32_t)(A.tmp[s] & 0x7fffffffull);
   if (src >= A.n_agents) {
     invariant_failed(A.status, kSiteGatherSrc, s);
@@ -327,28 +441,51 @@ __global__ void k_transpose_out(const double *__restrict__ src, double *__restri
   for (int c = 0; c < nc; ++c) dst[(int64_t)i * nc + c] = src[c * cap + i];
 }
 
+// Per-agent values of the cell list ([nc][cap], slot s) back to the agent-major layout and
+// the order of the arrays the cell list was built from: row = the index field of the slot key
+// the insertion sort left in tmp.
+__global__ void k_unsort_out(const double *__restrict__ src, const uint64_t *__restrict__ tmp,
+                             double *__restrict__ dst, uint32_t n, int nc, int64_t cap,
+                             int32_t *status) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t row = (uint32_t)(tmp[s] & 0x7fffffffull);
+  if (row >= n) {
+    invariant_failed(status, kSiteGatherSrc, s);
+    return;
+  }
+  for (int c = 0; c < nc; ++c) dst[(int64_t)row * nc + c] = src[c * cap + s];
+}
+
 }  // namespace
 
 static inline unsigned grid_for(uint64_t n, unsigned block) {
   return (unsigned)((n + block - 1) / block);
 }
 
-void launch_scan(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
-                 cudaStream_t st) {
+// status / sims non-null: a cell-list re-sort, which takes the voxel sizes of a simulation
+// whose step failed from the current cell list (k_scan_reduce, k_scan_single).
+static void scan_impl(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
+                      const int32_t *status, const SimDev *sims, cudaStream_t st) {
   const uint32_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb <= 1) {
-    k_scan_single<<<1, kScanThreads, 0, st>>>(count, n, start);
+    k_scan_single<<<1, kScanThreads, 0, st>>>(count, n, start, status, sims);
   } else {
-    k_scan_reduce<<<nb, kScanThreads, 0, st>>>(count, n, bsum);
+    k_scan_reduce<<<nb, kScanThreads, 0, st>>>(count, n, bsum, status, sims, start);
     k_scan_blocks<<<1, kScanThreads, 0, st>>>(bsum, nb, start, n);
     k_scan_final<<<nb, kScanThreads, 0, st>>>(count, n, bsum, start);
   }
 }
 
+void launch_scan(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
+                 cudaStream_t st) {
+  scan_impl(count, n, start, bsum, nullptr, nullptr, st);
+}
+
 void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
-  launch_scan(A.count, A.n_vox, A.start, bsum, st);
+  scan_impl(A.count, A.n_vox, A.start, bsum, A.initial ? nullptr : A.status, A.sims, st);
   if (A.n_agents) k_scatter<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
-  k_segsort<<<grid_for(A.n_vox, 256), 256, 0, st>>>(A);
+  k_segsort<<<grid_for(A.n_vox, kSegThreads), kSegThreads, 0, st>>>(A);
   if (A.n_agents) k_gather<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
 }
 
@@ -370,6 +507,11 @@ void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int
 void launch_transpose_out(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
                           cudaStream_t st) {
   if (n) k_transpose_out<<<grid_for(n, 256), 256, 0, st>>>(src, dst, n, nc, cap);
+}
+
+void launch_unsort_out(const double *src, const uint64_t *tmp, double *dst, uint32_t n, int nc,
+                       int64_t cap, int32_t *status, cudaStream_t st) {
+  if (n) k_unsort_out<<<grid_for(n, 256), 256, 0, st>>>(src, tmp, dst, n, nc, cap, status);
 }
 
 }  // namespace crg
@@ -427,7 +569,7 @@ __global__ void k_noalloc_keys(const crg::SimDev S, uint32_t n, const double *__
     if (r == 2) bad = 2;
   }
   if (bad) {
-    if (atomicCAS(&status[0], 0, bad == 1 ? CRG_EBOUNDARY : CRG_EINDEX) == 0) status[1] = (int32_t)i;
+    atomicCAS(&status[0], 0, bad == 1 ? CRG_EBOUNDARY : CRG_EINDEX);  // first error wins
     plain = 0;
   }
   voxel[i] = plain;
@@ -526,11 +668,12 @@ extern "C" int32_t crg_cell_list_noalloc(const crg_domain *d, int64_t n, const d
   A.tmp = tmp;
   A.status = status;
   const uint32_t nb = (nvox + crg::kScanTile - 1) / crg::kScanTile;
-  crg::k_scan_reduce<<<nb, crg::kScanThreads, 0, st>>>(count, nvox, bsum);
+  crg::k_scan_reduce<<<nb, crg::kScanThreads, 0, st>>>(count, nvox, bsum, nullptr, nullptr,
+                                                       nullptr);
   crg::k_scan_blocks<<<1, crg::kScanThreads, 0, st>>>(bsum, nb, start_out, nvox);
   crg::k_scan_final<<<nb, crg::kScanThreads, 0, st>>>(count, nvox, bsum, start_out);
   if (un) crg::k_scatter<<<(un + 255) / 256, 256, 0, st>>>(A);
-  crg::k_segsort<<<(nvox + 255) / 256, 256, 0, st>>>(A);
+  crg::k_segsort<<<(nvox + crg::kSegThreads - 1) / crg::kSegThreads, crg::kSegThreads, 0, st>>>(A);
   if (un) k_noalloc_order<<<(un + 255) / 256, 256, 0, st>>>(tmp, un, order_out);
   if (cudaGetLastError() != cudaSuccess) return CRG_ECUDA;
   int32_t h_status[4] = {0, 0, 0, 0};

@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
   }
-  if (*P.step_ctr >= S.stop_step) {  // frozen simulation
+  if (sim_frozen(P, S)) {  // frozen simulation
     frozen_copy(P, i, key, D);
     return;
   }
@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
     if (valid && k == 0) invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
   }
-  const bool live = valid && *P.step_ctr < S.stop_step;
+  const bool live = valid && !sim_frozen(P, S);
   if (valid && !live && k == 0) frozen_copy(P, i, key, D);
   const uint32_t v = key - S.voxel_off;
   int idx[D];
@@ -674,7 +674,7 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
     const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
     nb[c] = hi - lo[c] + 1;
   }
-  const bool frozen = valid && (*P.step_ctr >= S.stop_step);
+  const bool frozen = valid && sim_frozen(P, S);
   bool done = !valid || frozen;
   int c0 = lo[0], c1 = lo[1], c2 = lo[2];  // next neighbour box; c0 past the end: none left
   uint32_t b_next = 0, b_end = 0;

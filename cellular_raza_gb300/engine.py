@@ -121,6 +121,32 @@ class Simulation:
         rc = self._L.crg_step(self._h, int(n_steps))
         N.check(rc, "crg_step", self._h)
 
+    def forces(self, pos: np.ndarray) -> np.ndarray:
+        """Interaction force of every agent of `pos` ([n][n_vertices][dim], each voxel's agents
+        in chili's Vec order) as chili's step 1-3 accumulate it (crg_forces); the handle's
+        agents become these with zero velocity."""
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        n = pos.shape[0]
+        if pos.size != n * self.nc:
+            raise ValueError("pos must have shape [n][n_vertices][dim]")
+        out = np.empty_like(pos)
+        N.check(self._L.crg_forces(self._h, n, _dp(pos), _dp(out)), "crg_forces", self._h)
+        self.counts = [n]
+        return out
+
+    @property
+    def steps_done(self) -> int:
+        """Steps the handle's state has advanced since the last upload (crg_step_count)."""
+        n = C.c_int64()
+        N.check(self._L.crg_step_count(self._h, C.byref(n)), "crg_step_count")
+        return n.value
+
+    def clear_error(self):
+        """Clears the handle's error (crg_clear_error); returns (code, simulation)."""
+        sim = C.c_int32(-1)
+        code = self._L.crg_clear_error(self._h, C.byref(sim))
+        return code, sim.value
+
     @property
     def n_agents(self) -> int:
         n = C.c_int64()

@@ -138,8 +138,26 @@ int32_t crg_upload(crg_ctx *ctx, int64_t n, const int64_t *counts, const double 
 
 /* Advances every simulation of the handle by n_steps chili steps (the macro-generated
  * loop body, cellular_raza-core-proc-macro/src/run_sim.rs:380-403).  Stops at the first
- * device-reported error and returns it; crg_last_error gives the agent and step. */
+ * device-reported error and returns it; crg_last_error gives the agent and the step.
+ * The step that fails is not committed for the simulation that raised the error, and later
+ * steps leave that simulation unchanged (chili stops a run at its first error,
+ * chili/errors.rs:73-122): a single-simulation handle then holds the state after its last
+ * successful step, which crg_step_count reports.  crg_clear_error lets it continue. */
 int32_t crg_step(crg_ctx *ctx, int64_t n_steps);
+
+/* Interaction forces without a step: the per-agent force that chili's
+ * update_mechanics_interaction_step_1/2/3 accumulate into AuxStorageMechanics::current_force
+ * (cellular_raza-core/src/backend/chili/update_mechanics.rs:153-382, add_force in
+ * chili/aux_storage.rs:120-129), with chili's pair weights for the handle's n_subdomains.
+ * pos: [n][n_vertices][dim] doubles (n_vertices = 1 for point agents) listing the agents of
+ * every voxel in the order that voxel's Vec holds them (voxels in any order); force receives
+ * [n][n_vertices][dim] in the same order.  This is the body of a step-1 hook
+ * (run_simulation!'s update_mechanics_interaction_step_1 kwarg, cellular_raza-core-proc-macro/
+ * src/run_sim.rs:150-157,251-256) for a chili run with one subdomain: the hook adds the
+ * forces to each cell's aux storage and chili's own local_mechanics_update, apply_boundary
+ * and re-sort run unchanged.  The handle's agents are replaced by these (as crg_upload with
+ * zero velocities).  Single-simulation handles without a cell cycle; otherwise CRG_ENOTSUP. */
+int32_t crg_forces(crg_ctx *ctx, int64_t n, const double *pos, double *force);
 
 /* Copies the current agents out in cell-list order (sorted by voxel).  Any pointer may be
  * NULL.  voxel receives the voxel plain index (per simulation). */
@@ -320,7 +338,8 @@ int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
  *   order_out  device [n]: the point index held by each slot of the cell list (voxels
  *              ascending, input order inside a voxel) -- the order crg_upload produces
  *   start_out  device [n_voxels + 1]: first slot of every voxel, start_out[n_voxels] = n
- *   stream     cudaStream_t to run on (NULL: the default stream); the call waits for it
+ *   stream     cudaStream_t to run on (NULL: the default stream); the call synchronizes
+ *              it before returning (it reads the status word back)
  *
  * Limits: n <= CRG_NOALLOC_MAX_POINTS and n_voxels <= CRG_NOALLOC_MAX_VOXELS, otherwise
  * CRG_EINVAL before anything runs.  All calls share the scratch array: calls that overlap

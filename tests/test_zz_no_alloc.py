@@ -75,3 +75,27 @@ def test_noalloc_cell_list_matches_upload_two_calls():
         assert rc == N.CRG_OK, N.strerror(rc)
         for name, g, r in zip(("voxel", "order", "start"), got, want):
             assert np.array_equal(g, r), name
+
+
+def test_dense_voxels_sort_in_bounded_time():
+    """Voxels holding tens of thousands of points (an interaction range as large as the
+    domain puts 2^16 points into one voxel; a coarse grid gives segments below the
+    shared-memory sort's 2,048 entries).  The per-voxel ordering is a block-wide sorting
+    network for long segments, so these calls take milliseconds; the bound below is a
+    generous wall-time limit.  Results: exact, against crg_upload, and the single voxel's
+    order is the input order."""
+    import time
+
+    torch = pytest.importorskip("torch")
+    one = W.spheres(1 << 16, 100.0, seed=81, dim=3, interaction_range=150.0)  # 1 voxel
+    coarse = W.spheres(40_000, 100.0, seed=82, dim=2, interaction_range=20.0)  # 25 voxels
+    for w in (one, coarse):
+        t0 = time.perf_counter()
+        want = reference_cell_list(w)
+        rc, got = noalloc_cell_list(torch, w)
+        assert time.perf_counter() - t0 < 20.0
+        assert rc == N.CRG_OK, N.strerror(rc)
+        for name, g, r in zip(("voxel", "order", "start"), got, want):
+            assert np.array_equal(g, r), name
+    _, order, _ = noalloc_cell_list(torch, one)[1]
+    assert np.array_equal(order, np.arange(one.n, dtype=np.uint32))
