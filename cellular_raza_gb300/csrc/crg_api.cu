@@ -76,7 +76,8 @@ struct crg_ctx {
   int variant = 0;
   int block = 0;
   int profile = 0;
-  double prof_ms[4] = {0, 0, 0, 0};
+  double prof_ms[5] = {0, 0, 0, 0, 0};
+  std::vector<cudaEvent_t> pev;  // CRG_OPT_PROFILE: kProfEvents per step of a chunk
   int32_t err_code = CRG_OK;
   int64_t err_agent = -1, err_step = -1;
   int64_t steps_done = 0;
@@ -291,8 +292,15 @@ int32_t alloc_pass_list(crg_ctx *c, int64_t n) {
   return CRG_OK;
 }
 
+void free_events(crg_ctx *c) {
+  for (cudaEvent_t e : c->pev)
+    if (e) cudaEventDestroy(e);
+  c->pev.clear();
+}
+
 void free_all(crg_ctx *c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  free_events(c);
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
@@ -545,25 +553,41 @@ SortArgs sort_args(crg_ctx *c, int initial) {
 // Kernels one launch_force issues: the default rod path runs the pass walk, the pass kernel,
 // the rod-level fallback (returns at once unless the pass list overflowed) and the update.
 int force_kernel_count(const crg_ctx *c) {
-  if (c->kind == CRG_KIND_ROD) return c->variant == 0 ? (c->nv > 2 ? 5 : 4) : 1;
+  if (c->kind == CRG_KIND_ROD) return c->variant != 1 ? (c->nv > 2 ? 5 : 4) : 1;
   return c->precision == CRG_PREC_F64 ? 1 : 2;
 }
 
-// k0 / k1 (optional): events recorded around the dominant force kernel.
-void launch_force(crg_ctx *c, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr) {
+// k0 / k1 (optional): events recorded around the dominant force kernel; k2 / k3 around the
+// rod update kernel.
+void launch_force(crg_ctx *c, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr,
+                  cudaEvent_t k2 = nullptr, cudaEvent_t k3 = nullptr) {
   PackArgs P = pack_args(c);
   if (c->kind == CRG_KIND_SPHERE) {
-    if (k0) cudaEventRecord(k0, c->stream);
+    crg::record_event(k0, c->stream);
     crg::launch_spheres_step(c->dim, c->precision, P, c->block, c->stream);
-    if (k1) cudaEventRecord(k1, c->stream);
+    crg::record_event(k1, c->stream);
   } else {
-    crg::launch_rods_step(c->dim, c->nv, c->precision, P, c->block, c->stream, k0, k1);
+    crg::launch_rods_step(c->dim, c->nv, c->precision, P, c->block, c->stream, k0, k1, k2, k3);
   }
 }
 
-void launch_one_step(crg_ctx *c) {
-  launch_force(c);
+// Steps per profiled chunk, and the events of each of its steps (CRG_OPT_PROFILE): before
+// the force stage, around the dominant force kernel, between the force stage and the sort,
+// after the sort, around the rod update kernel.
+constexpr int kProfChunk = 32;
+constexpr int kProfEvents = 7;
+
+// One step.  With prof_step >= 0 (profiling) the step's events are recorded around its
+// phases (as event nodes when the step is being captured into a graph, so the kernels can
+// be timed as they run from the graph).
+void launch_one_step(crg_ctx *c, int prof_step = -1) {
+  cudaEvent_t *e = (prof_step >= 0 && !c->pev.empty()) ? &c->pev[kProfEvents * prof_step] : nullptr;
+  if (e) crg::record_event(e[0], c->stream);
+  launch_force(c, e ? e[1] : nullptr, e ? e[2] : nullptr, e ? e[5] : nullptr,
+               e ? e[6] : nullptr);
+  if (e) crg::record_event(e[3], c->stream);
   crg::launch_sort(sort_args(c, 0), c->bsum, c->stream);
+  if (e) crg::record_event(e[4], c->stream);
 }
 
 // Waits for the handle's stream and reads the device status word.  A CUDA failure is
@@ -604,7 +628,7 @@ int32_t ensure_graph(crg_ctx *c, int steps) {
   }
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < steps; ++k) launch_one_step(c);
+  for (int k = 0; k < steps; ++k) launch_one_step(c, c->profile ? k : -1);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess) return CRG_ECUDA;
   e = cudaGraphInstantiate(&c->gexec, g, 0);
@@ -860,30 +884,40 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
     return CRG_OK;
   }
   if (c->cycle) return step_cycle(c, n_steps);
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   if (c->profile) {
-    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
-    c->prof_ms[0] = c->prof_ms[1] = c->prof_ms[2] = c->prof_ms[3] = 0.0;
+    if (c->pev.empty()) {
+      c->pev.assign(kProfEvents * kProfChunk, nullptr);
+      for (auto &e : c->pev) CUDA_TRY(cudaEventCreate(&e));
+    }
+    for (double &x : c->prof_ms) x = 0.0;
   }
   int64_t left = n_steps;
   const int chunk = c->graph_chunk;
   while (left > 0) {
     if (c->profile) {
-      const int k = (int)std::min<int64_t>(left, 64);
+      // the steps run as they run unprofiled (from a captured graph when chunks are on),
+      // with event nodes between the phases; the chunk's times are read after it
+      const int k = (int)std::min<int64_t>(left, kProfChunk);
+      if (chunk > 0 && k == kProfChunk) {
+        int32_t r = ensure_graph(c, k);
+        if (r != CRG_OK) return r;
+        CUDA_TRY(cudaGraphLaunch(c->gexec, c->stream));
+      } else {
+        for (int s = 0; s < k; ++s) launch_one_step(c, s);
+      }
+      CUDA_TRY(cudaStreamSynchronize(c->stream));
       for (int s = 0; s < k; ++s) {
-        cudaEventRecord(ev[0], c->stream);
-        launch_force(c, ev[3], ev[4]);
-        cudaEventRecord(ev[1], c->stream);
-        crg::launch_sort(sort_args(c, 0), c->bsum, c->stream);
-        cudaEventRecord(ev[2], c->stream);
-        cudaEventSynchronize(ev[2]);
-        float a = 0.f, b = 0.f, d = 0.f;
-        cudaEventElapsedTime(&a, ev[0], ev[1]);
-        cudaEventElapsedTime(&b, ev[1], ev[2]);
-        cudaEventElapsedTime(&d, ev[3], ev[4]);
+        const cudaEvent_t *e = &c->pev[kProfEvents * s];
+        float a = 0.f, b = 0.f, d = 0.f, u = 0.f;
+        cudaEventElapsedTime(&a, e[0], e[3]);
+        cudaEventElapsedTime(&b, e[3], e[4]);
+        cudaEventElapsedTime(&d, e[1], e[2]);
+        if (c->kind == CRG_KIND_ROD && c->variant != 1)
+          cudaEventElapsedTime(&u, e[5], e[6]);  // recorded by the pass-list rod path only
         c->prof_ms[0] += a;
         c->prof_ms[1] += b;
         c->prof_ms[3] += d;
+        c->prof_ms[4] += u;
         c->prof_ms[2] += force_kernel_count(c) + crg::sort_kernel_count(c->n_vox);
       }
       left -= k;
@@ -906,8 +940,6 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
     int32_t r = read_status(c);
     if (r != CRG_OK) break;
   }
-  if (c->profile)
-    for (auto &e : ev) cudaEventDestroy(e);
   c->steps_done += n_steps - std::max<int64_t>(left, 0);
   // The failing step of a simulation is not committed and its later steps leave it frozen
   // (sim_frozen, failed_sim): a single simulation holds the state after its last good step.
@@ -1141,7 +1173,7 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   };
   std::vector<Shape> shapes;
   if (c->kind == CRG_KIND_ROD) {
-    shapes = {{0, 0}, {3, 0}, {1, 64}, {2, 0}};
+    shapes = {{0, 0}, {1, 64}};
   } else if (c->precision == CRG_PREC_F64) {
     shapes = {{0, 0}, {2, 0}, {3, 0}, {3, 64}, {1, 64}, {1, 128}, {1, 256}};
   } else {
@@ -1462,7 +1494,14 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
       if (value < 0 || value > 1024) return CRG_EINVAL;
       c->block = (int)value;
       break;
-    case CRG_OPT_PROFILE: c->profile = value ? 1 : 0; break;
+    case CRG_OPT_PROFILE:
+      c->profile = value ? 1 : 0;
+      invalidate_graph(c);  // a captured graph may hold the events
+      if (!c->profile) {
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        free_events(c);
+      }
+      break;
     case CRG_OPT_KERNEL_VARIANT:
       if (value < 0 || value > 3) return CRG_EINVAL;
       c->variant = (int)value;
@@ -1491,9 +1530,9 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
   return CRG_OK;
 }
 
-int32_t crg_profile(crg_ctx *c, double *out4) {
-  if (!c || !out4) return CRG_EINVAL;
-  for (int k = 0; k < 4; ++k) out4[k] = c->prof_ms[k];
+int32_t crg_profile(crg_ctx *c, double *out5) {
+  if (!c || !out5) return CRG_EINVAL;
+  for (int k = 0; k < 5; ++k) out5[k] = c->prof_ms[k];
   return CRG_OK;
 }
 

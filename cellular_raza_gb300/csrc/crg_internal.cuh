@@ -96,17 +96,18 @@ struct PackArgs {
   uint32_t *npass, *pass_off;  // [cap] number of passes of each rod, index of its first
   uint32_t *pass_a, *pass_b;   // [pass_cap] rod and candidate of each pass
   uint8_t *pass_meta;          // [pass_cap] bit 0: ext pass; bits 1-6: voxel of b - voxel of
-                               // a + 1 per axis, 2 bits each
+                               // a + 1 per axis, 2 bits each; bit 7: a step-3 pass, summed
+                               // per neighbour box before it is added
   double *mbuf;                // [nc][pass_cap] M / 2 of each pass, rows in vertex order
   int64_t pass_cap;
-  uint32_t *rctl;  // [0] passes reserved, [1] pass queue, [2] rod queue, [3] pass list
-                   // overflow (all zeroed before each step)
+  uint32_t *rctl;  // [0] passes reserved, [1] pass queue, [3] pass list overflow (all
+                   // zeroed before each step)
   double *frc;     // rods: [nc][cap] interaction force of the rod-level fallback kernel
   double *bend;    // rods: [nv - 2][dim][cap] curvature forces (k_rods_bend)
   uint32_t *fix_list;  // mixed spheres: agents whose force the FP64 fix-up kernel computes
                        // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
-  int32_t variant;    // force kernel: 0 warp-packed (default), 1 thread per agent
+  int32_t variant;    // force kernel: 0 default, 1 thread per agent (CRG_OPT_KERNEL_VARIANT)
   // cell cycle (rods; all null when off)
   const double *slen;       // [cap] spring length of each rod (current order)
   const double *grate;      // [cap] growth rate of each rod (current order)

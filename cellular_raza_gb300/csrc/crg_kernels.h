@@ -87,9 +87,11 @@ void launch_unsort_out(const double *src, const uint64_t *tmp, double *dst, uint
 
 // Force + integrator + boundary + next voxel key (+ histogram) for one step.
 void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, cudaStream_t st);
-// k0 / k1 (optional) are recorded on st right before and after the dominant force kernel.
+// k0 / k1 (optional) are recorded on st right before and after the dominant force kernel,
+// k2 / k3 around the update kernel of the pass-list path.
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
-                      cudaStream_t st, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr);
+                      cudaStream_t st, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr,
+                      cudaEvent_t k2 = nullptr, cudaEvent_t k3 = nullptr);
 int prepare_rods(int dim, int nv);  // 0 on success
 // Cell cycle of rods: neighbour counts of this step (before the update kernel), and after
 // the update and the scan of its division flags, the divisions (n_div > 0), then the voxel

@@ -10,20 +10,21 @@
 //   same voxel, b before a in the voxel: ext then own   (update_mechanics.rs:193-199,
 //   same voxel, b after a:                own then ext    a is the first or second cell)
 //   neighbour voxel, same subdomain:      own only        (:205-220; the ext half is dropped)
-//   neighbour voxel, other subdomain:     own then ext    (steps 2 and 3, :285-382)
+//   neighbour voxel, other subdomain:     own in step 2, after every local term, then ext in
+//                                         step 3, summed per voxel first (:285-382)
 // Vertex/segment evaluations whose FP32 distance exceeds the cutoff plus margin are zero
 // in FP64 as well and are skipped; the rest are evaluated in FP64 in the reference's
 // operation order.  RodMechanics::calculate_increment (bacterial_rods.rs:157-213), the
 // solver, apply_boundary (:489-534) and the centroid voxel key follow.
 //
-// The kernels (all produce identical bits): the default path lists every rod's passes
-// (one pass = own_a(b) or ext_a(b)) in that order (k_rods_walk), evaluates them one pass
-// per lane with the survivors of the warp's 32 passes in full FP64 batches
-// (k_rods_passq), computes the curvature forces per angle (k_rods_bend) and adds up each
-// rod's passes in order before the mechanics and the solver (k_rods_update); k_rods_queue
-// is the same evaluation with one rod per lane (fallback when the pass list overflows).
-// k_rods_step (one thread per rod), k_rods_packed and k_rods_pass are kept as cross-check
-// variants (CRG_OPT_KERNEL_VARIANT).
+// The FP64 kernels (both produce identical bits): the default path lists every rod's passes
+// (one pass = own_a(b) or ext_a(b)) in chili's order (k_rods_walk), evaluates them one pass
+// per lane with the survivors of the warp's 32 passes in full FP64 batches (k_rods_passq),
+// computes the curvature forces per angle (k_rods_bend) and adds up each rod's passes in
+// order before the mechanics and the solver (k_rods_update); k_rods_step is the same
+// evaluation with one rod per thread (CRG_OPT_KERNEL_VARIANT 1, and the fallback when the
+// pass list overflows).  With several subdomains the order is that of chili's steps 1, 2
+// and 3 (k_rods_step explains it).
 #include "crg_internal.cuh"
 #include "crg_kernels.h"
 
@@ -411,13 +412,29 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   P.nid[i] = P.id[i];
 }
 
-template <int D, int NV, int B>
+// Thread per rod, in the order chili's loop adds rod a's terms into its force accumulator
+// (update_mechanics.rs:153-382, determinism = true):
+//   phase 0, step 1: the boxes of a's subdomain, ascending: a's own voxel pair by pair
+//            (b before a: ext then own; b after a: own then ext), a neighbour voxel own only
+//            (the ext half is dropped, :205-220);
+//   phase 1, step 2: the boxes of other subdomains, ascending: own_a(b) / 2 for each b
+//            (PosInformation received and sorted by sender voxel, :304-330);
+//   phase 2, step 3: per box of another subdomain, ascending, one term: the sum over its
+//            rods b, in storage order, of ext_a(b) / 2 (the ForceInformation that voxel's
+//            subdomain returns, summed with xapy, :87-100, :344-382).
+// With CRG_WEIGHTS_PHYSICAL every box takes phase 0 with both halves.  Terms skipped by the
+// prefilter are +0 and change no sum.  FALLBACK: the kernel runs after a pass-list overflow
+// only (P.rctl[3]) and leaves the force in P.frc for k_rods_update; otherwise it runs the
+// update itself.
+template <int D, int NV, int B, bool FALLBACK>
 __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   constexpr int NC = NV * D;
   __shared__ double sPa[NC][B];
   __shared__ double sT[NC][B];
+  __shared__ double sG[NC][B];  // phase 2: the current box's ext sum
   __shared__ float sOa[NC][B];
   __shared__ float sOb[NC][B];
+  if (FALLBACK && !P.rctl[3]) return;  // the pass list fitted: k_rods_passq computed this step
   const int tid = threadIdx.x;
   const uint32_t i = blockIdx.x * B + tid;
   if (i >= P.n_agents) return;
@@ -429,8 +446,8 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
   }
-  if (sim_frozen(P, S)) {  // frozen simulation
-    frozen_copy(P, i, key, NC);
+  if (sim_frozen(P, S)) {  // frozen simulation (the fallback leaves it to k_rods_update)
+    if (!FALLBACK) frozen_copy(P, i, key, NC);
     return;
   }
   const uint32_t v = key - S.voxel_off;
@@ -460,6 +477,7 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
 #pragma unroll
   for (int k = 0; k < NC; ++k) a_nan |= !(oa[k] == oa[k]);
   const uint32_t sub_v = subdomain_of(S, v);
+  const bool physical = S.weight_mode == CRG_WEIGHTS_PHYSICAL;
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
   double acc[NC];
@@ -471,539 +489,106 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
     lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
     hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
   }
-  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
-    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
-      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
-        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
-                                    : (uint32_t)j0 * S.nvox[1] + j1;
-        const bool same = (w == v);
-        const bool twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
-                           subdomain_of(S, w) != sub_v;
-        // b's offsets in a's voxel frame: off_b + (corner_b - corner_a) = off_b + (j-idx) dx
-        float kd[D];
-        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
-        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
-        if (b0 > b1 || b1 > P.n_agents) {
-          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-          b1 = b0;
-        }
-        for (uint32_t b = b0; b < b1; ++b) {
-          if (b == i) continue;
-          float ob[NC];
-          float bmin[D], bmax[D];
-#pragma unroll
-          for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            bmin[c] = ob[c];
-            bmax[c] = ob[c];
-          }
-#pragma unroll
-          for (int k = D; k < NC; ++k) {
-            bmin[k % D] = fminf(bmin[k % D], ob[k]);
-            bmax[k % D] = fmaxf(bmax[k % D], ob[k]);
-          }
-          // Bounding boxes farther apart than the threshold on one axis: all 2 x NV x (NV-1)
-          // evaluations are beyond the cutoff.  (fminf/fmaxf drop NaNs, so a NaN anywhere
-          // disables the box test.)
-          bool far = false;
-          bool b_nan = false;
-#pragma unroll
-          for (int k = 0; k < NC; ++k) b_nan |= !(ob[k] == ob[k]);
-          if (!a_nan && !b_nan) {
-#pragma unroll
-            for (int c = 0; c < D; ++c)
-              far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
-          }
-          if (far) continue;
-#pragma unroll
-          for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
-          const double *posb = P.pos + b;
-          const bool ext_first = same && (b < i);
 #pragma unroll 1
-          for (int pass = 0; pass < 2; ++pass) {
-            const bool is_ext = (pass == 0) == ext_first;
-            if (is_ext && !twice) continue;
-            if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
-              add_half<NC, B>(acc, sT, tid);
+  for (int phase = 0; phase < 3; ++phase)
+    for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+      for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+        for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+          const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                      : (uint32_t)j0 * S.nvox[1] + j1;
+          const bool same = (w == v);
+          const bool local = physical || subdomain_of(S, w) == sub_v;
+          if (local != (phase == 0)) continue;
+          // b's offsets in a's voxel frame: off_b + (corner_b - corner_a) = off_b + (j-idx) dx
+          float kd[D];
+          kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+          kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+          if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+          uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+          if (b0 > b1 || b1 > P.n_agents) {
+            invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+            b1 = b0;
           }
-        }
-      }
-  rod_update<D, NV>(P, S, i, key, pa, acc);
-}
-
-// ---------------------------------------------------------------------------------------
-// Warp-packed variant.  The thread-per-rod kernel above leaves most FP64 lanes idle: each
-// thread evaluates a different number of vertex/segment pairs that survive the FP32
-// prefilter.  Here lane l of a warp owns rod a_l and enumerates its surviving evaluations
-// (its "items") in exactly the order k_rods_step visits them, K at a time, into a per-lane
-// slot list in shared memory.  The whole warp then evaluates every queued item in FP64 with
-// all lanes busy, and finally each lane folds its own results into its pass accumulator M
-// and the rod force in order.  Items that end a pass carry a flush flag (acc += M / 2,
-// M = 0); a pass whose last item went out in an earlier round gets a marker item.  The
-// arithmetic per item and the summation order are those of k_rods_step, so both kernels
-// produce identical bits.
-// ---------------------------------------------------------------------------------------
-constexpr uint32_t kItFlush = 1u;    // fold M into acc after this item
-constexpr uint32_t kItMarker = 2u;   // no evaluation: flush only
-constexpr uint32_t kItExt = 4u;      // ext_a(b) item (b's vertex against a's segment)
-constexpr uint32_t kItZero = 8u;     // evaluated: force is zero (beyond cutoff or at zero distance)
-
-__device__ __forceinline__ uint64_t pack_item(uint32_t b, uint32_t flags, int vx, int sy) {
-  return ((uint64_t)b << 32) | ((uint64_t)(sy & 15) << 8) | ((uint64_t)(vx & 15) << 4) | flags;
-}
-
-template <int D, int NV, int W, int K>
-__global__ void __launch_bounds__(W * 32) k_rods_packed(const PackArgs P) {
-  constexpr int NC = NV * D, NE = NV - 1, NS = NV * NE;
-  __shared__ uint64_t sItem[W][K][32];
-  __shared__ double sRes[W][K][2 * D][32];
-  __shared__ double sM[W][NC][32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint32_t warp_base = (blockIdx.x * W + wid) * 32;
-  const uint32_t i = warp_base + lane;
-  const bool valid = i < P.n_agents;
-  const int64_t cap = P.cap;
-  const uint32_t ii = valid ? i : 0u;
-  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
-  const SimDev &S = P.sims[sim];
-  uint32_t key = P.key[ii];
-  if (key - S.voxel_off >= S.n_vox) {
-    if (valid) invariant_failed(P.status, kSiteForceKey, i);
-    key = S.voxel_off;
-  }
-  const uint32_t v = key - S.voxel_off;
-  int idx[D];
-  unravel<D>(S, v, idx);
-  float amin[D], amax[D];
-  bool a_nan = false;
+          bool grp = false;  // phase 2: the box's ext sum holds a term
+          for (uint32_t b = b0; b < b1; ++b) {
+            if (b == i) continue;
+            float ob[NC];
+            float bmin[D], bmax[D];
 #pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    const float o = P.off[k * cap + ii];
-    a_nan |= !(o == o);
-    if (k < D) {
-      amin[k] = o;
-      amax[k] = o;
-    } else {
-      amin[k % D] = fminf(amin[k % D], o);
-      amax[k % D] = fmaxf(amax[k % D], o);
-    }
-  }
-  const uint32_t sub_v = subdomain_of(S, v);
-  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
-  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+            for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
 #pragma unroll
-  for (int k = 0; k < NC; ++k) sM[wid][k][lane] = 0.0;
-  double acc[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
-
-  // neighbourhood box (ascending plain index = j0 outer, last axis inner)
-  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
-    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
-    nb[c] = hi - lo[c] + 1;
-  }
-  const int n_box = nb[0] * nb[1] * nb[2];
-  // enumeration cursor
-  const bool frozen = valid && sim_frozen(P, S);
-  bool done = !valid || frozen;
-  int stage = 0;  // 0: next voxel, 1: next candidate, 2: inside a pass
-  int o_box = 0;
-  uint32_t b_next = 0, b_end = 0, cur_b = 0;
-  bool same = false, twice = false, ext_first = false, pending_flush = false;
-  int pass = 0, vs = 0, pass_items = 0;
-  float kd[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) kd[c] = 0.f;
-
-  while (__any_sync(0xffffffffu, !done || pending_flush)) {
-    // ---- 1. enumerate up to K items -------------------------------------------------
-    int cnt = 0;
-    int pass_items_round = 0;
-    if (pending_flush) {
-      sItem[wid][cnt++][lane] = pack_item(0, kItMarker, 0, 0);
-      pending_flush = false;
-    }
-    while (!done && cnt < K) {
-      if (stage == 0) {
-        if (o_box >= n_box) {
-          done = true;
-          break;
-        }
-        const int j2 = lo[2] + o_box % nb[2];
-        const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
-        const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
-        ++o_box;
-        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
-                                    : (uint32_t)j0 * S.nvox[1] + j1;
-        same = (w == v);
-        twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
-        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
-        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        b_next = P.start[S.voxel_off + w];
-        b_end = P.start[S.voxel_off + w + 1];
-        if (b_next > b_end || b_end > P.n_agents) {
-          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-          b_end = b_next;
-        }
-        stage = 1;
-        continue;
-      }
-      if (stage == 1) {
-        if (b_next >= b_end) {
-          stage = 0;
-          continue;
-        }
-        const uint32_t b = b_next++;
-        if (b == i) continue;
-        float bmin[D], bmax[D];
-        bool b_nan = false;
-#pragma unroll
-        for (int k = 0; k < NC; ++k) {
-          const float o = P.off[k * cap + b] + kd[k % D];
-          b_nan |= !(o == o);
-          if (k < D) {
-            bmin[k] = o;
-            bmax[k] = o;
-          } else {
-            bmin[k % D] = fminf(bmin[k % D], o);
-            bmax[k % D] = fmaxf(bmax[k % D], o);
-          }
-        }
-        bool far = false;
-        if (!a_nan && !b_nan) {
-#pragma unroll
-          for (int c = 0; c < D; ++c)
-            far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
-        }
-        if (far) continue;
-        cur_b = b;
-        ext_first = same && (b < i);
-        pass = 0;
-        vs = 0;
-        pass_items = 0;
-        pass_items_round = 0;
-        stage = 2;
-        continue;
-      }
-      // stage 2: scan the (vertex, segment) pairs of the current pass
-      const bool is_ext = (pass == 0) == ext_first;
-      if (is_ext && !twice) vs = NS;
-      while (vs < NS && cnt < K) {
-        const int vx = vs / NE, sy = vs - (vs / NE) * NE;
-        ++vs;
-        const uint32_t pr = is_ext ? cur_b : i;  // owner of the point
-        const uint32_t sr = is_ext ? i : cur_b;  // owner of the segment
-        const float pk = is_ext ? 1.f : 0.f;     // which side carries the corner shift
-        float p32[D], l0[D], l1[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) {
-          p32[c] = P.off[(vx * D + c) * cap + pr] + pk * kd[c];
-          l0[c] = P.off[(sy * D + c) * cap + sr] + (1.f - pk) * kd[c];
-          l1[c] = P.off[((sy + 1) * D + c) * cap + sr] + (1.f - pk) * kd[c];
-        }
-        if (seg_dist2_f32<D>(p32, l0, l1) > thr2) continue;
-        sItem[wid][cnt++][lane] = pack_item(cur_b, is_ext ? kItExt : 0u, vx, sy);
-        ++pass_items;
-        ++pass_items_round;
-      }
-      if (vs >= NS) {
-        if (pass_items > 0) {
-          if (pass_items_round > 0)
-            sItem[wid][cnt - 1][lane] |= kItFlush;
-          else if (cnt < K)
-            sItem[wid][cnt++][lane] = pack_item(0, kItMarker, 0, 0);
-          else
-            pending_flush = true;
-        }
-        ++pass;
-        vs = 0;
-        pass_items = 0;
-        pass_items_round = 0;
-        if (pass == 2) stage = 1;
-        if (pending_flush) break;
-      }
-    }
-    __syncwarp();
-
-    // ---- 2. evaluate every queued item with the whole warp ---------------------------
-    int incl = cnt;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += y;
-    }
-    const int excl = incl - cnt;
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    for (int base = 0; base < total; base += 32) {
-      const int j = base + lane;
-      // owner lane: the largest l with excl_l <= j
-      int l = 0;
-#pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int cand = l + step;
-        const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
-        if (cand < 32 && e <= j) l = cand;
-      }
-      const int ex_l = __shfl_sync(0xffffffffu, excl, l);
-      const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);  // parameters of the owner
-      if (j < total) {
-        const SimDev &So = P.sims[sim_l];
-        const int k = j - ex_l;
-        const uint64_t it = sItem[wid][k][l];
-        const uint32_t fl = (uint32_t)it & 15u;
-        if (!(fl & kItMarker)) {
-          const uint32_t b = (uint32_t)(it >> 32);
-          const uint32_t a = warp_base + l;
-          const int vx = (int)((it >> 4) & 15), sy = (int)((it >> 8) & 15);
-          const bool is_ext = fl & kItExt;
-          const uint32_t pr = is_ext ? b : a, sr = is_ext ? a : b;
-          double p[D], l0[D], l1[D], q[D], t, f[D];
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            p[c] = P.pos[(vx * D + c) * cap + pr];
-            l0[c] = P.pos[(sy * D + c) * cap + sr];
-            l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
-          }
-          nearest_point_f64<D>(p, l0, l1, q, t);
-          if (morse_full_f64<D>(p, q, So, f)) {
-            if (!is_ext) {
-#pragma unroll
-              for (int c = 0; c < D; ++c) sRes[wid][k][c][l] = f[c];
-            } else {
-              const double omt = dsub(1.0, t);
-#pragma unroll
-              for (int c = 0; c < D; ++c) {
-                const double fe = -f[c];
-                sRes[wid][k][c][l] = dmul(fe, omt);
-                sRes[wid][k][D + c][l] = dmul(fe, t);
-              }
+            for (int c = 0; c < D; ++c) {
+              bmin[c] = ob[c];
+              bmax[c] = ob[c];
             }
-          } else {
-            sItem[wid][k][l] = it | kItZero;
+#pragma unroll
+            for (int k = D; k < NC; ++k) {
+              bmin[k % D] = fminf(bmin[k % D], ob[k]);
+              bmax[k % D] = fmaxf(bmax[k % D], ob[k]);
+            }
+            // Bounding boxes farther apart than the threshold on one axis: all 2 x NV x
+            // (NV-1) evaluations are beyond the cutoff.  (fminf/fmaxf drop NaNs, so a NaN
+            // anywhere disables the box test.)
+            bool far = false;
+            bool b_nan = false;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) b_nan |= !(ob[k] == ob[k]);
+            if (!a_nan && !b_nan) {
+#pragma unroll
+              for (int c = 0; c < D; ++c)
+                far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+            }
+            if (far) continue;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
+            const double *posb = P.pos + b;
+            if (phase == 2) {  // step 3: ext_a(b) / 2 into the box's sum
+              if (rod_pass<D, NV, B>(true, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid)) {
+#pragma unroll
+                for (int k = 0; k < NC; ++k) {
+                  const double h = dmul(sT[k][tid], 0.5);
+                  sG[k][tid] = grp ? dadd(h, sG[k][tid]) : h;
+                }
+                grp = true;
+              }
+              continue;
+            }
+            const bool twice = phase == 0 && (same || physical);
+            const bool ext_first = same && (b < i);
+#pragma unroll 1
+            for (int pass = 0; pass < 2; ++pass) {
+              const bool is_ext = (pass == 0) == ext_first;
+              if (is_ext && !twice) continue;
+              if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
+                add_half<NC, B>(acc, sT, tid);
+            }
+          }
+          if (grp) {
+#pragma unroll
+            for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], sG[k][tid]);
           }
         }
-      }
-    }
-    __syncwarp();
-
-    // ---- 3. each lane folds its results in order ------------------------------------
-    for (int k = 0; k < cnt; ++k) {
-      const uint64_t it = sItem[wid][k][lane];
-      const uint32_t fl = (uint32_t)it & 15u;
-      if (!(fl & (kItMarker | kItZero))) {
-        const int vx = (int)((it >> 4) & 15), sy = (int)((it >> 8) & 15);
-        if (!(fl & kItExt)) {
+  if (FALLBACK) {
 #pragma unroll
-          for (int c = 0; c < D; ++c)
-            sM[wid][vx * D + c][lane] = dadd(sM[wid][vx * D + c][lane], sRes[wid][k][c][lane]);
-        } else {
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            sM[wid][sy * D + c][lane] = dadd(sM[wid][sy * D + c][lane], sRes[wid][k][c][lane]);
-            sM[wid][(sy + 1) * D + c][lane] =
-                dadd(sM[wid][(sy + 1) * D + c][lane], sRes[wid][k][D + c][lane]);
-          }
-        }
-      }
-      if (fl & (kItFlush | kItMarker)) {
-#pragma unroll
-        for (int q = 0; q < NC; ++q) {
-          acc[q] = dadd(acc[q], dmul(sM[wid][q][lane], 0.5));
-          sM[wid][q][lane] = 0.0;
-        }
-      }
-    }
-    __syncwarp();
+    for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = acc[k];
+  } else {
+    rod_update<D, NV>(P, S, i, key, pa, acc);
   }
-  if (!valid) return;
-  if (frozen) {
-    frozen_copy(P, i, key, NC);
-    return;
-  }
-  double pa[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
-  rod_update<D, NV>(P, S, i, key, pa, acc);
 }
 
 // ---------------------------------------------------------------------------------------
-// Pass-synchronous variant (default).  Each round every lane of the warp handles exactly one
-// pass -- own_a(b) or ext_a(b) for its next candidate rod b -- so the scan of the
-// NV x (NV-1) vertex/segment pairs is a uniform loop that records the FP32 survivors in a
-// bitmask; the warp then evaluates all survivors of all lanes in FP64 with every lane busy
-// (results to shared memory), and each lane folds its results into the pass matrix M in
-// (vertex, segment) order with compile-time indices and adds M / 2 to the rod force.
-// Same items, same per-item arithmetic, same order as k_rods_step: identical bits.
+// Pass-synchronous evaluation (default FP64 path).  Each round every lane of a warp handles
+// exactly one pass -- own_a(b) or ext_a(b) -- so the scan of the NV x (NV-1) vertex/segment
+// pairs is a uniform loop that records the FP32 survivors in a bitmask; the warp then
+// evaluates all survivors of all lanes in FP64 with every lane busy (results to shared
+// memory), and the pass matrix M is folded row by row in (vertex, segment) order.  Same
+// items, same per-item arithmetic, same order as k_rods_step: identical bits.
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ int nth_set_bit64(uint64_t m, int n) {  // n-th set bit (0-based)
   const uint32_t lo = (uint32_t)m;
   const int clo = __popc(lo);
   if (n < clo) return (int)__fns(lo, 0, n + 1);
   return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - clo + 1);
-}
-
-// One warp-wide pass step.  Every lane brings one pass (own_a(b) or ext_a(b) of its rod a
-// and candidate b; is_ext says which) with the bitmask of its FP32-surviving vertex/segment
-// pairs.  The warp evaluates all survivors in FP64 with every lane busy (results to shared
-// memory), folds them into the rows of each lane's pass matrix M in the reference's
-// (vertex, segment) order -- each non-empty (lane, row) is one unit of work -- and each lane
-// adds M / 2 to acc.  Lanes without a pass bring mask = 0.
-template <int D, int NV>
-__device__ __forceinline__ void eval_fold_pass(const PackArgs &P, double *sRes, int lane,
-                                               uint64_t mask, bool is_ext, uint32_t a,
-                                               uint32_t b, uint32_t sim, double *acc) {
-  constexpr int NE = NV - 1, NP = NV * NE, R = D + 1;
-  double *sRow = sRes + NP * R * 32;  // [NV][D][32]: folded rows of the pass matrix
-  const int64_t cap = P.cap;
-  const int cnt = __popcll(mask);
-
-  // ---- evaluate every survivor of the warp in FP64 ---------------------------------
-  int incl = cnt;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, incl, off);
-    if (lane >= off) incl += y;
-  }
-  const int excl = incl - cnt;
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
-  for (int base = 0; base < total; base += 32) {
-    const int j = base + lane;
-    int l = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-      const int cand = l + step;
-      const int e = __shfl_sync(0xffffffffu, excl, cand & 31);
-      if (cand < 32 && e <= j) l = cand;
-    }
-    const int ex_l = __shfl_sync(0xffffffffu, excl, l);
-    const uint32_t sim_l = __shfl_sync(0xffffffffu, sim, l);
-    const uint32_t b_l = __shfl_sync(0xffffffffu, b, l);
-    const uint32_t a_l = __shfl_sync(0xffffffffu, a, l);
-    const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
-    const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
-    const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
-    if (j < total) {
-      const int k = j - ex_l;
-      const int vs = nth_set_bit64(((uint64_t)mhi << 32) | mlo, k);
-      const int vx = vs / NE, sy = vs - vx * NE;
-      const uint32_t pr = ext_l ? b_l : a_l, sr = ext_l ? a_l : b_l;
-      double p[D], l0[D], l1[D], q[D], t, f[D];
-#pragma unroll
-      for (int c = 0; c < D; ++c) {
-        p[c] = P.pos[(vx * D + c) * cap + pr];
-        l0[c] = P.pos[(sy * D + c) * cap + sr];
-        l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
-      }
-      nearest_point_f64<D>(p, l0, l1, q, t);
-      if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
-#pragma unroll
-        for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
-      }
-#pragma unroll
-      for (int c = 0; c < D; ++c) sRes[(k * R + c) * 32 + l] = f[c];
-      sRes[(k * R + D) * 32 + l] = t;
-    }
-  }
-  __syncwarp();
-
-  // ---- fold the results row by row: each non-empty (rod, row) is one unit ----------
-  // Row r of the pass matrix M collects, in the reference's (vertex, segment) order,
-  //   own pass: f of items (r, 0..NE-1);
-  //   ext pass: for each vertex vx, -f*t of item (vx, r-1) then -f*(1-t) of item (vx, r).
-  uint32_t rowmask = 0;
-#pragma unroll
-  for (int r = 0; r < NV; ++r) {
-    bool has = false;
-    if (!is_ext) {
-      has = ((mask >> (r * NE)) & ((1ull << NE) - 1ull)) != 0ull;
-    } else {
-#pragma unroll
-      for (int vx = 0; vx < NV; ++vx) {
-        if (r >= 1) has |= ((mask >> (vx * NE + r - 1)) & 1ull) != 0ull;
-        if (r < NE) has |= ((mask >> (vx * NE + r)) & 1ull) != 0ull;
-      }
-    }
-    if (has) rowmask |= 1u << r;
-  }
-  const int rcnt = __popc(rowmask);
-  int rincl = rcnt;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, rincl, off);
-    if (lane >= off) rincl += y;
-  }
-  const int rexcl = rincl - rcnt;
-  const int rtotal = __shfl_sync(0xffffffffu, rincl, 31);
-  for (int base = 0; base < rtotal; base += 32) {
-    const int j = base + lane;
-    int l = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-      const int cand = l + step;
-      const int e = __shfl_sync(0xffffffffu, rexcl, cand & 31);
-      if (cand < 32 && e <= j) l = cand;
-    }
-    const int ex_l = __shfl_sync(0xffffffffu, rexcl, l);
-    const uint32_t rows_l = __shfl_sync(0xffffffffu, rowmask, l);
-    const bool ext_l = __shfl_sync(0xffffffffu, (int)is_ext, l) != 0;
-    const uint32_t mlo = __shfl_sync(0xffffffffu, (uint32_t)mask, l);
-    const uint32_t mhi = __shfl_sync(0xffffffffu, (uint32_t)(mask >> 32), l);
-    if (j < rtotal) {
-      const uint64_t m_l = ((uint64_t)mhi << 32) | mlo;
-      const int r = (int)__fns(rows_l, 0, j - ex_l + 1);
-      double m[D];
-#pragma unroll
-      for (int c = 0; c < D; ++c) m[c] = 0.0;
-      if (!ext_l) {
-#pragma unroll
-        for (int sy = 0; sy < NE; ++sy) {
-          const int vs = r * NE + sy;
-          if (!((m_l >> vs) & 1ull)) continue;
-          const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
-#pragma unroll
-          for (int c = 0; c < D; ++c) m[c] = dadd(m[c], sRes[(slot * R + c) * 32 + l]);
-        }
-      } else {
-#pragma unroll
-        for (int vx = 0; vx < NV; ++vx) {
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int sy = r - 1 + h;  // h = 0: item (vx, r-1) weight t; h = 1: (vx, r) weight 1-t
-            if (sy < 0 || sy >= NE) continue;
-            const int vs = vx * NE + sy;
-            if (!((m_l >> vs) & 1ull)) continue;
-            const int slot = __popcll(m_l & ((1ull << vs) - 1ull));
-            const double t = sRes[(slot * R + D) * 32 + l];
-            const double wgt = h == 0 ? t : dsub(1.0, t);
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-              const double fe = -sRes[(slot * R + c) * 32 + l];
-              m[c] = dadd(m[c], dmul(fe, wgt));
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < D; ++c) sRow[(r * D + c) * 32 + l] = m[c];
-    }
-  }
-  __syncwarp();
-  // acc += M / 2 for the rows this lane's pass touched (other rows of M are zero)
-#pragma unroll
-  for (int r = 0; r < NV; ++r)
-    if ((rowmask >> r) & 1u) {
-#pragma unroll
-      for (int c = 0; c < D; ++c)
-        acc[r * D + c] = dadd(acc[r * D + c], dmul(sRow[(r * D + c) * 32 + lane], 0.5));
-    }
-  __syncwarp();
 }
 
 // 0.0 + x, exactly: x itself except that -0.0 becomes +0.0.
@@ -1029,12 +614,6 @@ struct FoldScratch {
 };
 
 template <int D, int NV>
-constexpr size_t queue_smem_bytes() {  // k_rods_queue: results, accumulators, fold scratch
-  return sizeof(double) * ((size_t)2 * D * kQueueCap + (size_t)NV * D * 32) +
-         sizeof(FoldScratch);
-}
-
-template <int D, int NV>
 constexpr size_t passq_smem_bytes() {  // k_rods_passq: results, fold scratch
   return sizeof(double) * (size_t)2 * D * kQueueCap + sizeof(FoldScratch);
 }
@@ -1053,13 +632,14 @@ __device__ __forceinline__ uint32_t ext_row_bits(uint64_t mask, int r) {
   return em;
 }
 
-// The pass step of k_rods_queue.  Like eval_fold_pass, but
-//  * results go to a compacted buffer sRes [2D][kQueueCap] in chunks of whole lanes;
-//    an item stores f (own pass) or -f*t (ext pass) in the first D entries and -f*(1-t) in
-//    the last D, so the weights are applied while all lanes evaluate;
-//  * a (lane, row) unit sums only its own items (loops over set bits) and adds M / 2 to the
-//    lane's accumulator sAcc [NC][32] itself.
-// Per row the sums run over the same items in the same order as eval_fold_pass.
+// One warp-wide pass step of k_rods_passq.  Every lane brings one pass (own_a(b) or ext_a(b)
+// of its rod a and candidate b; is_ext says which) with the bitmask of its FP32-surviving
+// vertex/segment pairs.  The warp evaluates the survivors in FP64 with every lane busy into
+// a compacted buffer sRes [2D][kQueueCap], in chunks of whole lanes: an item stores f (own
+// pass) or -f*t (ext pass) in the first D entries and -f*(1-t) in the last D, so the weights
+// are applied while all lanes evaluate.  Then each non-empty (lane, row) of the pass matrix
+// M is one unit that sums its own items in the reference's (vertex, segment) order, and the
+// pass's M / 2 goes to its slot of mbuf (rows without items: +0).  sAcc is unused.
 template <int D, int NV, bool STORE>
 __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes, double *sAcc,
                                                 FoldScratch &F, int lane, uint64_t mask,
@@ -1242,18 +822,12 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
 #pragma unroll
       for (int c = 0; c < D; ++c) m[c] = plus_zero(sRes[(h * D + c) * CAP + slot]);
     };
-    // unit done: M / 2 to the pass's slot (STORE: 0 + M / 2) or added to the lane's rod
+    // unit done: 0 + M / 2 to the pass's slot
     auto finish_unit = [&]() {
+      (void)sAcc;
 #pragma unroll
-      for (int c = 0; c < D; ++c) {
-        const double hm = half_exact(m[c]);
-        if (STORE) {
-          P.mbuf[(r * D + c) * P.pass_cap + F.tpass[l]] = plus_zero(hm);
-        } else {
-          double &acc = sAcc[(r * D + c) * 32 + F.phys[l]];
-          acc = dadd(acc, hm);
-        }
-      }
+      for (int c = 0; c < D; ++c)
+        P.mbuf[(r * D + c) * P.pass_cap + F.tpass[l]] = plus_zero(half_exact(m[c]));
       ++k_unit;
       p = 32 * k_unit + ((k_unit & 1) ? 31 - lane : lane);
       act = p < n_units;
@@ -1276,344 +850,9 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
   }
 }
 
-template <int D, int NV>
-__global__ void __launch_bounds__(32) k_rods_pass(const PackArgs P) {
-  constexpr int NC = NV * D, NE = NV - 1;
-  extern __shared__ double sRes[];  // [NP][D + 1][32] item results, then [NV][D][32] rows
-  const int lane = threadIdx.x;
-  const uint32_t warp_base = blockIdx.x * 32;
-  const uint32_t i = warp_base + lane;
-  const bool valid = i < P.n_agents;
-  const int64_t cap = P.cap;
-  const uint32_t ii = valid ? i : 0u;
-  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
-  const SimDev &S = P.sims[sim];
-  uint32_t key = P.key[ii];
-  if (key - S.voxel_off >= S.n_vox) {
-    if (valid) invariant_failed(P.status, kSiteForceKey, i);
-    key = S.voxel_off;
-  }
-  const uint32_t v = key - S.voxel_off;
-  int idx[D];
-  unravel<D>(S, v, idx);
-  float oa[NC];
-  float amin[D], amax[D];
-  bool a_nan = false;
-#pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    oa[k] = P.off[k * cap + ii];
-    a_nan |= !(oa[k] == oa[k]);
-    if (k < D) {
-      amin[k] = oa[k];
-      amax[k] = oa[k];
-    } else {
-      amin[k % D] = fminf(amin[k % D], oa[k]);
-      amax[k % D] = fmaxf(amax[k % D], oa[k]);
-    }
-  }
-  const uint32_t sub_v = subdomain_of(S, v);
-  const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
-  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
-  double acc[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) acc[k] = 0.0;
-  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
-    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
-    nb[c] = hi - lo[c] + 1;
-  }
-  const int n_box = nb[0] * nb[1] * nb[2];
-  // cursor
-  const bool frozen = valid && sim_frozen(P, S);
-  bool done = !valid || frozen;
-  int o_box = 0;
-  uint32_t b_next = 0, b_end = 0, cur_b = 0;
-  bool same = false, twice = false, ext_first = false;
-  int n_pass = 0, pass = 0;  // passes of the current candidate / index of the next one
-  float kd[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) kd[c] = 0.f;
-
-  while (__any_sync(0xffffffffu, !done)) {
-    // ---- next pass of this lane: advance to the next non-far candidate if needed -------
-    while (!done && pass >= n_pass) {
-      if (b_next >= b_end) {
-        if (o_box >= n_box) {
-          done = true;
-          break;
-        }
-        const int j2 = lo[2] + o_box % nb[2];
-        const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
-        const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
-        ++o_box;
-        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
-                                    : (uint32_t)j0 * S.nvox[1] + j1;
-        same = (w == v);
-        twice = same || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
-        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
-        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        b_next = P.start[S.voxel_off + w];
-        b_end = P.start[S.voxel_off + w + 1];
-        if (b_next > b_end || b_end > P.n_agents) {
-          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-          b_end = b_next;
-        }
-        continue;
-      }
-      const uint32_t b = b_next++;
-      if (b == i) continue;
-      float bmin[D], bmax[D];
-      bool b_nan = false;
-#pragma unroll
-      for (int k = 0; k < NC; ++k) {
-        const float o = P.off[k * cap + b] + kd[k % D];
-        b_nan |= !(o == o);
-        if (k < D) {
-          bmin[k] = o;
-          bmax[k] = o;
-        } else {
-          bmin[k % D] = fminf(bmin[k % D], o);
-          bmax[k % D] = fmaxf(bmax[k % D], o);
-        }
-      }
-      bool far = false;
-      if (!a_nan && !b_nan) {
-#pragma unroll
-        for (int c = 0; c < D; ++c) far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
-      }
-      if (far) continue;
-      cur_b = b;
-      ext_first = same && (b < i);
-      n_pass = twice ? 2 : 1;
-      pass = 0;
-    }
-    const bool active = !done;
-    const bool is_ext = active && ((pass == 0) == ext_first);
-    ++pass;
-
-    // ---- scan the vertex/segment pairs of this pass (uniform loop) -------------------
-    uint64_t mask = 0;
-    if (active) {
-      float ob[NC];
-#pragma unroll
-      for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + cur_b] + kd[k % D];
-#pragma unroll
-      for (int vx = 0; vx < NV; ++vx)
-#pragma unroll
-        for (int sy = 0; sy < NE; ++sy) {
-          const float *pp = is_ext ? &ob[vx * D] : &oa[vx * D];
-          const float *s0 = is_ext ? &oa[sy * D] : &ob[sy * D];
-          const float *s1 = is_ext ? &oa[(sy + 1) * D] : &ob[(sy + 1) * D];
-          float p32[D], l0[D], l1[D];
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            p32[c] = pp[c];
-            l0[c] = s0[c];
-            l1[c] = s1[c];
-          }
-          if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
-        }
-    }
-    eval_fold_pass<D, NV>(P, sRes, lane, mask, is_ext, i, cur_b, sim, acc);
-  }
-  if (!valid) return;
-  if (frozen) {
-    frozen_copy(P, i, key, NC);
-    return;
-  }
-  double pa[NC];
-#pragma unroll
-  for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
-  rod_update<D, NV>(P, S, i, key, pa, acc);
-}
-
-// ---------------------------------------------------------------------------------------
-// Queue-fed pass-synchronous variant (default).  The per-pass work is that of k_rods_pass,
-// but a lane whose rod has no passes left stores the rod's interaction force to frc and
-// takes the next rod from a global counter (one atomic per warp and refill), so every lane
-// of a warp carries a pass until the queue drains instead of idling while the busiest rod of
-// a fixed group of 32 finishes.  The grid is sized to the resident warps of the device.
-// k_rods_update then applies mechanics, solver, boundary and next key per rod.  Per rod the
-// items, their arithmetic and their order are those of k_rods_step: identical bits.
-// ---------------------------------------------------------------------------------------
-template <int D, int NV>
-__global__ void __launch_bounds__(32) k_rods_queue(const PackArgs P) {
-  constexpr int NC = NV * D, NE = NV - 1;
-  if (!P.rctl[3]) return;  // the pass list fitted: k_rods_passq computed this step
-  extern __shared__ double sRes[];             // [2D][kQueueCap]: item results
-  double *sAcc = sRes + 2 * D * kQueueCap;     // [NC][32]: force accumulated on each lane's rod
-  FoldScratch &F = *reinterpret_cast<FoldScratch *>(sAcc + NC * 32);
-  const int lane = threadIdx.x;
-  const int64_t cap = P.cap;
-  const float inf = __int_as_float(0x7f800000);
-  // the rod of this lane and its candidate cursor
-  bool have = false, drained = false;
-  uint32_t i = 0, sim = 0, v = 0, sub_v = 0;
-  const SimDev *S = P.sims;
-  int idx[D];
-  float oa[NC], amin[D], amax[D];
-  bool a_nan = false;
-  float thr2 = inf, thr = inf;
-  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
-  int n_box = 0, o_box = 0;
-  uint32_t b_next = 0, b_end = 0, cur_b = 0;
-  bool same = false, twice = false, ext_first = false;
-  int n_pass = 0, pass = 0;
-  float kd[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    idx[c] = 0;
-    kd[c] = 0.f;
-  }
-
-  while (true) {
-    // ---- give every lane its next pass, refilling finished lanes from the queue -------
-    while (true) {
-      while (have && pass >= n_pass) {
-        if (b_next >= b_end) {
-          if (o_box >= n_box) {  // rod finished: hand its force to the update kernel
-#pragma unroll
-            for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = sAcc[k * 32 + lane];
-            have = false;
-            break;
-          }
-          const int j2 = lo[2] + o_box % nb[2];
-          const int j1 = lo[1] + (o_box / nb[2]) % nb[1];
-          const int j0 = lo[0] + o_box / (nb[1] * nb[2]);
-          ++o_box;
-          const uint32_t w = (D == 3) ? ((uint32_t)j0 * S->nvox[1] + j1) * S->nvox[2] + j2
-                                      : (uint32_t)j0 * S->nvox[1] + j1;
-          same = (w == v);
-          twice = same || S->weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(*S, w) != sub_v;
-          kd[0] = (float)(j0 - idx[0]) * S->dxf[0];
-          kd[1] = (float)(j1 - idx[1]) * S->dxf[1];
-          if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S->dxf[D - 1];
-          b_next = P.start[S->voxel_off + w];
-          b_end = P.start[S->voxel_off + w + 1];
-          if (b_next > b_end || b_end > P.n_agents) {
-            invariant_failed(P.status, kSiteForceRange, S->voxel_off + w);
-            b_end = b_next;
-          }
-          continue;
-        }
-        const uint32_t b = b_next++;
-        if (b == i) continue;
-        float bmin[D], bmax[D];
-        bool b_nan = false;
-#pragma unroll
-        for (int k = 0; k < NC; ++k) {
-          const float o = P.off[k * cap + b] + kd[k % D];
-          b_nan |= !(o == o);
-          if (k < D) {
-            bmin[k] = o;
-            bmax[k] = o;
-          } else {
-            bmin[k % D] = fminf(bmin[k % D], o);
-            bmax[k % D] = fmaxf(bmax[k % D], o);
-          }
-        }
-        bool far = false;
-        if (!a_nan && !b_nan) {
-#pragma unroll
-          for (int c = 0; c < D; ++c)
-            far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
-        }
-        if (far) continue;
-        cur_b = b;
-        ext_first = same && (b < i);
-        n_pass = twice ? 2 : 1;
-        pass = 0;
-      }
-      const bool need = !have && !drained;
-      const uint32_t want = __ballot_sync(0xffffffffu, need);
-      if (!want) break;
-      const int leader = __ffs(want) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(&P.rctl[2], (uint32_t)__popc(want));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if (need) {
-        const uint32_t t = base + (uint32_t)__popc(want & ((1u << lane) - 1u));
-        if (t >= P.n_agents) {
-          drained = true;
-        } else {
-          i = t;
-          sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
-          S = P.sims + sim;
-          if (!sim_frozen(P, *S)) {  // frozen rods are copied by the update kernel
-            uint32_t key = P.key[i];
-            if (key - S->voxel_off >= S->n_vox) {
-              invariant_failed(P.status, kSiteForceKey, i);
-              key = S->voxel_off;
-            }
-            v = key - S->voxel_off;
-            unravel<D>(*S, v, idx);
-            a_nan = false;
-#pragma unroll
-            for (int k = 0; k < NC; ++k) {
-              oa[k] = P.off[k * cap + i];
-              a_nan |= !(oa[k] == oa[k]);
-              if (k < D) {
-                amin[k] = oa[k];
-                amax[k] = oa[k];
-              } else {
-                amin[k % D] = fminf(amin[k % D], oa[k]);
-                amax[k % D] = fmaxf(amax[k % D], oa[k]);
-              }
-            }
-            sub_v = subdomain_of(*S, v);
-            thr2 = P.prefilter ? S->filt_thr2 : inf;
-            thr = P.prefilter ? sqrtf(S->filt_thr2) : inf;
-#pragma unroll
-            for (int k = 0; k < NC; ++k) sAcc[k * 32 + lane] = 0.0;
-#pragma unroll
-            for (int c = 0; c < D; ++c) {
-              lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
-              const int hi = idx[c] + 1 < S->nvox[c] ? idx[c] + 1 : S->nvox[c] - 1;
-              nb[c] = hi - lo[c] + 1;
-            }
-            n_box = nb[0] * nb[1] * nb[2];
-            o_box = 0;
-            b_next = b_end = 0;
-            n_pass = pass = 0;
-            have = true;
-          }
-        }
-      }
-    }
-    if (!__any_sync(0xffffffffu, have)) break;
-    const bool is_ext = have && ((pass == 0) == ext_first);
-    ++pass;
-
-    // ---- scan the vertex/segment pairs of this pass (uniform loop) -------------------
-    uint64_t mask = 0;
-    if (have) {
-      float ob[NC];
-#pragma unroll
-      for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + cur_b] + kd[k % D];
-#pragma unroll
-      for (int vx = 0; vx < NV; ++vx)
-#pragma unroll
-        for (int sy = 0; sy < NE; ++sy) {
-          const float *pp = is_ext ? &ob[vx * D] : &oa[vx * D];
-          const float *s0 = is_ext ? &oa[sy * D] : &ob[sy * D];
-          const float *s1 = is_ext ? &oa[(sy + 1) * D] : &ob[(sy + 1) * D];
-          float p32[D], l0[D], l1[D];
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            p32[c] = pp[c];
-            l0[c] = s0[c];
-            l1[c] = s1[c];
-          }
-          if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2)) mask |= 1ull << (vx * NE + sy);
-        }
-    }
-    eval_fold_queue<D, NV, false>(P, sRes, sAcc, F, lane, mask, is_ext, i, cur_b, sim, 0u,
-                                  false);
-  }
-}
+// pass_meta bit 7: an ext pass of chili's step 3, summed with the other such passes of the
+// same neighbour box before the sum is added to the rod's force.
+constexpr uint32_t kPassGroup = 0x80u;
 
 // ---------------------------------------------------------------------------------------
 // Pass list of the default rod path.  For every rod, in the order k_rods_step visits them:
@@ -1667,59 +906,66 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
     nb[c] = hi - lo[c] + 1;
   }
   const int n_box = nb[0] * nb[1] * nb[2];
-  // visit(b, meta) for every pass of rod i, in order
+  const bool physical = S.weight_mode == CRG_WEIGHTS_PHYSICAL;
+  // visit(b, meta) for every pass of rod i, in the order of k_rods_step: phase 0 the boxes of
+  // the rod's subdomain, phase 1 the own halves of the other boxes, phase 2 their ext halves,
+  // which are marked (kPassGroup) so that k_rods_update sums each box's ones before adding
   auto walk = [&](auto &&visit) {
-    for (int o = 0; o < n_box; ++o) {
-      const int j2 = lo[2] + o % nb[2];
-      const int j1 = lo[1] + (o / nb[2]) % nb[1];
-      const int j0 = lo[0] + o / (nb[1] * nb[2]);
-      const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
-                                  : (uint32_t)j0 * S.nvox[1] + j1;
-      const bool same = (w == v);
-      const bool twice =
-          same || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
-      const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};
-      float kd[D];
+    for (int phase = 0; phase < 3; ++phase)
+      for (int o = 0; o < n_box; ++o) {
+        const int j2 = lo[2] + o % nb[2];
+        const int j1 = lo[1] + (o / nb[2]) % nb[1];
+        const int j0 = lo[0] + o / (nb[1] * nb[2]);
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool same = (w == v);
+        const bool local = physical || subdomain_of(S, w) == sub_v;
+        if (local != (phase == 0)) continue;
+        const bool twice = phase == 0 && (same || physical);
+        const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};
+        float kd[D];
 #pragma unroll
-      for (int c = 0; c < D; ++c) kd[c] = (float)dj[c] * S.dxf[c];
-      const uint32_t box = (uint32_t)((dj[0] + 1) | ((dj[1] + 1) << 2) | ((dj[2] + 1) << 4));
-      uint32_t b = P.start[S.voxel_off + w], b_end = P.start[S.voxel_off + w + 1];
-      if (b > b_end || b_end > P.n_agents) {
-        invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-        b_end = b;
-      }
-      for (; b < b_end; ++b) {
-        if (b == i) continue;
-        float bmin[D], bmax[D];
-        bool b_nan = false;
+        for (int c = 0; c < D; ++c) kd[c] = (float)dj[c] * S.dxf[c];
+        const uint32_t box = (uint32_t)((dj[0] + 1) | ((dj[1] + 1) << 2) | ((dj[2] + 1) << 4));
+        uint32_t b = P.start[S.voxel_off + w], b_end = P.start[S.voxel_off + w + 1];
+        if (b > b_end || b_end > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b_end = b;
+        }
+        for (; b < b_end; ++b) {
+          if (b == i) continue;
+          float bmin[D], bmax[D];
+          bool b_nan = false;
 #pragma unroll
-        for (int k = 0; k < NC; ++k) {
-          const float o2 = P.off[k * cap + b] + kd[k % D];
-          b_nan |= !(o2 == o2);
-          if (k < D) {
-            bmin[k] = o2;
-            bmax[k] = o2;
+          for (int k = 0; k < NC; ++k) {
+            const float o2 = P.off[k * cap + b] + kd[k % D];
+            b_nan |= !(o2 == o2);
+            if (k < D) {
+              bmin[k] = o2;
+              bmax[k] = o2;
+            } else {
+              bmin[k % D] = fminf(bmin[k % D], o2);
+              bmax[k % D] = fmaxf(bmax[k % D], o2);
+            }
+          }
+          bool far = false;
+          if (!a_nan && !b_nan) {
+#pragma unroll
+            for (int c = 0; c < D; ++c)
+              far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+          }
+          if (far) continue;
+          if (phase == 2) {
+            visit(b, (box << 1) | 1u | kPassGroup);  // step 3: ext_a(b), summed per box
+          } else if (!twice) {
+            visit(b, box << 1);  // own_a(b) only: a neighbour voxel, or step 2
           } else {
-            bmin[k % D] = fminf(bmin[k % D], o2);
-            bmax[k % D] = fmaxf(bmax[k % D], o2);
+            const uint32_t ext_first = (same && b < i) ? 1u : 0u;
+            visit(b, (box << 1) | ext_first);
+            visit(b, (box << 1) | (ext_first ^ 1u));
           }
         }
-        bool far = false;
-        if (!a_nan && !b_nan) {
-#pragma unroll
-          for (int c = 0; c < D; ++c)
-            far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
-        }
-        if (far) continue;
-        if (!twice) {
-          visit(b, box << 1);  // own_a(b) only: weight 1/2
-        } else {
-          const uint32_t ext_first = (same && b < i) ? 1u : 0u;
-          visit(b, (box << 1) | ext_first);
-          visit(b, (box << 1) | (ext_first ^ 1u));
-        }
       }
-    }
   };
   uint32_t count = 0;
   if (live) walk([&](uint32_t, uint32_t) { ++count; });
@@ -1849,9 +1095,9 @@ __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
 }
 
 // Mechanics, solver, boundary and next key of every rod from its interaction force -- the
-// in-order sum of its passes' M / 2 in mbuf, or after a pass list overflow the force
-// k_rods_queue stored in frc -- and its curvature forces in bend.  Frozen simulations copy
-// their state.
+// in-order sum of its passes' M / 2 in mbuf, or after a pass list overflow the force the
+// thread-per-rod kernel stored in frc -- and its curvature forces in bend.  Frozen
+// simulations copy their state.
 template <int D, int NV, int CYC>
 __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   constexpr int NC = NV * D;
@@ -1874,15 +1120,42 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
     for (int k = 0; k < NC; ++k) acc[k] = P.frc[k * cap + i];
   } else {
     // the sum, in pass order, of the M / 2 that k_rods_passq stored for its passes (rows a
-    // pass does not touch are +0, which leaves the sum unchanged since it is never -0)
+    // pass does not touch are +0, which leaves the sum unchanged since it is never -0);
+    // passes marked kPassGroup (they come last) are summed per neighbour box first, and each
+    // box's sum is added as one term, as chili adds a ForceInformation
 #pragma unroll
     for (int k = 0; k < NC; ++k) acc[k] = 0.0;
-    const double *mb = P.mbuf + P.pass_off[i];
+    const uint32_t p0 = P.pass_off[i];
+    const double *mb = P.mbuf + p0;
+    const uint8_t *meta = P.pass_meta + p0;
     const uint32_t n = P.npass[i];
     const int64_t pcap = P.pass_cap;
+    double g[NC];
+    uint32_t gbox = 0xffffffffu;  // box of the open group (none)
     for (uint32_t p = 0; p < n; ++p) {
+      const uint32_t m = meta[p];
+      if (!(m & kPassGroup)) {
 #pragma unroll
-      for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], mb[k * pcap + p]);
+        for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], mb[k * pcap + p]);
+        continue;
+      }
+      const uint32_t box = (m >> 1) & 0x3fu;
+      if (box != gbox) {
+        if (gbox != 0xffffffffu) {
+#pragma unroll
+          for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], g[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NC; ++k) g[k] = mb[k * pcap + p];
+        gbox = box;
+      } else {
+#pragma unroll
+        for (int k = 0; k < NC; ++k) g[k] = dadd(mb[k * pcap + p], g[k]);
+      }
+    }
+    if (gbox != 0xffffffffu) {
+#pragma unroll
+      for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], g[k]);
     }
   }
   rod_update<D, NV, true, CYC>(P, S, i, key, pa, acc);
@@ -2178,75 +1451,49 @@ __global__ void k_cycle_counters(const PackArgs P) {
   P.vctr[v] += 2ull * (uint64_t)(P.dpre[P.start[v + 1]] - P.dpre[P.start[v]]);
 }
 
-// Resident warps of k_rods_queue / k_rods_passq on the current device, [D - 2][NV]
-// (set by prepare_rods).
-unsigned g_queue_warps[2][9] = {};
+// Resident warps of k_rods_passq on the current device, [D - 2][NV] (set by prepare_rods).
 unsigned g_passq_warps[2][9] = {};
 
 template <int D, int NV>
-constexpr size_t pass_smem_bytes() {
-  return sizeof(double) * ((size_t)(NV * (NV - 1)) * (D + 1) + (size_t)NV * D) * 32;
-}
-
-template <int D, int NV>
-void launch_t(const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1) {
+void launch_t(const PackArgs &P, int precision, int block, cudaStream_t st, cudaEvent_t k0,
+              cudaEvent_t k1, cudaEvent_t k2, cudaEvent_t k3) {
   (void)block;
-  if (k0) cudaEventRecord(k0, st);
+  (void)precision;
+  auto rec = [&](cudaEvent_t e) { record_event(e, st); };
+  constexpr int B = 64;
+  const unsigned rod_grid = (P.n_agents + B - 1) / B;
   if (P.variant == 1) {  // thread-per-rod kernel
-    constexpr int B = 64;
-    const unsigned grid = (P.n_agents + B - 1) / B;
-    k_rods_step<D, NV, B><<<grid, B, 0, st>>>(P);
-    if (k1) cudaEventRecord(k1, st);
-    return;
-  }
-  if (P.variant == 2) {  // slot-queue kernel
-    constexpr int W = 2, K = 8;
-    const unsigned grid = (P.n_agents + W * 32 - 1) / (W * 32);
-    k_rods_packed<D, NV, W, K><<<grid, W * 32, 0, st>>>(P);
-    if (k1) cudaEventRecord(k1, st);
+    rec(k0);
+    k_rods_step<D, NV, B, false><<<rod_grid, B, 0, st>>>(P);
+    rec(k1);
     return;
   }
   const unsigned warps = (P.n_agents + 31) / 32;
-  if (P.variant == 3) {  // pass-synchronous kernel over fixed groups of 32 rods
-    k_rods_pass<D, NV><<<warps, 32, pass_smem_bytes<D, NV>(), st>>>(P);
-    if (k1) cudaEventRecord(k1, st);
-    return;
-  }
-  const unsigned resident = g_queue_warps[D - 2][NV];
-  const unsigned grid = (resident && resident < warps) ? resident : warps;
   const unsigned pgrid = g_passq_warps[D - 2][NV] ? g_passq_warps[D - 2][NV] : warps;
   const unsigned rblocks = (P.n_agents + 127) / 128;
   cudaMemsetAsync(P.rctl, 0, 4 * sizeof(uint32_t), st);
   k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
-  if (k0) cudaEventRecord(k0, st);
+  rec(k0);
   k_rods_passq<D, NV><<<pgrid, 32, passq_smem_bytes<D, NV>(), st>>>(P);
-  if (k1) cudaEventRecord(k1, st);
-  k_rods_queue<D, NV><<<grid, 32, queue_smem_bytes<D, NV>(), st>>>(P);  // only on overflow
+  rec(k1);
+  k_rods_step<D, NV, B, true><<<rod_grid, B, 0, st>>>(P);  // returns at once unless overflow
   if (NV > 2) {
     const uint64_t nb = ((uint64_t)P.n_agents * (NV - 2) + 127) / 128;
     k_rods_bend<D, NV><<<(unsigned)nb, 128, 0, st>>>(P);
   }
+  rec(k2);
   if (P.dflag)
     k_rods_update<D, NV, 1><<<rblocks, 128, 0, st>>>(P);
   else
     k_rods_update<D, NV, 0><<<rblocks, 128, 0, st>>>(P);
+  rec(k3);
 }
 
 template <int D, int NV>
 cudaError_t prepare_t() {
-  const int smem = (int)pass_smem_bytes<D, NV>();
-  cudaError_t e = cudaFuncSetAttribute(k_rods_pass<D, NV>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  const int qsmem = (int)queue_smem_bytes<D, NV>();
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_rods_queue<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             qsmem);
   int dev = 0, sms = 0, per_sm = 0;
-  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_queue<D, NV>, 32, qsmem);
-  if (e == cudaSuccess) g_queue_warps[D - 2][NV] = (unsigned)(sms * per_sm);
   const int psmem = (int)passq_smem_bytes<D, NV>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_rods_passq<D, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2272,16 +1519,16 @@ cudaError_t prepare_d(int nv) {
 }
 
 template <int D>
-void launch_d(int nv, const PackArgs &P, int block, cudaStream_t st, cudaEvent_t k0,
-              cudaEvent_t k1) {
+void launch_d(int nv, const PackArgs &P, int precision, int block, cudaStream_t st,
+              cudaEvent_t k0, cudaEvent_t k1, cudaEvent_t k2, cudaEvent_t k3) {
   switch (nv) {
-    case 2: launch_t<D, 2>(P, block, st, k0, k1); break;
-    case 3: launch_t<D, 3>(P, block, st, k0, k1); break;
-    case 4: launch_t<D, 4>(P, block, st, k0, k1); break;
-    case 5: launch_t<D, 5>(P, block, st, k0, k1); break;
-    case 6: launch_t<D, 6>(P, block, st, k0, k1); break;
-    case 7: launch_t<D, 7>(P, block, st, k0, k1); break;
-    case 8: launch_t<D, 8>(P, block, st, k0, k1); break;
+    case 2: launch_t<D, 2>(P, precision, block, st, k0, k1, k2, k3); break;
+    case 3: launch_t<D, 3>(P, precision, block, st, k0, k1, k2, k3); break;
+    case 4: launch_t<D, 4>(P, precision, block, st, k0, k1, k2, k3); break;
+    case 5: launch_t<D, 5>(P, precision, block, st, k0, k1, k2, k3); break;
+    case 6: launch_t<D, 6>(P, precision, block, st, k0, k1, k2, k3); break;
+    case 7: launch_t<D, 7>(P, precision, block, st, k0, k1, k2, k3); break;
+    case 8: launch_t<D, 8>(P, precision, block, st, k0, k1, k2, k3); break;
     default: break;
   }
 }
@@ -2294,14 +1541,14 @@ int prepare_rods(int dim, int nv) {
 }
 
 void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int block,
-                      cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1) {
-  (void)precision;  // rods run the FP64 path
+                      cudaStream_t st, cudaEvent_t k0, cudaEvent_t k1, cudaEvent_t k2,
+                      cudaEvent_t k3) {
   if (!P.n_agents) return;
   if (block <= 0 || block > 128) block = 64;
   if (dim == 3)
-    launch_d<3>(nv, P, block, st, k0, k1);
+    launch_d<3>(nv, P, precision, block, st, k0, k1, k2, k3);
   else
-    launch_d<2>(nv, P, block, st, k0, k1);
+    launch_d<2>(nv, P, precision, block, st, k0, k1, k2, k3);
 }
 
 template <int D>

@@ -263,10 +263,10 @@ class Simulation:
         return {"variant": v.value, "block": b.value, "ms_per_step": ms.value}
 
     def profile(self):
-        out = (C.c_double * 4)()
+        out = (C.c_double * 5)()
         N.check(self._L.crg_profile(self._h, out), "crg_profile")
         return {"force_ms": out[0], "sort_ms": out[1], "kernels": int(out[2]),
-                "kernel_ms": out[3]}
+                "kernel_ms": out[3], "update_ms": out[4]}
 
 
 def measure_fma_peaks():

@@ -285,12 +285,12 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * with crg_set_option(ctx, CRG_OPT_DEBUG_FORCES, 1) before that step. */
 #define CRG_OPT_DEBUG_FORCES 5
 /* Force kernel: 0 (default) automatic; 1 one thread per agent (the simple reference
- * formulation).  Rods: 0 = pass list (walk, pass kernel, bend, update), 2 warp-packed with
- * per-lane slot queues, 3 warp-packed over fixed groups of 32 rods.  FP64 spheres: 0 = warp
- * per agent up to 38,912 agents, lane per agent above; 2 warp per agent; 3 lane per agent
- * (warp-packed survivors; CRG_OPT_BLOCK 64 scans 64 candidates per lane and round instead
- * of 32).  Mixed spheres: 3 lane per agent (warp-packed survivors), else one thread per
- * agent.  All variants of one precision produce identical results. */
+ * formulation).  Rods: 0 = pass list (walk, pass kernel, bend, update), 1 thread per rod
+ * (also the pass list's overflow fallback).  FP64 spheres: 0 = agent groups up to 38,912
+ * agents, lane per agent above; 2 agent groups; 3 lane per agent (warp-packed survivors;
+ * CRG_OPT_BLOCK 64 scans 64 candidates per lane and round instead of 32).  Mixed spheres:
+ * 3 lane per agent (warp-packed survivors), else one thread per agent.  All variants of one
+ * precision produce identical results. */
 #define CRG_OPT_KERNEL_VARIANT 6
 /* Rods, default kernel: capacity of the pass list in passes (one pass = one candidate pair
  * half, about 11 per rod in a dense 2D colony).  A step whose list does not fit computes its
@@ -308,10 +308,12 @@ int32_t crg_debug_neighbor_stats(crg_ctx *ctx, uint32_t *n_cand, uint32_t *n_int
 
 /* Device time of the kernels of the last crg_step call, split by phase (ms):
  * [0] force+update, [1] sort; [2] number of kernels launched; [3] the dominant force
- * kernel alone (rods: the pass kernel; spheres: the force kernel).  Requires
- * CRG_OPT_PROFILE = 1 (events disable graph capture). */
+ * kernel alone (rods: the pass kernel; spheres: the force kernel); [4] the rod update
+ * kernel alone (pass-list rod path; else 0).  Requires CRG_OPT_PROFILE = 1: the steps still
+ * run from captured CUDA graphs, which then carry event nodes between the phases, and the
+ * host reads the times after every chunk of 32 steps. */
 #define CRG_OPT_PROFILE 4
-int32_t crg_profile(crg_ctx *ctx, double *out4);
+int32_t crg_profile(crg_ctx *ctx, double *out5);
 
 /* Measures the FP64 and FP32 fused-multiply-add throughput of the current device with a
  * dependent-chain microbenchmark (TFLOP/s, 2 flops per FMA). */

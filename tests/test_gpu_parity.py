@@ -224,14 +224,13 @@ def test_large_grids_many_scan_tiles(gpu, oracle):
 
 @pytest.mark.parametrize("n_sub", [1, 16])
 def test_rod_kernel_variants_bitwise_identical(gpu, n_sub):
-    """The queue-fed warp-packed rod kernel (default), the thread-per-rod kernel, the
-    slot-queue kernel and the fixed-group warp-packed kernel evaluate the same items in the
-    same order: identical bits after many steps (16 subdomains: mixed weight classes)."""
+    """The pass-list rod path (default) and the thread-per-rod kernel evaluate the same items
+    and add them in the same order: identical bits after many steps (16 subdomains: terms
+    of chili's steps 2 and 3, summed per voxel)."""
     r = W.rods_2d(seed=61, n=20_000, n_subdomains=n_sub)
     a = E.run(r, 150)
-    for variant in (1, 2, 3):
-        b = E.run(r, 150, options={N.OPT_KERNEL_VARIANT: variant})
-        assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    b = E.run(r, 150, options={N.OPT_KERNEL_VARIANT: 1})
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
 
 
 def test_rod_pass_list_overflow_falls_back_and_grows(gpu):
