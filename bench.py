@@ -9,8 +9,10 @@ workload (rods_2d) 100,000 bacterial rods x 6 vertices, 500 explicit-Euler steps
   e2e    the same run through the public C ABI with host buffers: crg_upload from pinned
          host memory, crg_step, crg_download to host, every bench step.
   cpu_baseline  the oracle (a C++ restatement of chili, multi-threaded by subdomains like
-         chili) on the host cores on a bounded sample of the same workload.
---impl reference times that CPU implementation alone, with all host threads.
+         chili) on this host's cores: all usable cores (one chili subdomain per thread) on
+         the whole timed run, and one thread on a bounded sample, with the core count and
+         CPU model of the host.  The GPU arm runs the same subdomain weight map.
+--impl reference times that CPU implementation alone, with all usable host cores.
 
 Multi-GPU: the path is replicated, not sharded (independent simulations); each rank runs
 the workload on its own GPU and rank 0 reports the sum of agent-steps over the max time.
@@ -46,6 +48,22 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the mixed-precision, ensemble and served measurements")
+    # a small run for profilers (ncu): direct launches, every kernel a separate launch
+    p.add_argument("--profile-case", action="store_true",
+                   help="run --case-steps steps of the workload with direct launches (no CUDA "
+                        "graphs), print the wall time and exit")
+    p.add_argument("--case-steps", type=int, default=10)
+    p.add_argument("--case-n", type=int, default=0, help="agents (0: the workload's size)")
+    p.add_argument("--case-subdomains", type=int, default=16)
+    p.add_argument("--case-precision", default=None, choices=[None, "f64", "mixed"])
+    p.add_argument("--case-variant", type=int, default=0, help="CRG_OPT_KERNEL_VARIANT")
+    p.add_argument("--case-workload", default=None,
+                   choices=[None, "rods_2d", "spheres_3d", "spheres_3d_large"])
+    # the served form over several arrival rates (minutes of GPU time: not in the default run)
+    p.add_argument("--served-sweep", action="store_true",
+                   help="run the request stream at --sweep-rates and print one JSON line")
+    p.add_argument("--sweep-rates", default="15,25,40,80")
+    p.add_argument("--sweep-requests", type=int, default=1000)
     return p.parse_args()
 
 
@@ -56,17 +74,58 @@ def dist_env():
     return rank, world, local
 
 
-# chili's n_threads for every arm: the number of subdomains fixes chili's pair weights, so
-# both arms and the parity tests run the same physics whatever the host's core count.
-N_SUBDOMAINS = 16
 # The rods workload is unstable under the reference's own RodMechanics: crushed rods fold
 # to angles where the tan(angle/2) curvature force diverges and the run ends with a
-# BoundaryError near step 450 (the oracle and the GPU stop at the same rod and step).
-# The timed run therefore covers the first 400 of the 500 configured steps.
+# BoundaryError near step 450 (the oracle and the GPU stop at the same rod and step,
+# tests/test_gpu_fullsize.py).  The timed run therefore covers the first 400 of the 500
+# configured steps.
 RODS_TIMED_STEPS = 400
 
 
-def make_workload(name, n_sub=N_SUBDOMAINS):
+def n_subdomains():
+    """chili's n_threads for every arm: one subdomain per usable host core, the run the CPU
+    arm makes on all cores.  The number of subdomains fixes chili's pair weights, so the GPU
+    arm runs the same weight map (the same physics) as the all-core CPU run."""
+    from cellular_raza_gb300 import workloads as W
+
+    return W.host_threads()
+
+
+def host_cpu():
+    """Processor count, usable cores and CPU model of this host (where the CPU arms run)."""
+    import platform
+
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=20).stdout
+        f = {}
+        for ln in out.splitlines():
+            if ":" in ln:
+                k, v = ln.split(":", 1)
+                f.setdefault(k.strip(), v.strip())
+        model = f.get("Model name")
+        vendor = f.get("Vendor ID")
+        if model and vendor and vendor not in model:
+            model = f"{vendor} {model}"
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as fh:
+                for ln in fh:
+                    if ln.lower().startswith("model name"):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    from cellular_raza_gb300 import workloads as W
+
+    return {"nproc": os.cpu_count(), "usable_cores": W.host_threads(),
+            "cpu_model": model or "unknown", "arch": platform.machine()}
+
+
+def make_workload(name, n_sub=None):
+    n_sub = n_subdomains() if n_sub is None else n_sub
     from cellular_raza_gb300 import workloads as W
 
     if name == "rods_2d":
@@ -151,20 +210,33 @@ def committed_traffic(kernel_key):
 
 # ----------------------------------------------------------------------------- CPU arms
 
-def cpu_run(w, n_threads, seconds, max_steps):
-    """Times the oracle on a bounded sample: steps chosen so the run takes ~`seconds`."""
+def oracle_rate(w, threads, seconds):
+    """The oracle on `threads` threads (= chili subdomains) over the first steps of the
+    workload, as many as fit in about `seconds` (all of them when they fit)."""
     import pyoracle
 
     pyoracle.build()
-    m = w.model.replace(n_subdomains=n_threads)
+    m = w.model.replace(n_subdomains=threads)
     probe = pyoracle.run(m, w.pos, w.vel, 1)["elapsed_s"]
-    steps = int(max(1, min(max_steps, seconds / max(probe, 1e-6))))
+    steps = int(max(1, min(w.n_steps, seconds / max(probe, 1e-6))))
     r = pyoracle.run(m, w.pos, w.vel, steps)
-    return {"value": w.n * steps / r["elapsed_s"], "unit": "agent-steps/s", "cores": n_threads,
-            "kind": "port",
-            "sample": f"{w.name}: {w.n} agents x {steps} of {w.n_steps} steps, "
-                      f"{n_threads} threads = {n_threads} chili subdomains "
-                      f"({r['elapsed_s']:.1f} s)"}
+    return w.n * steps / r["elapsed_s"], steps, r["elapsed_s"]
+
+
+def cpu_run(w, n_threads, seconds):
+    """CPU baseline on this host: all usable cores (one subdomain each, the GPU arm's weight
+    map) and one thread, each on a bounded sample of the same workload."""
+    host = host_cpu()
+    v_all, s_all, t_all = oracle_rate(w, n_threads, seconds)
+    v_one, s_one, t_one = oracle_rate(w, 1, seconds)
+    return {"value": v_all, "unit": "agent-steps/s", "cores": n_threads, "threads": n_threads,
+            "kind": "port", **host,
+            "sample": f"{w.name}: {w.n} agents x {s_all} of {w.n_steps} steps, {n_threads} "
+                      f"threads = {n_threads} chili subdomains ({t_all:.1f} s)",
+            "single_thread": {"value": v_one, "unit": "agent-steps/s", "threads": 1,
+                              "sample": f"{w.name}: {w.n} agents x the first {s_one} of "
+                                        f"{w.n_steps} steps, 1 thread = 1 subdomain "
+                                        f"({t_one:.1f} s)"}}
 
 
 def workload_config(w, n_subdomains, world):
@@ -181,23 +253,25 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    n_threads = N_SUBDOMAINS  # chili runs one OS thread per subdomain
+    n_threads = n_subdomains()  # chili runs one OS thread per subdomain
     w = make_workload(args.workload)
     import pyoracle
 
     pyoracle.build()
     m = w.model.replace(n_subdomains=n_threads)
     probe = pyoracle.run(m, w.pos, w.vel, 1)["elapsed_s"]
-    # each bench step is a bounded sample of the workload sized to ~8 s
-    steps = int(max(1, min(w.n_steps, 8.0 / max(probe, 1e-6))))
+    # a bench step is the whole timed run when it takes at most ~20 s on this host, else the
+    # first steps of it that do (stated in `sample`)
+    steps = int(max(1, min(w.n_steps, 20.0 / max(probe, 1e-6))))
     for _ in range(args.warmup):
         pyoracle.run(m, w.pos, w.vel, 1)
     t_total = 0.0
     for _ in range(args.steps):
         t_total += pyoracle.run(m, w.pos, w.vel, steps)["elapsed_s"]
     value = w.n * steps * args.steps / t_total
-    sample = (f"{w.name}: {w.n} agents x {steps} of {w.n_steps} steps per bench step, "
-              f"{n_threads} threads")
+    sample = (f"{w.name}: {w.n} agents x {steps} of {w.n_steps} steps per bench step "
+              f"({'the whole run' if steps == w.n_steps else 'its first steps'}), "
+              f"{n_threads} threads = {n_threads} chili subdomains")
     line = {
         "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
@@ -205,7 +279,8 @@ def reference_arm(args):
         "data": "synthetic (seeded PCG64)", "impl": "reference",
         "config": workload_config(w, n_threads, 1),
         "cpu_baseline": {"value": value, "unit": "agent-steps/s", "cores": n_threads,
-                         "kind": "port", "sample": sample},
+                         "threads": n_threads, "kind": "port", **host_cpu(),
+                         "sample": sample},
         "e2e": {"value": value, "unit": "agent-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -214,7 +289,27 @@ def reference_arm(args):
 
 # ----------------------------------------------------------------------------- GPU arm
 
-def algorithmic_flops(w, stats):
+def mean_interactions(sim, w, every):
+    """In-range pair evaluations per step averaged over the run that is timed: the neighbour
+    statistics of the state before step 1, 1 + every, ..., and after the last step
+    (trapezoidal mean), from a separate untimed pass over the same steps."""
+    import numpy as np
+
+    sim.snapshot(restore=True)
+    done, samples = 0, []
+    while True:
+        st = sim.neighbor_stats()
+        samples.append((done, float(st["n_inter"].astype(np.float64).sum())))
+        if done >= w.n_steps:
+            break
+        k = min(every, w.n_steps - done)
+        sim.step(k)
+        done += k
+    area = sum((b[0] - a[0]) * (a[1] + b[1]) / 2.0 for a, b in zip(samples, samples[1:]))
+    return area / w.n_steps, len(samples)
+
+
+def algorithmic_flops(w, n_inter):
     """FP64 work of one step's force stage once the FP32 prefilter has removed the
     evaluations beyond the cutoff (sqrt, exp, division count one flop each), as
     (whole force stage, dominant kernel).
@@ -223,7 +318,6 @@ def algorithmic_flops(w, stats):
     a.calc(a, b) (18 nearest point, 6 distance, 21 force) in the pass kernel (a lower bound:
     the ext halves of weight-1 pairs come on top) + 250 per rod (springs, curvature,
     update) in the update kernel."""
-    n_inter = float(stats["n_inter"].astype("float64").sum())
     if w.model.kind == "rod":
         return 45.0 * n_inter + 250.0 * w.n, 45.0 * n_inter
     f = 30.0 * n_inter + 21.0 * w.n
@@ -362,7 +456,7 @@ def extra_cycle(n_rods=2000, steps=600):
     from cellular_raza_gb300 import workloads as W
 
     w = W.rod_colony(n=n_rods, side=300.0 * math.sqrt(n_rods / 150.0), seed=2024,
-                     n_subdomains=N_SUBDOMAINS)
+                     n_subdomains=n_subdomains())
     with E.Simulation.single(w.model, 8 * w.n) as sim:
         sim.upload(w.pos, w.vel)
         sim.set_spring_lengths(w.spring_length)
@@ -379,7 +473,7 @@ def extra_cycle(n_rods=2000, steps=600):
             "timing": "wall clock around the crg_step calls"}
 
 
-def extra_served(n_requests=160, rate_hz=8.0):
+def served_stream(n_requests, rate_hz, seed=2024):
     """Poisson stream of simulation requests (N log-uniform [128, 262144], steps uniform
     [100, 2000], 2D/3D and FP64/mixed 50/50) through the request server (continuous batching,
     160 GB admission budget): p50/p99 submit-to-result latency and served agent-steps/s."""
@@ -387,7 +481,7 @@ def extra_served(n_requests=160, rate_hz=8.0):
     from cellular_raza_gb300 import serve as SV
     from cellular_raza_gb300 import workloads as W
 
-    reqs = W.request_stream(seed=2024, n_requests=n_requests, rate_hz=rate_hz)
+    reqs = W.request_stream(seed=seed, n_requests=n_requests, rate_hz=rate_hz)
     lat = []
     with SV.Server(hbm_budget_bytes=160 << 30, steps_per_tick=32) as srv:
         t0 = time.perf_counter()
@@ -404,11 +498,62 @@ def extra_served(n_requests=160, rate_hz=8.0):
             work += r.workload.n * r.workload.n_steps
         makespan = time.perf_counter() - t0
     lat = np.array(lat)
-    return {"workload": "request_stream", "requests": n_requests, "rate_hz": rate_hz,
+    offered = sum(r.workload.n * r.workload.n_steps for r in reqs) / reqs[-1].arrival_s
+    return {"rate_hz": rate_hz, "requests": n_requests,
             "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)),
-            "served_agent_steps_per_s": work / makespan, "makespan_s": makespan,
-            "note": f"{n_requests} of the 20,000-request stream at one rate"}
+            "mean_latency_s": float(lat.mean()),
+            "served_agent_steps_per_s": work / makespan,
+            "offered_agent_steps_per_s": offered, "makespan_s": makespan}
+
+
+def sequential_plain(n_requests, sample, seed=2024):
+    """The same request stream run one request at a time as plain FP64 simulations (one
+    handle each: upload, every step, download), timed on a sample of `sample` requests spread
+    evenly over the stream and scaled to all of them."""
+    from cellular_raza_gb300 import engine as E
+    from cellular_raza_gb300 import workloads as W
+
+    reqs = W.request_stream(seed=seed, n_requests=n_requests, rate_hz=1.0)
+    stride = max(1, len(reqs) // sample)
+    pick = reqs[::stride][:sample]
+    t_sum, work_sum = 0.0, 0
+    for r in pick:
+        w = r.workload
+        t0 = time.perf_counter()
+        E.run(W.Workload(w.name, w.model.replace(precision="f64"), w.pos, w.vel, w.n_steps))
+        t_sum += time.perf_counter() - t0
+        work_sum += w.n * w.n_steps
+    total_work = sum(r.workload.n * r.workload.n_steps for r in reqs)
+    return {"agent_steps_per_s": work_sum / t_sum,
+            "seconds_for_the_stream": t_sum * total_work / work_sum,
+            "sample": f"{len(pick)} of {n_requests} requests (every {stride}th), plain FP64, "
+                      f"wall clock per request including upload and download, scaled by "
+                      f"agent-steps"}
+
+
+def extra_served(n_requests=1000, rate_hz=40.0):
+    """The request stream at one arrival rate, beside sequential plain runs of it."""
+    out = served_stream(n_requests, rate_hz)
+    seq = sequential_plain(n_requests, 40)
+    out["sequential_plain_f64"] = seq
+    out["speedup_over_sequential"] = out["served_agent_steps_per_s"] / seq["agent_steps_per_s"]
+    out["note"] = (f"{n_requests} requests of the 20,000-request stream at {rate_hz} Hz; "
+                   "bench.py --served-sweep runs four rates")
+    return out
+
+
+def served_sweep(args):
+    """Four arrival rates x 1,000 requests of the request stream, and the sequential plain
+    comparison (one JSON line)."""
+    rates = [float(x) for x in args.sweep_rates.split(",")]
+    rows = [served_stream(args.sweep_requests, r) for r in rates]
+    seq = sequential_plain(args.sweep_requests, 60)
+    for row in rows:
+        row["speedup_over_sequential"] = row["served_agent_steps_per_s"] / seq["agent_steps_per_s"]
+    print(json.dumps({"workload": "request_stream", "sweep": rows,
+                      "sequential_plain_f64": seq, "hbm_budget_bytes": 160 << 30,
+                      "steps_per_tick": 32}), flush=True)
 
 
 def crg_arm(args):
@@ -426,12 +571,11 @@ def crg_arm(args):
     from cellular_raza_gb300 import _native as N
     from cellular_raza_gb300 import engine as E
 
-    n_cpu = N_SUBDOMAINS
-    w = make_workload(args.workload)
+    n_cpu = n_subdomains()
+    w = make_workload(args.workload, n_cpu)
     sim = E.Simulation.single(w.model, w.n)
     sim.upload(w.pos, w.vel)
     sim.snapshot()
-    stats = sim.neighbor_stats()
     ext = torch.cuda.ExternalStream(sim.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
 
@@ -506,18 +650,22 @@ def crg_arm(args):
     h2d = 2 * nbytes
     d2h = 2 * nbytes + 8 * w.n + 4 * w.n
 
-    # roofline of the dominant (force) kernel: per-launch device time with CUDA events on
-    # the library's stream, from a profiled pass over the same run
+    # Per-kernel device time from a profiled pass over the same run: the steps run from the
+    # same captured graphs, which then hold event nodes between the phases and around the
+    # dominant force kernel and the rod update kernel (CUDA events on the library's stream)
     sim.set_option(N.OPT_PROFILE, 1)
     sim.snapshot(restore=True)
-    prof_steps = min(w.n_steps, 100)
-    sim.step(prof_steps)
+    sim.step(w.n_steps)
     prof = sim.profile()
     sim.set_option(N.OPT_PROFILE, 0)
+    prof_steps = w.n_steps
     force_ms = prof["force_ms"] / prof_steps
     sort_ms = prof["sort_ms"] / prof_steps
     kernel_ms = prof["kernel_ms"] / prof_steps
-    flops, kernel_flops = algorithmic_flops(w, stats)
+    update_ms = prof["update_ms"] / prof_steps
+    # the work those steps did: in-range evaluations averaged over the same steps
+    n_inter, n_samples = mean_interactions(sim, w, every=25 if w.n_steps <= 500 else 50)
+    flops, kernel_flops = algorithmic_flops(w, n_inter)
     peaks = measured_peaks()
     fma = E.measure_fma_peaks()
     fp64_peak = fma["fp64_tflops"]
@@ -532,6 +680,9 @@ def crg_arm(args):
                 "peak_source": "measured DFMA microbenchmark (crg_measure_fma_peaks) on this GPU",
                 "kernel": kernel, "kernel_ms_per_launch": kernel_ms,
                 "algorithmic_flop_per_launch": kernel_flops,
+                "in_range_evaluations_per_step": n_inter,
+                "work_samples": f"{n_samples} states over the {w.n_steps} timed steps",
+                "timing": "CUDA event nodes in the captured step graphs, all timed steps",
                 "force_stage_ms_per_step": force_ms, "force_stage_flop_per_step": flops,
                 "force_stage_tflops": flops / (force_ms * 1e-3) / 1e12,
                 "sort_ms_per_step": sort_ms}
@@ -542,10 +693,21 @@ def crg_arm(args):
     nc = w.model.nc
     sort_bytes = w.n * (2 * 2 * 8 * nc + 2 * 8 + 4 * 4 + 4 * nc + 8 * 3)
     hbm = peaks.get("hbm_gbs")
-    roofline_sort = {"bound": "hbm", "achieved": sort_bytes / (sort_ms * 1e-3) / 1e9,
-                     "peak": hbm, "unit": "GB/s",
-                     "frac": (sort_bytes / (sort_ms * 1e-3) / 1e9 / hbm) if hbm else None,
-                     "bytes_per_step": sort_bytes}
+
+    def hbm_line(nbytes, ms):
+        gbs = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else None
+        return {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                "frac": (gbs / hbm) if (hbm and gbs) else None, "bytes_per_step": nbytes,
+                "ms_per_step": ms, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"}
+
+    roofline_sort = hbm_line(sort_bytes, sort_ms)
+    roofline_update = None
+    if w.model.kind == "rod" and update_ms > 0:
+        # k_rods_update, algorithmic bytes per rod: positions, velocities and the interaction
+        # force read, next positions and velocities written (5 x 8 x nc), key and id read and
+        # written (2 x (4 + 8))
+        roofline_update = hbm_line(w.n * (5 * 8 * nc + 2 * 12), update_ms)
+        roofline_update["kernel"] = "k_rods_update"
     gpu_launches = prof["kernels"] // prof_steps * w.n_steps * args.steps if prof_steps else None
 
     sim.close()
@@ -561,7 +723,7 @@ def crg_arm(args):
                 extras[name] = {"error": f"{type(e).__name__}: {e}"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_run(w, n_cpu, args.cpu_seconds, w.n_steps)
+        cpu = cpu_run(w, n_cpu, args.cpu_seconds)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": world,
@@ -573,6 +735,7 @@ def crg_arm(args):
                     "d2h_bytes_per_step": d2h},
             "roofline": roofline,
             "roofline_sort": roofline_sort,
+            "roofline_update": roofline_update,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": gpu_launches,
@@ -587,9 +750,38 @@ def crg_arm(args):
         dist.destroy_process_group()
 
 
+def profile_case(args):
+    """The command the ncu captures summarised under profiles/ run: the seeded workload
+    (`--case-workload`, default `--workload`) for `--case-steps` steps through the C ABI with
+    direct launches, so each kernel of a step is its own launch."""
+    from cellular_raza_gb300 import _native as N
+    from cellular_raza_gb300 import engine as E
+    from cellular_raza_gb300 import workloads as W
+
+    kw = {"n_subdomains": args.case_subdomains}
+    if args.case_n:
+        kw["n"] = args.case_n
+    if args.case_precision:
+        kw["precision"] = args.case_precision
+    w = getattr(W, args.case_workload or args.workload)(seed=2024, **kw)
+    with E.Simulation.single(w.model, w.n) as sim:
+        sim.set_option(N.OPT_GRAPH_CHUNK, 0)
+        sim.set_option(N.OPT_KERNEL_VARIANT, args.case_variant)
+        sim.upload(w.pos, w.vel)
+        t = time.perf_counter()
+        sim.step(args.case_steps)
+        sim.download()
+        print(f"{w.name}: {w.n} agents x {args.case_steps} steps in "
+              f"{time.perf_counter() - t:.3f} s")
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile_case:
+        profile_case(args)
+    elif args.served_sweep:
+        served_sweep(args)
+    elif args.impl == "reference":
         reference_arm(args)
     else:
         crg_arm(args)

@@ -25,6 +25,17 @@ import numpy as np
 DENSITY_3D = 4096 / 200.0 ** 3  # 5.12e-4 agents per unit^3
 
 
+def host_threads() -> int:
+    """Cores this process may run on: chili's n_threads for a run on all of them (one
+    subdomain per thread, chili/setup.rs:17-27), which also fixes chili's pair weights."""
+    import os
+
+    try:
+        return max(1, len(os.sched_getaffinity(0)))
+    except AttributeError:
+        return max(1, os.cpu_count() or 1)
+
+
 @dataclasses.dataclass
 class Model:
     """Domain + agent parameters of one simulation (mirrors crg_domain + crg_model)."""
