@@ -15,6 +15,7 @@
 #include <new>
 #include <vector>
 
+#include "crg_host.h"
 #include "crg_internal.cuh"
 #include "crg_kernels.h"
 
@@ -949,6 +950,45 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
   return c->err_code;
 }
 
+}  // extern "C"
+
+namespace crg {
+
+int32_t step_launch(crg_ctx *c, int64_t n_steps) {
+  if (!c || n_steps < 0 || n_steps > 256 || c->cycle || c->profile) return CRG_EINVAL;
+  if (c->err_code != CRG_OK) return c->err_code;
+  if (n_steps == 0 || c->n_agents == 0) return CRG_OK;
+  int64_t left = n_steps;
+  const int chunk = c->graph_chunk;
+  if (chunk > 0 && left >= chunk) {
+    int32_t r = ensure_graph(c, chunk);
+    if (r != CRG_OK) return r;
+    for (; left >= chunk; left -= chunk) CUDA_TRY(cudaGraphLaunch(c->gexec, c->stream));
+  }
+  for (; left > 0; --left) launch_one_step(c);
+  CUDA_TRY(cudaGetLastError());
+  return CRG_OK;
+}
+
+int32_t step_wait(crg_ctx *c, int64_t n_steps) {
+  if (!c) return CRG_EINVAL;
+  if (c->err_code != CRG_OK) return c->err_code;
+  if (n_steps == 0 || c->n_agents == 0) {
+    c->steps_done += n_steps;
+    return CRG_OK;
+  }
+  read_status(c);
+  c->steps_done += n_steps;
+  if (c->n_sims == 1 && c->err_code != CRG_OK && c->err_code != CRG_ECUDA &&
+      c->err_code != CRG_EINTERNAL && c->err_step >= 1)
+    c->steps_done = std::min(c->steps_done, c->err_step - 1);
+  return c->err_code;
+}
+
+}  // namespace crg
+
+extern "C" {
+
 int32_t crg_download(crg_ctx *c, double *pos, double *vel, uint64_t *ids, uint32_t *voxel) {
   if (!c) return CRG_EINVAL;
   const uint32_t n = c->n_agents;
@@ -1030,8 +1070,38 @@ struct CkptHeader {
   int32_t version, n_sims, nc, dim, kind, order;
   uint32_t n_agents, n_vox;
   int64_t steps_done;
+  uint64_t params;  // params_hash of the handle's domains and models
 };
 constexpr char kCkptMagic[8] = {'C', 'R', 'G', 'C', 'K', 'P', 'T', '1'};
+constexpr int32_t kCkptVersion = 3;
+
+// FNV-1a over every field of the handle's domains, models and capacities (field by field:
+// crg_model has padding bytes), so a checkpoint loads only into a handle that steps the same
+// simulations.
+uint64_t params_hash(const crg_ctx *c) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void *p, size_t n) {
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    for (size_t k = 0; k < n; ++k) h = (h ^ b[k]) * 1099511628211ull;
+  };
+  for (int s = 0; s < c->n_sims; ++s) {
+    const crg_domain &d = c->doms[s];
+    const crg_model &m = c->mods[s];
+    mix(&d.dim, 4), mix(&d.voxel_mode, 4), mix(d.min, 24), mix(d.max, 24);
+    mix(&d.interaction_range, 8), mix(d.n_voxels, 24), mix(&d.n_subdomains, 4);
+    mix(&d.weight_mode, 4);
+    mix(&m.kind, 4), mix(&m.n_vertices, 4), mix(&m.solver_order, 4), mix(&m.precision, 4);
+    const double *dv[] = {&m.mass, &m.damping, &m.spring_tension, &m.rigidity,
+                          &m.spring_length, &m.diffusion, &m.radius, &m.stiffness,
+                          &m.cutoff, &m.strength, &m.dt, &m.kb_temperature,
+                          &m.growth_rate, &m.division_length, &m.sense_range,
+                          &m.sense_saturation};
+    for (const double *x : dv) mix(x, 8);
+    mix(&m.rng_seed, 8), mix(&m.cycle, 4);
+    mix(&c->caps[s], 8);
+  }
+  return h;
+}
 
 // The checkpoint's device slices, in blob order: per array, its first n_agents entries of
 // each component (arrays are component-major with stride cap).
@@ -1077,7 +1147,8 @@ int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
   CkptHeader h;
   std::memset(&h, 0, sizeof(h));
   std::memcpy(h.magic, kCkptMagic, 8);
-  h.version = 2;
+  h.version = kCkptVersion;
+  h.params = params_hash(c);
   h.n_sims = c->n_sims;
   h.nc = c->nc;
   h.dim = c->dim;
@@ -1114,9 +1185,10 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
   const char *p = (const char *)buf;
   CkptHeader h;
   std::memcpy(&h, p, sizeof(h));
-  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 2 || h.n_sims != c->n_sims ||
-      h.nc != c->nc || h.dim != c->dim || h.kind != c->kind || h.order != c->order ||
-      h.n_vox != c->n_vox || bytes < (int64_t)ckpt_bytes(c, h.n_agents))
+  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != kCkptVersion ||
+      h.n_sims != c->n_sims || h.nc != c->nc || h.dim != c->dim || h.kind != c->kind ||
+      h.order != c->order || h.n_vox != c->n_vox || h.params != params_hash(c) ||
+      h.n_agents > (uint64_t)c->cap || bytes < (int64_t)ckpt_bytes(c, h.n_agents))
     return CRG_EINVAL;
   p += sizeof(h);
   std::vector<uint32_t> aoff(c->n_sims + 1);
@@ -1129,6 +1201,20 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
   for (int s = 0; s < c->n_sims; ++s, p += 2 * sizeof(int64_t)) {
     std::memcpy(&stops[s], p, sizeof(int64_t));
     std::memcpy(&bases[s], p + sizeof(int64_t), sizeof(int64_t));
+  }
+  // The cell starts (after the per-agent slices): they index every per-agent array, so a
+  // damaged blob must not reach the device.  start[0] = 0, non-decreasing, start[n_vox] =
+  // n_agents, and each simulation's first voxel starts at its first agent.
+  {
+    size_t slice_bytes = 0;
+    for (const CkptSlice &sl : ckpt_slices(c)) slice_bytes += sl.elem * sl.comps * h.n_agents;
+    std::vector<uint32_t> st((size_t)c->n_vox + 1);
+    std::memcpy(st.data(), p + slice_bytes, sizeof(uint32_t) * st.size());
+    if (st[0] != 0 || st[c->n_vox] != h.n_agents) return CRG_EINVAL;
+    for (uint32_t v = 0; v < c->n_vox; ++v)
+      if (st[v + 1] < st[v]) return CRG_EINVAL;
+    for (int s = 0; s < c->n_sims; ++s)
+      if (st[c->sims_h[s].voxel_off] != aoff[s]) return CRG_EINVAL;
   }
   CUDA_TRY(cudaStreamSynchronize(c->stream));
   invalidate_graph(c);

@@ -3,14 +3,18 @@
 // chili runs one simulation per run_simulation! call (cellular_raza-core-proc-macro/src/
 // run_sim.rs:411-480).  The server keeps many simulations resident on the device at once:
 //   * requests are queued on submit (inputs copied) and admitted first-come first-served
-//     while their estimated HBM footprint fits the budget;
+//     while their estimated HBM footprint fits the budget -- counting the copy of a class's
+//     running simulations that exists while its pack is rebuilt (crg_repack copies them into
+//     the new pack before the old one is freed);
 //   * admitted simulations join the pack of their class (agent kind, dimension, vertex count,
 //     precision, solver order) through crg_repack: the running simulations keep their
 //     device-resident state, the new ones are uploaded, all advance in the same launches;
 //   * each simulation gets a stop step, so it freezes exactly after its requested number of
 //     steps even in the middle of a tick; finished simulations are downloaded, their waiters
 //     woken, and they leave the pack at the next repack;
-//   * a device error raised by one simulation fails that request only.
+//   * a device error raised by one simulation fails that request only;
+//   * every class's pack has its own stream, and the launches of all packs for a tick are
+//     enqueued before the server waits for any of them, so the classes overlap on the device.
 // One background thread drives the device; submit/wait may be called from any thread.
 #include <algorithm>
 #include <chrono>
@@ -28,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/crg.h"
+#include "crg_host.h"
 
 namespace {
 
@@ -45,6 +50,7 @@ struct Request {
   std::vector<uint64_t> ids;
   double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;
   int64_t footprint = 0;
+  bool counted = false;   // footprint counted in the server's bytes in use
   int64_t remaining = 0;  // steps left at the last repack of its pack
   int32_t status = CRG_OK;
   bool done = false;
@@ -106,22 +112,33 @@ struct crg_server {
 
 namespace {
 
+// Returns r's footprint to the budget (under the server mutex): once its state has left the
+// device, i.e. when its pack dropped it or it never got into one.
+void release(crg_server *s, Request *r) {
+  if (r->counted) {
+    s->in_use -= r->footprint;
+    r->counted = false;
+  }
+}
+
 void finish(crg_server *s, Request *r, int32_t status) {
   std::lock_guard<std::mutex> lk(s->mu);
   r->status = status;
   r->done = true;
   r->t_done = now_s();
-  s->in_use -= r->footprint;
+  if (!r->in_pack) release(s, r);  // else its state stays on the device until it leaves
   s->n_active -= 1;
   s->n_completed += 1;
   s->cv_done.notify_all();
   s->cv_work.notify_all();
 }
 
-// The server thread drops r (it left its pack): free it if its waiter already collected it.
+// The server thread drops r (it left its pack): its device memory is gone; free it if its
+// waiter already collected it.
 void leave_pack(crg_server *s, Request *r) {
   std::lock_guard<std::mutex> lk(s->mu);
   r->in_pack = false;
+  release(s, r);
   if (r->collected) s->reqs.erase(r->ticket);
 }
 
@@ -197,18 +214,118 @@ int32_t repack(crg_server *s, Class &c, std::vector<Request *> &incoming) {
   return CRG_OK;
 }
 
+// Device bytes of a class's unfinished simulations: what a rebuild of its pack holds twice.
+int64_t active_bytes(const Class &c) {
+  int64_t b = 0;
+  for (const Request *r : c.sims)
+    if (!r->done) b += r->footprint;
+  return b;
+}
+
+// Advances every pack by one tick.  All packs' launches are enqueued first (each pack on its
+// own stream), then each is waited for; a device error of one simulation fails that request,
+// which is frozen (stop step 0) and leaves at the next repack.
+void tick_all(crg_server *s) {
+  struct Tick {
+    Class *c;
+    int64_t before, target;
+    int32_t rc;
+  };
+  std::vector<Tick> ticks;
+  for (auto &kv : s->classes) {
+    Class &c = kv.second;
+    if (!c.pack) continue;
+    Tick t{&c, 0, 0, CRG_OK};
+    for (Request *r : c.sims)
+      if (!r->done)
+        t.before += std::max<int64_t>(0, std::min<int64_t>(s->tick, r->remaining - c.steps_since_repack)) * r->n;
+    int64_t t_now = 0;
+    crg_step_count(c.pack, &t_now);
+    t.target = t_now + s->tick;
+    t.rc = s->tick <= 256 ? crg::step_launch(c.pack, s->tick) : CRG_EINVAL;
+    ticks.push_back(t);
+  }
+  for (Tick &t : ticks) {
+    Class &c = *t.c;
+    int64_t t_now = 0;
+    int32_t rc = t.rc == CRG_OK ? crg::step_wait(c.pack, s->tick) : CRG_OK;
+    crg_step_count(c.pack, &t_now);
+    if (t.rc != CRG_OK) {  // not launched (a tick above 256 steps): step synchronously
+      rc = crg_step(c.pack, t.target - t_now);
+      crg_step_count(c.pack, &t_now);
+    }
+    bool dead = false;
+    while (rc != CRG_OK) {
+      int32_t sim = -1;
+      const int32_t code = crg_clear_error(c.pack, &sim);
+      if (sim < 0 || sim >= (int32_t)c.sims.size() || code == CRG_ECUDA ||
+          code == CRG_EINTERNAL) {
+        s->fatal = code;  // not attributable to one simulation
+        for (Request *r : c.sims)
+          if (!r->done) finish(s, r, code);
+        dead = true;
+        break;
+      }
+      Request *bad = c.sims[sim];
+      if (!bad->done) finish(s, bad, code);
+      crg_set_sim_stop(c.pack, sim, 0);  // freeze it; it leaves at the next repack
+      if (t_now >= t.target) break;
+      rc = crg_step(c.pack, t.target - t_now);
+      crg_step_count(c.pack, &t_now);
+    }
+    if (dead) {
+      crg_destroy(c.pack);
+      c.pack = nullptr;
+      leave_all(s, c);
+      c.steps_since_repack = 0;
+      continue;
+    }
+    c.steps_since_repack += s->tick;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->agent_steps += t.before;
+    }
+    // completions
+    for (size_t k = 0; k < c.sims.size(); ++k) {
+      Request *r = c.sims[k];
+      if (r->done || c.steps_since_repack < r->remaining) continue;
+      int64_t n = 0;
+      const size_t len = (size_t)r->n * (r->pos.size() / std::max<int64_t>(r->n, 1));
+      r->pos.assign(len, 0.0);
+      r->vel.assign(len, 0.0);
+      r->ids.assign((size_t)r->n, 0);
+      int32_t rc2 = crg_sim_download(c.pack, (int32_t)k, &n, r->pos.data(), r->vel.data(),
+                                     r->ids.data());
+      finish(s, r, rc2);
+    }
+  }
+}
+
 void serve_loop(crg_server *s) {
   cudaSetDevice(s->device);
   for (;;) {
     std::vector<Request *> admitted;
     bool any_active = false;
+    // bytes each class holds that a rebuild of its pack would copy, before this tick's
+    // admissions (read on the server thread, which alone changes the packs)
+    std::map<uint64_t, int64_t> dup;
+    for (auto &kv : s->classes) dup[kv.first] = active_bytes(kv.second);
     {
       std::unique_lock<std::mutex> lk(s->mu);
       if (s->stop) break;
-      while (!s->queue.empty() && s->queue.front()->footprint <= s->budget - s->in_use) {
+      // Admit while the resident state plus the largest rebuild copy of any class fits:
+      // a class's rebuild holds its unfinished simulations twice (this tick's admissions
+      // become unfinished simulations of the next rebuild).
+      while (!s->queue.empty()) {
         Request *r = s->queue.front();
+        const uint64_t k = class_key(r->dom, r->mod);
+        int64_t worst = dup[k] + r->footprint;
+        for (auto &d : dup) worst = std::max(worst, d.second);
+        if (r->footprint + worst > s->budget - s->in_use) break;
         s->queue.pop_front();
         s->in_use += r->footprint;
+        r->counted = true;
+        dup[k] += r->footprint;
         s->n_active += 1;
         r->t_admit = now_s();
         admitted.push_back(r);
@@ -235,62 +352,7 @@ void serve_loop(crg_server *s) {
         for (Request *r : kv.second) finish(s, r, rc);
       }
     }
-    // advance every pack by one tick
-    for (auto &kv : s->classes) {
-      Class &c = kv.second;
-      if (!c.pack) continue;
-      int64_t before = 0;
-      for (Request *r : c.sims)
-        if (!r->done) before += std::max<int64_t>(0, std::min<int64_t>(s->tick, r->remaining - c.steps_since_repack)) * r->n;
-      int64_t t_now = 0;
-      crg_step_count(c.pack, &t_now);
-      const int64_t target = t_now + s->tick;
-      bool dead = false;
-      for (;;) {
-        const int32_t rc = crg_step(c.pack, target - t_now);
-        crg_step_count(c.pack, &t_now);
-        if (rc == CRG_OK) break;
-        int32_t sim = -1;
-        const int32_t code = crg_clear_error(c.pack, &sim);
-        if (sim < 0 || sim >= (int32_t)c.sims.size() || code == CRG_ECUDA ||
-            code == CRG_EINTERNAL) {
-          s->fatal = code;  // not attributable to one simulation
-          for (Request *r : c.sims)
-            if (!r->done) finish(s, r, code);
-          dead = true;
-          break;
-        }
-        Request *bad = c.sims[sim];
-        if (!bad->done) finish(s, bad, code);
-        crg_set_sim_stop(c.pack, sim, 0);  // freeze it; it leaves at the next repack
-        if (t_now >= target) break;
-      }
-      if (dead) {
-        crg_destroy(c.pack);
-        c.pack = nullptr;
-        leave_all(s, c);
-        c.steps_since_repack = 0;
-        continue;
-      }
-      c.steps_since_repack += s->tick;
-      {
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->agent_steps += before;
-      }
-      // completions
-      for (size_t k = 0; k < c.sims.size(); ++k) {
-        Request *r = c.sims[k];
-        if (r->done || c.steps_since_repack < r->remaining) continue;
-        int64_t n = 0;
-        const size_t len = (size_t)r->n * (r->pos.size() / std::max<int64_t>(r->n, 1));
-        r->pos.assign(len, 0.0);
-        r->vel.assign(len, 0.0);
-        r->ids.assign((size_t)r->n, 0);
-        int32_t rc2 = crg_sim_download(c.pack, (int32_t)k, &n, r->pos.data(), r->vel.data(),
-                                       r->ids.data());
-        finish(s, r, rc2);
-      }
-    }
+    tick_all(s);
   }
   for (auto &kv : s->classes) {
     if (kv.second.pack) crg_destroy(kv.second.pack);
@@ -329,7 +391,7 @@ int32_t crg_server_submit(crg_server *s, const crg_domain *d, const crg_model *m
   r->pos.assign(pos, pos + len);
   r->vel.assign(vel, vel + len);
   r->footprint = footprint_bytes(*d, *m, n);
-  if (r->footprint > s->budget) return CRG_ENOMEM;  // could never be admitted
+  if (2 * r->footprint > s->budget) return CRG_ENOMEM;  // could never be admitted
   r->t_submit = now_s();
   std::lock_guard<std::mutex> lk(s->mu);
   r->ticket = s->next_ticket++;

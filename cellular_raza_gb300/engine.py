@@ -245,9 +245,9 @@ class Simulation:
         capacities (crg_checkpoint_load); stepping continues bit for bit."""
         buf = C.create_string_buffer(blob, len(blob))
         N.check(self._L.crg_checkpoint_load(self._h, buf, len(blob)), "crg_checkpoint_load")
-        # per-simulation agent ranges: the uint32 offsets after the 48-byte header
+        # per-simulation agent ranges: the uint32 offsets after the 56-byte header
         n = len(self.models)
-        off = struct.unpack_from(f"<{n + 1}I", blob, 48)
+        off = struct.unpack_from(f"<{n + 1}I", blob, 56)
         self.counts = [off[s + 1] - off[s] for s in range(n)]
 
     def stream(self) -> int:

@@ -196,11 +196,15 @@ int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_
 /* ---- serving ----------------------------------------------------------------------------
  * A request server keeps many simulations resident on the device and advances them together
  * (continuous batching): requests are admitted first-come first-served while their
- * estimated device footprint fits `hbm_budget_bytes`; admitted simulations join the running
- * pack of their class (kind, dim, vertices, precision, solver order) without moving the
- * running ones off the device (crg_repack); every simulation stops exactly after its own
- * number of steps (crg_set_sim_stop); the pack advances `steps_per_tick` steps between
- * admissions.  A result is bit-identical to running the same simulation alone.
+ * estimated device footprint fits `hbm_budget_bytes`, counting the transient copy of a
+ * class's unfinished simulations that a pack rebuild holds (so the device never holds more
+ * than the budget); admitted simulations join the running pack of their class (kind, dim,
+ * vertices, precision, solver order) without moving the running ones off the device
+ * (crg_repack); every simulation stops exactly after its own number of steps
+ * (crg_set_sim_stop); the packs advance `steps_per_tick` steps between admissions, each on
+ * its own stream, all of them enqueued before the server waits for any, so different classes
+ * overlap on the device.  A result is bit-identical to running the same simulation alone.
+ * A request whose footprint exceeds half the budget is refused at submit (CRG_ENOMEM).
  * One background thread drives the device; submit/wait are thread-safe. */
 typedef struct crg_server crg_server;
 int32_t crg_server_create(int64_t hbm_budget_bytes, int32_t steps_per_tick, crg_server **out);
@@ -249,7 +253,9 @@ int32_t crg_snapshot(crg_ctx *ctx, int32_t op);
  * with the same domains, models and capacities (a fresh one, or the same one later),
  * restores the state so that stepping continues bit for bit as if it had not stopped.
  * The blob starts with a header that load checks (magic, version, kind, dimension,
- * vertices, solver order, simulation and voxel counts).  Replaces nothing in the
+ * vertices, solver order, simulation and voxel counts, and a hash of every field of the
+ * domains, models and capacities); load also checks the cell starts (monotone, from 0 to
+ * the agent count, each simulation's first voxel at its first agent) before any copy.  Replaces nothing in the
  * reference: chili's save points store cells through serde for analysis, and resuming a
  * run from them is not implemented there (cellular_raza-core/src/lib.rs:14-22). */
 int32_t crg_checkpoint_size(crg_ctx *ctx, int64_t *bytes);

@@ -76,3 +76,37 @@ def test_checkpoint_rejects_other_handles(gpu):
     with pytest.raises(N.CrgError):
         b.resume(blob[:100])
     b.close()
+
+
+def test_checkpoint_rejects_other_parameters_and_damaged_cell_starts(gpu):
+    """A blob loads only into a handle with the same domains, models and capacities (a hash of
+    every field is in the header), and cell starts that could index outside the arrays are
+    refused before anything reaches the device."""
+    import math
+    import struct
+
+    w = W.spheres_3d(seed=76, n=2000)
+    a = E.Simulation([w.model], [w.n])
+    a.upload(w.pos, w.vel)
+    a.step(3)
+    blob = a.checkpoint()
+    a.close()
+    other = E.Simulation([w.model.replace(dt=0.02)], [w.n])  # same shapes, other dt
+    with pytest.raises(N.CrgError) as e:
+        other.resume(blob)
+    assert e.value.code == N.CRG_EINVAL
+    other.close()
+    # the cell starts are the blob's last n_vox + 1 uint32 values before the step counter
+    m = w.model
+    n_vox = math.prod(max(1, math.floor((m.domain_max[k] - m.domain_min[k]) /
+                                        m.interaction_range)) for k in range(m.dim))
+    at = len(blob) - 8 - 4 * (n_vox + 1)
+    bad = bytearray(blob)
+    struct.pack_into("<I", bad, at + 4 * 5, 0xFFFFFF00)  # start[5] far past n_agents
+    same = E.Simulation([w.model], [w.n])
+    with pytest.raises(N.CrgError) as e:
+        same.resume(bytes(bad))
+    assert e.value.code == N.CRG_EINVAL
+    same.resume(blob)  # the intact blob still loads
+    same.step(2)
+    same.close()

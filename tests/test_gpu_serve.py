@@ -66,7 +66,23 @@ def test_admission_respects_budget(gpu):
                 except N.CrgError as e:
                     assert e.code == N.CRG_ETIMEDOUT
         assert peak > 0
+        # finished simulations leave their pack at the next rebuild, which returns their
+        # bytes: the server ends at zero
+        t0 = time.perf_counter()
+        while srv.stats()["bytes_in_use"] and time.perf_counter() - t0 < 5.0:
+            time.sleep(0.01)
+        assert srv.stats()["bytes_in_use"] == 0
     assert len(results) == len(reqs)
+
+
+def test_request_needing_more_than_half_the_budget_is_refused(gpu):
+    """A pack rebuild holds a class's running simulations twice, so a request larger than
+    half the budget could never be admitted: submit refuses it."""
+    w = W.spheres(20_000, 340.0, seed=97, dim=3)
+    with SV.Server(hbm_budget_bytes=4 << 20, steps_per_tick=8) as srv:
+        with pytest.raises(N.CrgError) as e:
+            srv.submit(w, 10)
+        assert e.value.code == N.CRG_ENOMEM
 
 
 def test_error_fails_only_its_request(gpu):
