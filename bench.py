@@ -403,6 +403,58 @@ def extra_mixed_large(torch):
     return out
 
 
+def extra_rods_mixed(torch, n_sub):
+    """The headline rod workload (100,000 rods x 6 vertices, 2D, chili's weights for n_sub
+    subdomains) in mixed precision against FP64: throughput of the timed run, the force
+    error on the initial state and the position error after one, ten and all timed steps
+    (normwise: max |mixed - f64| / max |f64|)."""
+    import numpy as np
+    from cellular_raza_gb300 import _native as N
+    from cellular_raza_gb300 import engine as E
+
+    w = make_workload("rods_2d", n_sub)
+    out = {"workload": "rods_2d", "agents": w.n, "steps": w.n_steps, "n_subdomains": n_sub}
+    res = {}
+    for prec in ("mixed", "f64"):
+        m = w.model.replace(precision=prec)
+        sim = E.Simulation.single(m, w.n)
+        res[(prec, "force")] = sim.forces(w.pos)
+        sim.upload(w.pos, w.vel)
+        sim.snapshot()
+        sim.step(3)  # warm-up (graph instantiation)
+        ms = timed_run(torch, sim, w.n_steps)
+        out[f"{prec}_agent_steps_per_s"] = w.n * w.n_steps / (ms / 1e3)
+        out[f"{prec}_ms_per_step"] = ms / w.n_steps
+        res[(prec, w.n_steps)] = sim.download(order="id")["pos"]
+        sim.set_option(N.OPT_PROFILE, 1)  # per-phase device times of the same run
+        sim.snapshot(restore=True)
+        sim.step(w.n_steps)
+        p = sim.profile()
+        out[f"{prec}_force_stage_ms_per_step"] = p["force_ms"] / w.n_steps
+        out[f"{prec}_pair_kernel_ms_per_step"] = p["kernel_ms"] / w.n_steps
+        out[f"{prec}_update_ms_per_step"] = p["update_ms"] / w.n_steps
+        sim.set_option(N.OPT_PROFILE, 0)
+        for k in (1, 10):
+            sim.snapshot(restore=True)
+            sim.step(k)
+            res[(prec, k)] = sim.download(order="id")["pos"]
+        sim.close()
+
+    def normwise(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    fa, fb = res[("mixed", "force")], res[("f64", "force")]
+    out["force_normwise_rel_err"] = normwise(fa, fb)
+    per_rod = (np.linalg.norm((fa - fb).reshape(w.n, -1), axis=1) /
+               np.maximum(np.linalg.norm(fb.reshape(w.n, -1), axis=1), 1e-300))
+    out["force_per_rod_rel_err_p50"] = float(np.median(per_rod))
+    out["force_per_rod_rel_err_p9999"] = float(np.percentile(per_rod, 99.99))
+    for k in (1, 10, w.n_steps):
+        out[f"pos_normwise_rel_err_{k}_steps"] = normwise(res[("mixed", k)], res[("f64", k)])
+    out["speedup_mixed_over_f64"] = out["mixed_agent_steps_per_s"] / out["f64_agent_steps_per_s"]
+    return out
+
+
 def extra_ensemble(torch):
     """1,024 independent 3D Morse simulations (log-uniform sizes, varied strength/damping),
     mixed precision, packed into the same launches (graph-captured step loop, autotuned force
@@ -713,7 +765,8 @@ def crg_arm(args):
     sim.close()
     extras = {}
     if world == 1 and not args.no_extras:
-        for name, fn in (("mixed_large", lambda: extra_mixed_large(torch)),
+        for name, fn in (("rods_mixed", lambda: extra_rods_mixed(torch, n_cpu)),
+                         ("mixed_large", lambda: extra_mixed_large(torch)),
                          ("ensemble", lambda: extra_ensemble(torch)),
                          ("served", extra_served),
                          ("cell_cycle", extra_cycle)):
@@ -740,6 +793,7 @@ def crg_arm(args):
             "clocks": clk.summary(),
             "gpu_launches": gpu_launches,
             "fma_peaks_tflops": fma,
+            "rods_mixed": extras.get("rods_mixed"),
             "mixed_large": extras.get("mixed_large"),
             "ensemble": extras.get("ensemble"),
             "served": extras.get("served"),

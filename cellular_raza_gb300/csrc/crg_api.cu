@@ -63,6 +63,7 @@ struct crg_ctx {
   uint32_t *srank = nullptr;
   uint32_t *h_ndiv = nullptr;  // pinned
   double *frc = nullptr;
+  float2 *hl = nullptr;  // mixed-precision rods: hi / lo split of the positions
   double *fbuf = nullptr;  // crg_forces: the interaction force of every slot
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
@@ -195,6 +196,9 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.mrs_r = m.radius + m.radius;
   S.mrs_k = (-2.0 * m.strength) * m.stiffness;
   S.mrs_nstiff = -m.stiffness;
+  S.mrs_r_f = (float)S.mrs_r;
+  S.mrs_k_f = (float)S.mrs_k;
+  S.mrs_nstiff_f = (float)S.mrs_nstiff;
   if (std::isnan(m.cutoff))
     S.cutoff_bits = INT64_MAX;  // d > NaN never holds
   else if (!(m.cutoff > 0.0))
@@ -241,7 +245,8 @@ int32_t check_model(const crg_model &m) {
     return CRG_ENOTSUP;
   if (m.solver_order < 1 || m.solver_order > 3) return CRG_EINVAL;
   if (m.precision != CRG_PREC_F64 && m.precision != CRG_PREC_MIXED) return CRG_EINVAL;
-  if (m.kind == CRG_KIND_ROD && m.precision != CRG_PREC_F64) return CRG_ENOTSUP;
+  // mixed-precision rods: the cell cycle's sensing and division run on FP64 rods only
+  if (m.kind == CRG_KIND_ROD && m.precision != CRG_PREC_F64 && m.cycle) return CRG_ENOTSUP;
   // NewtonDamped has no diffusion; Brownian divides by k_B T (mechanics.rs:354)
   if (m.kind == CRG_KIND_SPHERE && m.diffusion != 0.0) return CRG_EINVAL;
   if (m.kind == CRG_KIND_BROWNIAN && !(m.kb_temperature != 0.0)) return CRG_EINVAL;
@@ -305,7 +310,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
+                  c->step_ctr, c->dbg_force, c->frc, c->hl, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
                   c->staging, c->snap, c->slen, c->nslen, c->grate, c->ngrate, c->parent,
                   c->nparent, c->vctr, c->nsense, c->dflag, c->dpre, c->dbsum, c->srank};
   for (void *p : ptrs)
@@ -347,6 +352,7 @@ int32_t allocate(crg_ctx *c) {
   if (c->kind == CRG_KIND_ROD) {
     A(frc, cap * nc);
     A(bend, cap * (c->nv > 2 ? c->nv - 2 : 1) * c->dim);
+    if (c->precision != CRG_PREC_F64) A(hl, cap * nc);
     A(rctl, 4);
     A(npass, cap);
     A(pass_off, cap);
@@ -485,6 +491,7 @@ PackArgs pack_args(crg_ctx *c) {
   P.rctl = c->rctl;
   P.fix_list = c->fix_list;
   P.bend = c->bend;
+  P.hl = c->hl;
   P.npass = c->npass;
   P.pass_off = c->pass_off;
   P.pass_a = c->pass_a;
@@ -553,8 +560,14 @@ SortArgs sort_args(crg_ctx *c, int initial) {
 
 // Kernels one launch_force issues: the default rod path runs the pass walk, the pass kernel,
 // the rod-level fallback (returns at once unless the pass list overflowed) and the update.
+// Rods: the pass-list path (walk, pass kernel, overflow fallback, bend, update) runs unless
+// the FP64 thread-per-rod variant was chosen; mixed precision always takes it.
+bool rod_pass_list(const crg_ctx *c) {
+  return c->kind == CRG_KIND_ROD && (c->variant != 1 || c->precision != CRG_PREC_F64);
+}
+
 int force_kernel_count(const crg_ctx *c) {
-  if (c->kind == CRG_KIND_ROD) return c->variant != 1 ? (c->nv > 2 ? 5 : 4) : 1;
+  if (c->kind == CRG_KIND_ROD) return rod_pass_list(c) ? (c->nv > 2 ? 5 : 4) : 1;
   return c->precision == CRG_PREC_F64 ? 1 : 2;
 }
 
@@ -913,7 +926,7 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
         cudaEventElapsedTime(&a, e[0], e[3]);
         cudaEventElapsedTime(&b, e[3], e[4]);
         cudaEventElapsedTime(&d, e[1], e[2]);
-        if (c->kind == CRG_KIND_ROD && c->variant != 1)
+        if (rod_pass_list(c))
           cudaEventElapsedTime(&u, e[5], e[6]);  // recorded by the pass-list rod path only
         c->prof_ms[0] += a;
         c->prof_ms[1] += b;
@@ -1258,7 +1271,9 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
     int variant, block;
   };
   std::vector<Shape> shapes;
-  if (c->kind == CRG_KIND_ROD) {
+  if (c->kind == CRG_KIND_ROD && c->precision != CRG_PREC_F64) {
+    shapes = {{0, 0}};  // mixed-precision rods have one path
+  } else if (c->kind == CRG_KIND_ROD) {
     shapes = {{0, 0}, {1, 64}};
   } else if (c->precision == CRG_PREC_F64) {
     shapes = {{0, 0}, {2, 0}, {3, 0}, {3, 64}, {1, 64}, {1, 128}, {1, 256}};

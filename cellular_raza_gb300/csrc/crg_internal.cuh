@@ -39,6 +39,7 @@ struct SimDev {
   // Morse terms that do not depend on the pair, each rounded exactly as the per-pair
   // expression rounds them: radius + radius, (-2 * strength) * stiffness, -stiffness.
   double mrs_r, mrs_k, mrs_nstiff;
+  float mrs_r_f, mrs_k_f, mrs_nstiff_f;  // the same terms in FP32 (mixed-precision rods)
   // Mechanics of point agents: 0 NewtonDamped, 1 Brownian, 2 Langevin; stochastic terms.
   int32_t mech;
   int32_t stochastic;  // Brownian, Langevin, or RodMechanics with diffusion != 0
@@ -104,6 +105,8 @@ struct PackArgs {
                    // zeroed before each step)
   double *frc;     // rods: [nc][cap] interaction force of the rod-level fallback kernel
   double *bend;    // rods: [nv - 2][dim][cap] curvature forces (k_rods_bend)
+  float2 *hl;      // mixed-precision rods: [nc][cap] each coordinate x as FP32 hi = (float)x
+                   // and lo = (float)(x - hi), written by k_rods_walk (null on FP64)
   uint32_t *fix_list;  // mixed spheres: agents whose force the FP64 fix-up kernel computes
                        // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)

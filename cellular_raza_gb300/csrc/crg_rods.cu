@@ -412,6 +412,213 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   P.nid[i] = P.id[i];
 }
 
+// ---------------------------------------------------------------------------------------
+// Mixed precision (CRG_PREC_MIXED).  The pair arithmetic of RodInteraction -- nearest point
+// on the segment and the Morse force -- runs in FP32; springs, curvature, damping, the
+// solver, the boundary and the state stay FP64 (k_rods_bend, k_rods_update).  FP32 loses
+// nothing in the coordinate differences: every coordinate x is carried as hi = (float)x
+// and lo = (float)(x - hi), and a difference is (hi_p - hi_q) + (lo_p - lo_q), within 2^-23
+// of its own size plus 2^-47 |x| however far from the origin the rods are.  Whether a
+// vertex/segment pair interacts is decided as on the FP64 path (mixed_item), so no pair
+// switches on or off.  Sums are FP32 with Kahan compensation: per pass matrix row, over a
+// rod's passes in chili's order (the step-3 ext passes of a box summed first, as on the
+// FP64 path), and converted to FP64 once per rod.  Every FP32 operation uses an explicit
+// rounding intrinsic, so the pass kernel and the rod-level fallback produce the same bits.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void kahan_add_f(float &s, float &c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+// FP32 compensated sums of the NC entries of a force matrix.
+template <int NC>
+struct KahanRows {
+  float s[NC], c[NC];
+  __device__ __forceinline__ void set(const float *x, int64_t stride) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      s[k] = x[k * stride];
+      c[k] = 0.f;
+    }
+  }
+  __device__ __forceinline__ void add(const float *x, int64_t stride) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) kahan_add_f(s[k], c[k], x[k * stride]);
+  }
+  __device__ __forceinline__ float value(int k) const { return __fsub_rn(s[k], c[k]); }
+  __device__ __forceinline__ void add(const KahanRows &g) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) kahan_add_f(s[k], c[k], g.value(k));
+  }
+};
+
+// Vertex vx of a rod (FP64 positions pp) against segment sy of another (ps) in FP64, as the
+// FP64 path evaluates it: the full force on the vertex and t.  Out of line: rare.
+template <int D>
+__device__ __noinline__ bool item_f64(int vx, int sy, const double *pp, const double *ps,
+                                      int64_t cap, const SimDev &S, double *f, double &t) {
+  double p[D], l0[D], l1[D], q[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    p[c] = pp[(vx * D + c) * cap];
+    l0[c] = ps[(sy * D + c) * cap];
+    l1[c] = ps[((sy + 1) * D + c) * cap];
+  }
+  nearest_point_f64<D>(p, l0, l1, q, t);
+  return morse_full_f64<D>(p, q, S, f);
+}
+
+// Whether vertex vx and segment sy interact, decided from the FP64 distance exactly as the
+// FP64 path decides it (out of line: rare).
+template <int D>
+__device__ __noinline__ bool interacts_f64(int vx, int sy, const double *pp, const double *ps,
+                                           int64_t cap, const SimDev &S) {
+  double p[D], l0[D], l1[D], q[D], t;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    p[c] = pp[(vx * D + c) * cap];
+    l0[c] = ps[(sy * D + c) * cap];
+    l1[c] = ps[((sy + 1) * D + c) * cap];
+  }
+  nearest_point_f64<D>(p, l0, l1, q, t);
+  double n2 = 0.0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const double z = dsub(p[c], q[c]);
+    n2 = (c == 0) ? dmul(z, z) : dadd(n2, dmul(z, z));
+  }
+  const double dist = __dsqrt_rn(n2);
+  const long long db = __double_as_longlong(dist);
+  const unsigned long long mag = (unsigned long long)db & 0x7fffffffffffffffull;
+  return !(mag <= 0x7ff0000000000000ull && (mag == 0ull || db > S.cutoff_bits));
+}
+
+// One vertex/segment item in FP32: vertex vx of rod p (hi / lo coordinates hp, FP64 pp)
+// against segment sy of rod s (hs, ps).  Returns false when the pair does not interact,
+// else the force f on the vertex and t.  nearest_point_from_point_to_line and
+// calculate_morse_interaction (interaction.rs:497-509, 151-182).  A pair whose FP32
+// distance lies within the prefilter margin of the cutoff or of zero is decided from the
+// FP64 distance; a NaN distance (NaN or infinite coordinates, a degenerate segment) or a
+// force beyond the FP32 range takes the FP64 item.
+template <int D>
+__device__ __forceinline__ bool mixed_item(int vx, int sy, const float2 *hp, const float2 *hs,
+                                           const double *pp, const double *ps, int64_t cap,
+                                           const SimDev &S, float *f, float &t) {
+  float ab[D], ap[D], dot = 0.f, nsq = 0.f;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const float2 x = hp[(vx * D + c) * cap];
+    const float2 l0 = hs[(sy * D + c) * cap];
+    const float2 l1 = hs[((sy + 1) * D + c) * cap];
+    ab[c] = __fadd_rn(__fsub_rn(l1.x, l0.x), __fsub_rn(l1.y, l0.y));
+    ap[c] = __fadd_rn(__fsub_rn(x.x, l0.x), __fsub_rn(x.y, l0.y));
+    dot = __fmaf_rn(ab[c], ap[c], dot);
+    nsq = __fmaf_rn(ab[c], ab[c], nsq);
+  }
+  t = __fdiv_rn(dot, nsq);
+  t = t < 0.f ? 0.f : t;  // NaN stays NaN, as in FP64
+  t = t > 1.f ? 1.f : t;
+  float z[D], d2 = 0.f;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    z[c] = __fmaf_rn(-t, ab[c], ap[c]);  // vertex minus nearest point
+    d2 = __fmaf_rn(z[c], z[c], d2);
+  }
+  if (d2 == d2) {
+    const float dist = __fsqrt_rn(d2);
+    if (fabsf(__fsub_rn(dist, S.cutoff_f)) <= S.band_f || dist <= S.band_f) {
+      if (!interacts_f64<D>(vx, sy, pp, ps, cap, S)) return false;
+    } else if (dist > S.cutoff_f) {
+      return false;
+    }
+    const float e = expf(__fmul_rn(S.mrs_nstiff_f, __fsub_rn(dist, S.mrs_r_f)));
+    const float force = __fmul_rn(__fmul_rn(S.mrs_k_f, e), __fsub_rn(1.f, e));
+    if (fabsf(force) <= 3.0e38f) {  // finite, with room for the division by dist <= cutoff
+      const float sc = __fdiv_rn(force, dist);
+#pragma unroll
+      for (int c = 0; c < D; ++c) f[c] = __fmul_rn(z[c], sc);
+      return true;
+    }
+  }
+  double f64[D], t64;
+  if (!item_f64<D>(vx, sy, pp, ps, cap, S, f64, t64)) return false;
+#pragma unroll
+  for (int c = 0; c < D; ++c) f[c] = __double2float_rn(f64[c]);
+  t = __double2float_rn(t64);
+  return true;
+}
+
+// M / 2 of one pass in mixed precision, to out[(row * D + c) * stride].  is_ext = false:
+// own_a(b), a's vertices against b's segments, row vx collecting the force of items
+// (vx, 0..NV-2); true: ext_a(b), b's vertices against a's segments, row r collecting
+// -f (1 - t) of items (vx, r) and -f t of items (vx, r - 1).  The FP32 prefilter on the
+// offsets (oa, ob: a's and b's in a's voxel frame) marks the items to evaluate; own and
+// ext passes run the same loop (groups of items sharing a row) so a warp with both kinds
+// does not split.  ha / hb, pa / pb: hi / lo and FP64 coordinates of a and b (stride cap).
+template <int D, int NV>
+__device__ __forceinline__ void mixed_pass(bool is_ext, const float *oa, const float *ob,
+                                           const float2 *ha, const float2 *hb,
+                                           const double *pa, const double *pb, int64_t cap,
+                                           const SimDev &S, float thr2, float *out,
+                                           int64_t stride) {
+  constexpr int NE = NV - 1;
+  // survivor bit of item (vx, sy): own vx * NE + sy (groups by vertex), ext sy * NV + vx
+  // (groups by segment)
+  uint64_t mask = 0;
+#pragma unroll
+  for (int vx = 0; vx < NV; ++vx)
+#pragma unroll
+    for (int sy = 0; sy < NE; ++sy) {
+      float p32[D], l0[D], l1[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        p32[c] = is_ext ? ob[vx * D + c] : oa[vx * D + c];
+        l0[c] = is_ext ? oa[sy * D + c] : ob[sy * D + c];
+        l1[c] = is_ext ? oa[(sy + 1) * D + c] : ob[(sy + 1) * D + c];
+      }
+      if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2))
+        mask |= 1ull << (is_ext ? sy * NV + vx : vx * NE + sy);
+    }
+  const float2 *hp = is_ext ? hb : ha, *hs = is_ext ? ha : hb;
+  const double *pp = is_ext ? pb : pa, *ps = is_ext ? pa : pb;
+  const int n_grp = is_ext ? NE : NV, g_size = is_ext ? NV : NE;
+  const uint32_t g_mask = (1u << g_size) - 1u;
+  float cs[D], cc[D], ns[D], nc[D];  // row g and (ext) row g + 1
+#pragma unroll
+  for (int k = 0; k < D; ++k) cs[k] = cc[k] = ns[k] = nc[k] = 0.f;
+#pragma unroll 1
+  for (int g = 0; g < n_grp; ++g) {
+    uint32_t m = (uint32_t)(mask >> (g * g_size)) & g_mask;
+    while (m) {
+      const int j = __ffs(m) - 1;
+      m &= m - 1u;
+      float f[D], t;
+      if (!mixed_item<D>(is_ext ? j : g, is_ext ? g : j, hp, hs, pp, ps, cap, S, f, t))
+        continue;
+      const float w0 = is_ext ? -__fsub_rn(1.f, t) : 1.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) kahan_add_f(cs[k], cc[k], __fmul_rn(f[k], w0));
+      if (is_ext) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) kahan_add_f(ns[k], nc[k], __fmul_rn(f[k], -t));
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      out[(g * D + k) * stride] = __fmul_rn(__fsub_rn(cs[k], cc[k]), 0.5f);
+      cs[k] = ns[k];
+      cc[k] = nc[k];
+      ns[k] = nc[k] = 0.f;
+    }
+  }
+  if (is_ext) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[(NE * D + k) * stride] = __fmul_rn(__fsub_rn(cs[k], cc[k]), 0.5f);
+  }
+}
+
 // Thread per rod, in the order chili's loop adds rod a's terms into its force accumulator
 // (update_mechanics.rs:153-382, determinism = true):
 //   phase 0, step 1: the boxes of a's subdomain, ascending: a's own voxel pair by pair
@@ -425,8 +632,9 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 // With CRG_WEIGHTS_PHYSICAL every box takes phase 0 with both halves.  Terms skipped by the
 // prefilter are +0 and change no sum.  FALLBACK: the kernel runs after a pass-list overflow
 // only (P.rctl[3]) and leaves the force in P.frc for k_rods_update; otherwise it runs the
-// update itself.
-template <int D, int NV, int B, bool FALLBACK>
+// update itself.  MIXED (with FALLBACK): the passes in mixed precision (mixed_pass), added
+// up with the Kahan sums of k_rods_update's mixed fold, every listed pass included.
+template <int D, int NV, int B, bool FALLBACK, bool MIXED = false>
 __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   constexpr int NC = NV * D;
   __shared__ double sPa[NC][B];
@@ -434,7 +642,9 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   __shared__ double sG[NC][B];  // phase 2: the current box's ext sum
   __shared__ float sOa[NC][B];
   __shared__ float sOb[NC][B];
-  if (FALLBACK && !P.rctl[3]) return;  // the pass list fitted: k_rods_passq computed this step
+  __shared__ float sM[MIXED ? NC : 1][B];  // MIXED: M / 2 of the current pass
+  static_assert(FALLBACK || !MIXED, "the mixed rod-level kernel is the fallback only");
+  if (FALLBACK && !P.rctl[3]) return;  // the pass list fitted: the pass kernel computed this step
   const int tid = threadIdx.x;
   const uint32_t i = blockIdx.x * B + tid;
   if (i >= P.n_agents) return;
@@ -459,8 +669,10 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   for (int k = 0; k < NC; ++k) {
     pa[k] = P.pos[k * cap + i];
     oa[k] = P.off[k * cap + i];
-    sPa[k][tid] = pa[k];
-    sOa[k][tid] = oa[k];
+    if (!MIXED) {
+      sPa[k][tid] = pa[k];
+      sOa[k][tid] = oa[k];
+    }
   }
   float amin[D], amax[D];
 #pragma unroll
@@ -483,6 +695,9 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   double acc[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) acc[k] = 0.0;
+  KahanRows<NC> macc, mgrp;  // MIXED: the rod's sum and the box's step-3 sum
+#pragma unroll
+  for (int k = 0; k < NC; ++k) macc.s[k] = macc.c[k] = 0.f;
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -539,36 +754,62 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
                 far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
             }
             if (far) continue;
-#pragma unroll
-            for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
-            const double *posb = P.pos + b;
-            if (phase == 2) {  // step 3: ext_a(b) / 2 into the box's sum
-              if (rod_pass<D, NV, B>(true, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid)) {
-#pragma unroll
-                for (int k = 0; k < NC; ++k) {
-                  const double h = dmul(sT[k][tid], 0.5);
-                  sG[k][tid] = grp ? dadd(h, sG[k][tid]) : h;
-                }
-                grp = true;
-              }
-              continue;
-            }
-            const bool twice = phase == 0 && (same || physical);
-            const bool ext_first = same && (b < i);
+            if constexpr (MIXED) {
+              const bool twice = phase == 0 && (same || physical);
+              const bool ext_first = same && (b < i);
 #pragma unroll 1
-            for (int pass = 0; pass < 2; ++pass) {
-              const bool is_ext = (pass == 0) == ext_first;
-              if (is_ext && !twice) continue;
-              if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
-                add_half<NC, B>(acc, sT, tid);
+              for (int pass = 0; pass < 2; ++pass) {
+                const bool is_ext = phase == 2 || ((pass == 0) == ext_first);
+                if (phase != 2 && is_ext && !twice) continue;
+                if (phase == 2 && pass == 1) break;
+                mixed_pass<D, NV>(is_ext, oa, ob, P.hl + i, P.hl + b, P.pos + i, P.pos + b, cap,
+                                  S, thr2, &sM[0][tid], B);
+                if (phase != 2) {
+                  macc.add(&sM[0][tid], B);
+                } else if (grp) {  // step 3: ext_a(b) / 2 into the box's sum
+                  mgrp.add(&sM[0][tid], B);
+                } else {
+                  mgrp.set(&sM[0][tid], B);
+                  grp = true;
+                }
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < NC; ++k) sOb[k][tid] = ob[k];
+              const double *posb = P.pos + b;
+              if (phase == 2) {  // step 3: ext_a(b) / 2 into the box's sum
+                if (rod_pass<D, NV, B>(true, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid)) {
+#pragma unroll
+                  for (int k = 0; k < NC; ++k) {
+                    const double h = dmul(sT[k][tid], 0.5);
+                    sG[k][tid] = grp ? dadd(h, sG[k][tid]) : h;
+                  }
+                  grp = true;
+                }
+                continue;
+              }
+              const bool twice = phase == 0 && (same || physical);
+              const bool ext_first = same && (b < i);
+#pragma unroll 1
+              for (int pass = 0; pass < 2; ++pass) {
+                const bool is_ext = (pass == 0) == ext_first;
+                if (is_ext && !twice) continue;
+                if (rod_pass<D, NV, B>(is_ext, posb, cap, S, thr2, sPa, sT, sOa, sOb, tid))
+                  add_half<NC, B>(acc, sT, tid);
+              }
             }
           }
-          if (grp) {
+          if constexpr (MIXED) {
+            if (grp) macc.add(mgrp);
+          } else if (grp) {
 #pragma unroll
             for (int k = 0; k < NC; ++k) acc[k] = dadd(acc[k], sG[k][tid]);
           }
         }
-  if (FALLBACK) {
+  if constexpr (MIXED) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = (double)macc.value(k);
+  } else if (FALLBACK) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) P.frc[k * cap + i] = acc[k];
   } else {
@@ -874,6 +1115,14 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
   const SimDev &S = P.sims[sim];
   const bool live = valid && !sim_frozen(P, S);  // frozen rods have no passes
+  if (P.hl && live) {  // mixed precision: the hi / lo split of the rod's coordinates
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      const double x = P.pos[k * cap + i];
+      const float hi = __double2float_rn(x);
+      P.hl[k * cap + i] = make_float2(hi, __double2float_rn(dsub(x, (double)hi)));
+    }
+  }
   uint32_t key = P.key[ii];
   if (key - S.voxel_off >= S.n_vox) {
     if (live) invariant_failed(P.status, kSiteForceKey, i);
@@ -1065,6 +1314,35 @@ __global__ void __launch_bounds__(32, 24) k_rods_passq(const PackArgs P) {
   }
 }
 
+// Mixed precision: the passes of the list, one per thread (grid-stride), each pass's M / 2
+// as FP32 to its slot of the pass buffer for k_rods_update's mixed fold.
+template <int D, int NV>
+__global__ void __launch_bounds__(128) k_rods_passmix(const PackArgs P) {
+  constexpr int NC = NV * D;
+  if (P.rctl[3]) return;  // overflow: the rod-level kernel computes this step
+  const uint32_t total = P.rctl[0];
+  const int64_t cap = P.cap;
+  float *mb = reinterpret_cast<float *>(P.mbuf);
+  const float inf = __int_as_float(0x7f800000);
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += gridDim.x * blockDim.x) {
+    const uint32_t a = P.pass_a[t], b = P.pass_b[t], meta = P.pass_meta[t];
+    const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, a);
+    const SimDev &S = P.sims[sim];
+    float kd[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) kd[c] = (float)((int)((meta >> (1 + 2 * c)) & 3u) - 1) * S.dxf[c];
+    float oa[NC], ob[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      oa[k] = P.off[k * cap + a];
+      ob[k] = P.off[k * cap + b] + kd[k % D];
+    }
+    mixed_pass<D, NV>((meta & 1u) != 0u, oa, ob, P.hl + a, P.hl + b, P.pos + a, P.pos + b, cap,
+                      S, P.prefilter ? S.filt_thr2 : inf, mb + t, P.pass_cap);
+  }
+}
+
 // Curvature forces of every angle of every live rod, one thread per (angle, rod), into
 // P.bend [NV - 2][D][cap] for k_rods_update (the acos / tan work, spread over more threads
 // than the per-rod update can keep resident).
@@ -1097,8 +1375,9 @@ __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
 // Mechanics, solver, boundary and next key of every rod from its interaction force -- the
 // in-order sum of its passes' M / 2 in mbuf, or after a pass list overflow the force the
 // thread-per-rod kernel stored in frc -- and its curvature forces in bend.  Frozen
-// simulations copy their state.
-template <int D, int NV, int CYC>
+// simulations copy their state.  MIX: the pass buffer holds FP32 M / 2 (k_rods_passmix),
+// added up with Kahan sums in FP32 and converted to FP64 once.
+template <int D, int NV, int CYC, bool MIX = false>
 __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   constexpr int NC = NV * D;
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1118,6 +1397,35 @@ __global__ void __launch_bounds__(128) k_rods_update(const PackArgs P) {
   if (P.rctl[3]) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) acc[k] = P.frc[k * cap + i];
+  } else if constexpr (MIX) {
+    // the fold below in FP32 Kahan sums, in the same order, step-3 boxes summed first
+    const uint32_t p0 = P.pass_off[i];
+    const float *mb = reinterpret_cast<const float *>(P.mbuf) + p0;
+    const uint8_t *meta = P.pass_meta + p0;
+    const uint32_t n = P.npass[i];
+    const int64_t pcap = P.pass_cap;
+    KahanRows<NC> sum, g;
+#pragma unroll
+    for (int k = 0; k < NC; ++k) sum.s[k] = sum.c[k] = 0.f;
+    uint32_t gbox = 0xffffffffu;
+    for (uint32_t p = 0; p < n; ++p) {
+      const uint32_t m = meta[p];
+      if (!(m & kPassGroup)) {
+        sum.add(mb + p, pcap);
+        continue;
+      }
+      const uint32_t box = (m >> 1) & 0x3fu;
+      if (box != gbox) {
+        if (gbox != 0xffffffffu) sum.add(g);
+        g.set(mb + p, pcap);
+        gbox = box;
+      } else {
+        g.add(mb + p, pcap);
+      }
+    }
+    if (gbox != 0xffffffffu) sum.add(g);
+#pragma unroll
+    for (int k = 0; k < NC; ++k) acc[k] = (double)sum.value(k);
   } else {
     // the sum, in pass order, of the M / 2 that k_rods_passq stored for its passes (rows a
     // pass does not touch are +0, which leaves the sum unchanged since it is never -0);
@@ -1451,8 +1759,10 @@ __global__ void k_cycle_counters(const PackArgs P) {
   P.vctr[v] += 2ull * (uint64_t)(P.dpre[P.start[v + 1]] - P.dpre[P.start[v]]);
 }
 
-// Resident warps of k_rods_passq on the current device, [D - 2][NV] (set by prepare_rods).
+// Resident warps of k_rods_passq and resident blocks of k_rods_passmix on the current
+// device, [D - 2][NV] (set by prepare_rods).
 unsigned g_passq_warps[2][9] = {};
+unsigned g_passmix_blocks[2][9] = {};
 
 template <int D, int NV>
 void launch_t(const PackArgs &P, int precision, int block, cudaStream_t st, cudaEvent_t k0,
@@ -1462,27 +1772,37 @@ void launch_t(const PackArgs &P, int precision, int block, cudaStream_t st, cuda
   auto rec = [&](cudaEvent_t e) { record_event(e, st); };
   constexpr int B = 64;
   const unsigned rod_grid = (P.n_agents + B - 1) / B;
-  if (P.variant == 1) {  // thread-per-rod kernel
+  const bool mixed = precision != CRG_PREC_F64;
+  if (P.variant == 1 && !mixed) {  // FP64 thread-per-rod kernel
     rec(k0);
     k_rods_step<D, NV, B, false><<<rod_grid, B, 0, st>>>(P);
     rec(k1);
     return;
   }
   const unsigned warps = (P.n_agents + 31) / 32;
-  const unsigned pgrid = g_passq_warps[D - 2][NV] ? g_passq_warps[D - 2][NV] : warps;
   const unsigned rblocks = (P.n_agents + 127) / 128;
   cudaMemsetAsync(P.rctl, 0, 4 * sizeof(uint32_t), st);
   k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
   rec(k0);
-  k_rods_passq<D, NV><<<pgrid, 32, passq_smem_bytes<D, NV>(), st>>>(P);
-  rec(k1);
-  k_rods_step<D, NV, B, true><<<rod_grid, B, 0, st>>>(P);  // returns at once unless overflow
+  if (mixed) {  // FP32 pair forces; each launch returns at once unless it is this step's
+    const unsigned mgrid = g_passmix_blocks[D - 2][NV] ? g_passmix_blocks[D - 2][NV] : rblocks;
+    k_rods_passmix<D, NV><<<mgrid, 128, 0, st>>>(P);
+    rec(k1);
+    k_rods_step<D, NV, B, true, true><<<rod_grid, B, 0, st>>>(P);
+  } else {
+    const unsigned pgrid = g_passq_warps[D - 2][NV] ? g_passq_warps[D - 2][NV] : warps;
+    k_rods_passq<D, NV><<<pgrid, 32, passq_smem_bytes<D, NV>(), st>>>(P);
+    rec(k1);
+    k_rods_step<D, NV, B, true><<<rod_grid, B, 0, st>>>(P);
+  }
   if (NV > 2) {
     const uint64_t nb = ((uint64_t)P.n_agents * (NV - 2) + 127) / 128;
     k_rods_bend<D, NV><<<(unsigned)nb, 128, 0, st>>>(P);
   }
   rec(k2);
-  if (P.dflag)
+  if (mixed)
+    k_rods_update<D, NV, 0, true><<<rblocks, 128, 0, st>>>(P);
+  else if (P.dflag)
     k_rods_update<D, NV, 1><<<rblocks, 128, 0, st>>>(P);
   else
     k_rods_update<D, NV, 0><<<rblocks, 128, 0, st>>>(P);
@@ -1501,6 +1821,10 @@ cudaError_t prepare_t() {
   if (e == cudaSuccess)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rods_passq<D, NV>, 32, psmem);
   if (e == cudaSuccess) g_passq_warps[D - 2][NV] = (unsigned)(sms * per_sm);
+  int mix_per_sm = 0;
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mix_per_sm, k_rods_passmix<D, NV>, 128, 0);
+  if (e == cudaSuccess) g_passmix_blocks[D - 2][NV] = (unsigned)(sms * (mix_per_sm > 0 ? mix_per_sm : 1));
   return e;
 }
 
