@@ -48,6 +48,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the mixed-precision, ensemble and served measurements")
+    p.add_argument("--extras", default="rods_mixed,mixed_large,ensemble,served,cell_cycle",
+                   help="comma-separated extras to run (default: all)")
     # a small run for profilers (ncu): direct launches, every kernel a separate launch
     p.add_argument("--profile-case", action="store_true",
                    help="run --case-steps steps of the workload with direct launches (no CUDA "
@@ -765,11 +767,14 @@ def crg_arm(args):
     sim.close()
     extras = {}
     if world == 1 and not args.no_extras:
+        wanted = set(args.extras.split(","))
         for name, fn in (("rods_mixed", lambda: extra_rods_mixed(torch, n_cpu)),
                          ("mixed_large", lambda: extra_mixed_large(torch)),
                          ("ensemble", lambda: extra_ensemble(torch)),
                          ("served", extra_served),
                          ("cell_cycle", extra_cycle)):
+            if name not in wanted:
+                continue
             try:
                 extras[name] = fn()
             except Exception as e:  # reported, not fatal for the headline line
