@@ -407,14 +407,16 @@ def extra_mixed_large(torch):
 
 def extra_rods_mixed(torch, n_sub):
     """The headline rod workload (100,000 rods x 6 vertices, 2D, chili's weights for n_sub
-    subdomains) in mixed precision against FP64: throughput of the timed run, the force
-    error on the initial state and the position error after one, ten and all timed steps
-    (normwise: max |mixed - f64| / max |f64|)."""
+    subdomains) in mixed precision against FP64 over its first 200 steps (the unstable rods
+    of this input end both runs in a BoundaryError later, at a step that depends on the last
+    bits): throughput, the force error on the initial state and the position error after
+    one, ten and 200 steps (normwise: max |mixed - f64| / max |f64|)."""
     import numpy as np
     from cellular_raza_gb300 import _native as N
     from cellular_raza_gb300 import engine as E
 
     w = make_workload("rods_2d", n_sub)
+    w.n_steps = 200
     out = {"workload": "rods_2d", "agents": w.n, "steps": w.n_steps, "n_subdomains": n_sub}
     res = {}
     for prec in ("mixed", "f64"):

@@ -417,8 +417,8 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 // on the segment and the Morse force -- runs in FP32; springs, curvature, damping, the
 // solver, the boundary and the state stay FP64 (k_rods_bend, k_rods_update).  FP32 loses
 // nothing in the coordinate differences: every coordinate x is carried as hi = (float)x
-// and lo = (float)(x - hi), and a difference is (hi_p - hi_q) + (lo_p - lo_q), within 2^-23
-// of its own size plus 2^-47 |x| however far from the origin the rods are.  Whether a
+// and lo = (float)(x - hi), and differences are formed as hi + lo pairs (diff_hl), exact
+// to ~2^-48 |x| however far from the origin the rods are.  Whether a
 // vertex/segment pair interacts is decided as on the FP64 path (mixed_item), so no pair
 // switches on or off.  Sums are FP32 with Kahan compensation: per pass matrix row, over a
 // rod's passes in chili's order (the step-3 ext passes of a box summed first, as on the
@@ -495,37 +495,67 @@ __device__ __noinline__ bool interacts_f64(int vx, int sy, const double *pp, con
   return !(mag <= 0x7ff0000000000000ull && (mag == 0ull || db > S.cutoff_bits));
 }
 
+// (a.x + a.y) - (b.x + b.y) for hi / lo coordinates as an unevaluated sum hi + lo: hi the
+// FP32 difference of the hi parts, lo its exact rounding error (Knuth's TwoSum) plus the
+// difference of the lo parts, so hi + lo is the difference to ~2^-48 of the coordinates.
+__device__ __forceinline__ void diff_hl(float2 a, float2 b, float &hi, float &lo) {
+  const float nb = -b.x;
+  const float s = __fadd_rn(a.x, nb);
+  const float bv = __fsub_rn(s, a.x);
+  const float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bv)), __fsub_rn(nb, bv));
+  hi = s;
+  lo = __fadd_rn(err, __fsub_rn(a.y, b.y));
+}
+
 // One vertex/segment item in FP32: vertex vx of rod p (hi / lo coordinates hp, FP64 pp)
 // against segment sy of rod s (hs, ps).  Returns false when the pair does not interact,
 // else the force f on the vertex and t.  nearest_point_from_point_to_line and
-// calculate_morse_interaction (interaction.rs:497-509, 151-182).  A pair whose FP32
-// distance lies within the prefilter margin of the cutoff or of zero is decided from the
-// FP64 distance; a NaN distance (NaN or infinite coordinates, a degenerate segment) or a
-// force beyond the FP32 range takes the FP64 item.
+// calculate_morse_interaction (interaction.rs:497-509, 151-182).
+// The vertex-to-segment vector z must be accurate relative to its own length, which for
+// crossing rods is far below the segment length: the differences x - l0 and l1 - l0 are
+// carried as hi + lo pairs, z = (x - l0) - t (l1 - l0) is formed from them, and for an
+// interior nearest point one projection step removes the along-segment error that the
+// FP32 t leaves in z.  Then the direction of the force is accurate to a few FP32 ulps and
+// its magnitude to the FP32 distance.  A pair whose FP32 distance lies within the
+// prefilter margin of the cutoff or of zero is decided from the FP64 distance; a NaN
+// distance (NaN or infinite coordinates, a degenerate segment) or a force beyond the FP32
+// range takes the FP64 item.
 template <int D>
 __device__ __forceinline__ bool mixed_item(int vx, int sy, const float2 *hp, const float2 *hs,
                                            const double *pp, const double *ps, int64_t cap,
                                            const SimDev &S, float *f, float &t) {
-  float ab[D], ap[D], dot = 0.f, nsq = 0.f;
+  float abh[D], abl[D], aph[D], apl[D], ab[D], dot = 0.f, nsq = 0.f;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
     const float2 x = hp[(vx * D + c) * cap];
     const float2 l0 = hs[(sy * D + c) * cap];
     const float2 l1 = hs[((sy + 1) * D + c) * cap];
-    ab[c] = __fadd_rn(__fsub_rn(l1.x, l0.x), __fsub_rn(l1.y, l0.y));
-    ap[c] = __fadd_rn(__fsub_rn(x.x, l0.x), __fsub_rn(x.y, l0.y));
-    dot = __fmaf_rn(ab[c], ap[c], dot);
+    diff_hl(l1, l0, abh[c], abl[c]);
+    diff_hl(x, l0, aph[c], apl[c]);
+    ab[c] = __fadd_rn(abh[c], abl[c]);
+    dot = __fmaf_rn(ab[c], __fadd_rn(aph[c], apl[c]), dot);
     nsq = __fmaf_rn(ab[c], ab[c], nsq);
   }
   t = __fdiv_rn(dot, nsq);
-  t = t < 0.f ? 0.f : t;  // NaN stays NaN, as in FP64
+  const bool interior = t > 0.f && t < 1.f;  // false for NaN
+  t = t < 0.f ? 0.f : t;                      // NaN stays NaN, as in FP64
   t = t > 1.f ? 1.f : t;
-  float z[D], d2 = 0.f;
+  float z[D];
 #pragma unroll
-  for (int c = 0; c < D; ++c) {
-    z[c] = __fmaf_rn(-t, ab[c], ap[c]);  // vertex minus nearest point
-    d2 = __fmaf_rn(z[c], z[c], d2);
+  for (int c = 0; c < D; ++c)
+    z[c] = __fadd_rn(__fmaf_rn(-t, abh[c], aph[c]), __fmaf_rn(-t, abl[c], apl[c]));
+  if (interior) {  // z is then short: its component along the segment is t's error
+    float zd = 0.f;
+#pragma unroll
+    for (int c = 0; c < D; ++c) zd = __fmaf_rn(z[c], ab[c], zd);
+    const float dt = __fdiv_rn(zd, nsq);
+    t = __fadd_rn(t, dt);
+#pragma unroll
+    for (int c = 0; c < D; ++c) z[c] = __fmaf_rn(-dt, ab[c], z[c]);
   }
+  float d2 = 0.f;
+#pragma unroll
+  for (int c = 0; c < D; ++c) d2 = __fmaf_rn(z[c], z[c], d2);
   if (d2 == d2) {
     const float dist = __fsqrt_rn(d2);
     if (fabsf(__fsub_rn(dist, S.cutoff_f)) <= S.band_f || dist <= S.band_f) {
@@ -535,7 +565,7 @@ __device__ __forceinline__ bool mixed_item(int vx, int sy, const float2 *hp, con
     }
     const float e = expf(__fmul_rn(S.mrs_nstiff_f, __fsub_rn(dist, S.mrs_r_f)));
     const float force = __fmul_rn(__fmul_rn(S.mrs_k_f, e), __fsub_rn(1.f, e));
-    if (fabsf(force) <= 3.0e38f) {  // finite, with room for the division by dist <= cutoff
+    if (fabsf(force) <= 3.0e38f && dist > 0.f) {  // finite, and a direction to scale
       const float sc = __fdiv_rn(force, dist);
 #pragma unroll
       for (int c = 0; c < D; ++c) f[c] = __fmul_rn(z[c], sc);

