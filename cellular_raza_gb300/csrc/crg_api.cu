@@ -143,6 +143,11 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
     if (!(d.min[i] < d.max[i])) return CRG_EBOUNDARY;  // check_min_max (:149-162)
     S.min[i] = d.min[i];
     S.max[i] = d.max[i];
+    long long bmin, bmax;
+    std::memcpy(&bmin, &d.min[i], sizeof(bmin));
+    std::memcpy(&bmax, &d.max[i], sizeof(bmax));
+    S.min_key[i] = crg::f64_order_key_bits(bmin);
+    S.max_key[i] = crg::f64_order_key_bits(bmax);
     uint64_t nvox;
     if (d.voxel_mode == 0) {
       // from_boundaries_and_interaction_range (cartesian_cuboid_n.rs:183-222)

@@ -24,6 +24,7 @@ struct SimDev {
   int32_t dim;
   int32_t nvox[3];
   double min[3], max[3], dx[3];
+  long long min_key[3], max_key[3];  // f64_order_key of min and max (boundary compares)
   float dxf[3];
   float inv_dxf[3];  // (float)(1 / dx): the FP32 voxel-index estimate (voxel_of)
   uint32_t voxel_off, n_vox;
@@ -144,6 +145,29 @@ __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a,
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
 
+// 0.0 + x, exactly: x itself except that -0.0 becomes +0.0 (integer instructions only).
+__device__ __forceinline__ double plus_zero(double x) {
+  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
+// Comparisons of an FP64 value with a finite bound on the integer pipe, leaving the FP64
+// pipe to arithmetic.  f64_order_key maps every non-NaN double to an int64 in the same
+// order (both zeros to 0); a NaN compares false, as in IEEE.
+__host__ __device__ __forceinline__ long long f64_order_key_bits(long long b) {
+  return b >= 0 ? b : -(b & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ bool f64_is_nan(long long b) {
+  return (unsigned long long)(b & 0x7fffffffffffffffll) > 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool f64_lt_key(double x, long long bound_key) {  // x < bound
+  const long long b = __double_as_longlong(x);
+  return !f64_is_nan(b) && f64_order_key_bits(b) < bound_key;
+}
+__device__ __forceinline__ bool f64_gt_key(double x, long long bound_key) {  // x > bound
+  const long long b = __double_as_longlong(x);
+  return !f64_is_nan(b) && f64_order_key_bits(b) > bound_key;
+}
+
 // ---- random stream of the stochastic mechanics --------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
 // SC'11): ten rounds of two 32x32->64 multiplies with the round keys bumped by the Weyl
@@ -218,7 +242,8 @@ __device__ __forceinline__ int voxel_of(const SimDev &S, const double *p, uint32
   uint64_t idx[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    const double d = dsub(p[i], S.min[i]);
+    // p - (+-0.0) is p itself except for p = -0.0 with min = -0.0, whose index is 0 either way
+    const double d = S.min_key[i] == 0 ? p[i] : dsub(p[i], S.min[i]);
     const float q = __fmul_rn(__double2float_rn(d), S.inv_dxf[i]);
     const float fl = floorf(q), fr = q - fl;  // exact for 0 <= q < 2^23
     const float eps = __fmaf_rn(q, 4.0e-7f, 1.0e-6f);

@@ -202,11 +202,13 @@ __device__ __forceinline__ void bend_force(const SimDev &S, const double *c1, co
 #pragma unroll
   for (int c = 1; c < D; ++c) prod = dadd(prod, dmul(c1[c], c2[c]));
   const double n1 = norm_f64<D>(c1), n2 = norm_f64<D>(c2);
+  // zero tests and the clamp to [-1, 1] on the integer pipe (same results, NaN included)
+  auto is_zero = [](double x) { return (__double_as_longlong(x) & 0x7fffffffffffffffll) == 0; };
   double angle = 0.0;
-  if (!(n1 == 0.0 || n2 == 0.0)) {
+  if (!(is_zero(n1) || is_zero(n2))) {
     double cang = ddiv(prod, dmul(n1, n2));
-    if (cang < -1.0) cang = -1.0;
-    if (cang > 1.0) cang = 1.0;
+    if (f64_lt_key(cang, -0x3ff0000000000000ll)) cang = -1.0;  // key of -1.0
+    if (f64_gt_key(cang, 0x3ff0000000000000ll)) cang = 1.0;    // key of 1.0
     angle = acos(cang);
   }
   double fd[D];
@@ -214,9 +216,10 @@ __device__ __forceinline__ void bend_force(const SimDev &S, const double *c1, co
   for (int c = 0; c < D; ++c) fd[c] = dsub(c1[c], c2[c]);
   const double fdn = norm_f64<D>(fd);
   const double tn = tan(dmul(0.5, angle));
+  const bool fd_zero = is_zero(fdn);
 #pragma unroll
   for (int c = 0; c < D; ++c) {
-    const double fdir = (fdn != 0.0) ? ddiv(fd[c], fdn) : fd[c];
+    const double fdir = !fd_zero ? ddiv(fd[c], fdn) : fd[c];
     f[c] = dmul(dmul(dmul(fdir, 2.0), S.rigidity), tn);
   }
 }
@@ -237,18 +240,19 @@ __device__ __forceinline__ void rod_finish(const PackArgs &P, const SimDev &S, u
     for (int c = 0; c < D; ++c) {
       double &p = np[s * D + c];
       double &u = nvl[s * D + c];
-      if (p < S.min[c]) {
+      if (f64_lt_key(p, S.min_key[c])) {  // p < min, on the integer pipe
         p = dsub(dmul(S.min[c], 2.0), p);
         u = fabs(u);
       }
-      if (p > S.max[c]) {
+      if (f64_gt_key(p, S.max_key[c])) {  // p > max
         p = dsub(dmul(S.max[c], 2.0), p);
         u = -fabs(u);
       }
     }
 #pragma unroll
   for (int k = 0; k < NC; ++k)
-    if (np[k] < S.min[k % D] || np[k] > S.max[k % D]) inside = false;
+    if (f64_lt_key(np[k], S.min_key[k % D]) || f64_gt_key(np[k], S.max_key[k % D]))
+      inside = false;
   if (!inside) set_status(P.status, CRG_EBOUNDARY, id, *P.step_ctr + 1, S.sim_index);
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
@@ -303,13 +307,13 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 #pragma unroll
   for (int s = 0; s + 1 < NV; ++s) {
     const double nrm = norm_f64<D>(dist[s]);
-    if (nrm != 0.0) {
+    if ((__double_as_longlong(nrm) & 0x7fffffffffffffffll) != 0) {  // nrm != 0.0
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         const double dir = ddiv(dist[s][c], nrm);
         const double fi = dmul(dmul(-dir, S.spring_tension), dsub(nrm, l0));
-        tf[s * D + c] = dadd(tf[s * D + c], dmul(fi, 0.5));
-        tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], dmul(-fi, 0.5));
+        tf[s * D + c] = dadd(tf[s * D + c], half_exact(fi));  // x * 0.5 on the bit pattern
+        tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], half_exact(-fi));
       }
     }
   }
@@ -326,9 +330,9 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       const double f = fb[c];
-      tf[s * D + c] = dadd(tf[s * D + c], dmul(-f, 0.5));
+      tf[s * D + c] = dadd(tf[s * D + c], half_exact(-f));
       tf[(s + 1) * D + c] = dadd(tf[(s + 1) * D + c], f);
-      tf[(s + 2) * D + c] = dadd(tf[(s + 2) * D + c], dmul(-f, 0.5));
+      tf[(s + 2) * D + c] = dadd(tf[(s + 2) * D + c], half_exact(-f));
     }
   }
   // damping
@@ -351,11 +355,18 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
   }
   // solver (dx = v, dv = total force)
   double np[NC], nvl[NC];
-  if (S.order == 1) {
+  // x + 0.0 (dv_rand, and dx_rand without diffusion) is plus_zero(x) exactly
+  if (S.order == 1 && !S.stochastic) {
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      np[k] = plus_zero(dadd(dmul(va[k], dt), pa[k]));
+      nvl[k] = plus_zero(dadd(dmul(tf[k], dt), va[k]));
+    }
+  } else if (S.order == 1) {
 #pragma unroll
     for (int k = 0; k < NC; ++k) {
       np[k] = dadd(dadd(dmul(va[k], dt), pa[k]), rx[k]);
-      nvl[k] = dadd(dadd(dmul(tf[k], dt), va[k]), 0.0);
+      nvl[k] = plus_zero(dadd(dmul(tf[k], dt), va[k]));
     }
   } else {
     const bool ab3 = (S.order == 3) && P.hmeta[i];
@@ -366,12 +377,12 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
         const double px = P.hist[k * cap + i], pv = P.hist[(NC + k) * cap + i];
         np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dadd(dmul(px, f1), dmul(va[k], f2))), dt),
                           pa[k]), rx[k]);
-        nvl[k] = dadd(dadd(dmul(dadd(dmul(tf[k], f0), dadd(dmul(pv, f1), dmul(tf[k], f2))), dt),
-                           va[k]), 0.0);
+        nvl[k] = plus_zero(dadd(dmul(dadd(dmul(tf[k], f0), dadd(dmul(pv, f1), dmul(tf[k], f2))), dt),
+                                va[k]));
       } else {
         const double f0 = 3.0 / 2.0, f1 = -1.0 / 2.0;
         np[k] = dadd(dadd(dmul(dadd(dmul(va[k], f0), dmul(va[k], f1)), dt), pa[k]), rx[k]);
-        nvl[k] = dadd(dadd(dmul(dadd(dmul(tf[k], f0), dmul(tf[k], f1)), dt), va[k]), 0.0);
+        nvl[k] = plus_zero(dadd(dmul(dadd(dmul(tf[k], f0), dmul(tf[k], f1)), dt), va[k]));
       }
       P.nhist[k * cap + i] = va[k];
       P.nhist[(NC + k) * cap + i] = tf[k];
@@ -862,10 +873,6 @@ __device__ __forceinline__ int nth_set_bit64(uint64_t m, int n) {  // n-th set b
   return 32 + (int)__fns((uint32_t)(m >> 32), 0, n - clo + 1);
 }
 
-// 0.0 + x, exactly: x itself except that -0.0 becomes +0.0.
-__device__ __forceinline__ double plus_zero(double x) {
-  return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
-}
 
 // Items of one chunk of the queue kernel's result buffer.  Every lane's items fit (at most
 // NV * (NV - 1) <= 56), so a round needs more than one chunk only when the warp's passes

@@ -174,7 +174,7 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
       dxv[c] = va[c];
       dvv[c] = dadd(dmul(im, acc[c]), dmul(-S.damping, va[c]));
     }
-  } else if (__all_sync(__activemask(), S.mass == 1.0)) {
+  } else if (__all_sync(__activemask(), __double_as_longlong(S.mass) == 0x3ff0000000000000ll)) {
     // F / 1 is F exactly (every input, NaN and signed zeros included): no division
 #pragma unroll
     for (int c = 0; c < D; ++c) {
@@ -215,7 +215,13 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
   // Solvers (chili/solvers.rs:23-55, 156-347).
   double np[D], nvl[D];
   uint8_t meta = 0;
-  if (S.order == 1) {
+  if (S.order == 1 && !S.stochastic) {  // + rx and + rv add +0.0: plus_zero, exactly
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      np[c] = plus_zero(dadd(dmul(dxv[c], dt), pa[c]));
+      nvl[c] = plus_zero(dadd(dmul(dvv[c], dt), va[c]));
+    }
+  } else if (S.order == 1) {
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       np[c] = dadd(dadd(dmul(dxv[c], dt), pa[c]), rx[c]);
@@ -248,22 +254,23 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
     P.nhmeta[i] = meta;
   }
 
-  // CartesianSubDomain::apply_boundary (cartesian_cuboid_n.rs:594-631).
+  // CartesianSubDomain::apply_boundary (cartesian_cuboid_n.rs:594-631), the comparisons
+  // with the domain bounds on the integer pipe (same results, NaN included).
   bool inside = true;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
-    if (np[c] < S.min[c]) {
+    if (f64_lt_key(np[c], S.min_key[c])) {
       np[c] = dsub(dmul(2.0, S.min[c]), np[c]);
       nvl[c] = fabs(nvl[c]);
     }
-    if (np[c] > S.max[c]) {
+    if (f64_gt_key(np[c], S.max_key[c])) {
       np[c] = dsub(dmul(2.0, S.max[c]), np[c]);
       nvl[c] = -fabs(nvl[c]);
     }
   }
 #pragma unroll
   for (int c = 0; c < D; ++c)
-    if (np[c] < S.min[c] || np[c] > S.max[c]) inside = false;
+    if (f64_lt_key(np[c], S.min_key[c]) || f64_gt_key(np[c], S.max_key[c])) inside = false;
   if (!inside) set_status(P.status, CRG_EBOUNDARY, P.id[i], *P.step_ctr + 1, S.sim_index);
   if (S.mech == 1) {  // Brownian::set_velocity is a no-op: the velocity stays as it was
 #pragma unroll
@@ -288,8 +295,17 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
   atomicAdd(&P.count[nk], 1u);
 }
 
+// Mixed thread-per-agent kernel: prefilter survivors buffered per thread (candidate index
+// and box code in dynamic shared memory, [kSurv][blockDim]) and evaluated in candidate
+// order once kSurv are buffered and at the end.  The scan itself is cheap, and a warp then
+// runs the FP32 Morse over buffered survivors with most lanes busy instead of once per scan
+// position with the few lanes whose candidate survived.
+constexpr int kSurv = 16;
+constexpr size_t mixed_step_smem(int block) { return (size_t)kSurv * block * 5; }
+
 template <int D, int PREC>
 __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
+  extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n_agents) return;
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
@@ -332,6 +348,33 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
     hi[c] = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
   }
+  // MIXED: the buffered survivors, evaluated in order (the scan's own arithmetic for zf)
+  const uint32_t bd = blockDim.x, tid = threadIdx.x;
+  uint32_t *sB = sSurv;
+  uint8_t *sM = reinterpret_cast<uint8_t *>(sSurv + kSurv * bd);
+  int ns = 0;
+  auto flush = [&]() {
+    for (int q = 0; q < ns; ++q) {
+      const uint32_t b = sB[q * bd + tid], m = sM[q * bd + tid];
+      float kd[D], zf[D], d2 = 0.0f;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        kd[c] = (float)((int)((m >> (2 * c)) & 3u) - 1) * S.dxf[c];
+        zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
+        d2 = fmaf(zf[c], zf[c], d2);
+      }
+      float h[D];
+      if (mixed_half<D>(P, S, pa, b, zf, d2, h)) {
+        const bool twice = (m >> 6) & 1u;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          kahan_add(fs[c], fcmp[c], h[c]);
+          if (twice) kahan_add(fs[c], fcmp[c], h[c]);
+        }
+      }
+    }
+    ns = 0;
+  };
   for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
     for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
       for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
@@ -382,18 +425,16 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
               nan_seen = true;
               continue;
             }
-            float h[D];
-            if (mixed_half<D>(P, S, pa, b, zf, d2, h)) {
-#pragma unroll
-              for (int c = 0; c < D; ++c) {
-                kahan_add(fs[c], fcmp[c], h[c]);
-                if (twice) kahan_add(fs[c], fcmp[c], h[c]);
-              }
-            }
+            const int dj2 = (D == 3) ? j2 - idx[D - 1] : 0;
+            sB[ns * bd + tid] = b;
+            sM[ns * bd + tid] = (uint8_t)((j0 - idx[0] + 1) | ((j1 - idx[1] + 1) << 2) |
+                                          ((dj2 + 1) << 4) | (twice ? 0x40 : 0));
+            if (++ns == kSurv) flush();
           }
         }
       }
   if (PREC != CRG_PREC_F64) {
+    flush();
     if (nan_seen) {  // k_spheres_fix computes this agent's force and update in FP64
       P.fix_list[atomicAdd(&P.rctl[0], 1u)] = i;
       return;
@@ -943,14 +984,14 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
     if (precision == CRG_PREC_F64) {
       k_spheres_step<3, CRG_PREC_F64><<<grid, block, 0, st>>>(P);
     } else {
-      k_spheres_step<3, CRG_PREC_MIXED><<<grid, block, 0, st>>>(P);
+      k_spheres_step<3, CRG_PREC_MIXED><<<grid, block, mixed_step_smem(block), st>>>(P);
       k_spheres_fix<3><<<32, 128, 0, st>>>(P);  // returns at once when nothing was handed over
     }
   } else {
     if (precision == CRG_PREC_F64) {
       k_spheres_step<2, CRG_PREC_F64><<<grid, block, 0, st>>>(P);
     } else {
-      k_spheres_step<2, CRG_PREC_MIXED><<<grid, block, 0, st>>>(P);
+      k_spheres_step<2, CRG_PREC_MIXED><<<grid, block, mixed_step_smem(block), st>>>(P);
       k_spheres_fix<2><<<32, 128, 0, st>>>(P);
     }
   }
