@@ -477,26 +477,43 @@ def extra_ensemble(torch):
     sim.snapshot()
     tune = sim.autotune(5)
     sim.step(3)
-    ms = timed_run(torch, sim, steps)
+    ms = timed_run(torch, sim, steps)  # restores the snapshot first: ends after `steps`
+    final = sim.download(order="id")["pos"]
     sim.close()
     batched = n_total * steps / (ms / 1e3)
-    sample = ws[::len(ws) // 24][:24]
+    stride = len(ws) // 24
+    sample_idx = list(range(0, len(ws), stride))[:24]
+    off = np.cumsum([0] + [w.n for w in ws])
     t_seq = 0.0
-    for w in sample:
+    errs, errs_norm = [], []
+    for s in sample_idx:
+        w = ws[s]
         s1 = E.Simulation.single(w.model.replace(precision="f64"), w.n)
         s1.upload(w.pos, w.vel)
         s1.snapshot()
         s1.step(3)
         t_seq += timed_run(torch, s1, steps) / 1e3
+        ref = s1.download(order="id")["pos"]
         s1.close()
-    seq_total_s = t_seq * len(ws) / len(sample)
+        mixed = final[off[s]:off[s + 1]]
+        dx = np.linalg.norm((mixed - ref).reshape(w.n, -1), axis=1)
+        x = np.linalg.norm(ref.reshape(w.n, -1), axis=1)
+        errs.append(float((dx / x).max()))
+        errs_norm.append(float(dx.max() / x.max()))
+    seq_total_s = t_seq * len(ws) / len(sample_idx)
     sequential = n_total * steps / seq_total_s
     return {"workload": "ensemble", "sims": len(ws), "agents": n_total, "steps": steps,
             "precision": "mixed", "autotune": tune, "batched_agent_steps_per_s": batched,
             "batched_ms_per_step": ms / steps,
             "sequential_f64_agent_steps_per_s": sequential,
-            "sequential_sample": f"{len(sample)} of {len(ws)} simulations, scaled",
-            "speedup": batched / sequential}
+            "sequential_sample": f"{len(sample_idx)} of {len(ws)} simulations, scaled",
+            "speedup": batched / sequential,
+            "mixed_vs_f64_error": {
+                "definition": "final positions of the batched mixed run against the sampled "
+                              "simulations run alone in FP64, after all steps",
+                "max_rel_pos_err": max(errs),  # per agent |dx| / |x|, worst simulation
+                "max_normwise_rel_pos_err": max(errs_norm),  # max |dx| / max |x|
+                "median_sim_max_rel_pos_err": float(np.median(errs))}}
 
 
 def extra_cycle(n_rods=2000, steps=600):
