@@ -229,6 +229,26 @@ __device__ __forceinline__ uint32_t subdomain_of(const SimDev &S, uint32_t v) {
   return v < S.sd_switch ? v / S.sd_avg : (v - S.sd_switch) / S.sd_div2 + S.sd_n;
 }
 
+// The voxels of one subdomain are a contiguous range of plain indices (the chunks above):
+// the subdomain holding voxel v, as the range [lo, hi) that another voxel w shares with it
+// exactly when subdomain_of(w) == subdomain_of(v).  One division per agent instead of one per
+// neighbour box.
+struct SubRange {
+  uint32_t lo, hi;
+  __device__ __forceinline__ bool same(uint32_t w) const { return w - lo < hi - lo; }
+};
+__device__ __forceinline__ SubRange subdomain_range(const SimDev &S, uint32_t v) {
+  SubRange r;
+  if (v < S.sd_switch) {
+    r.lo = (v / S.sd_avg) * S.sd_avg;
+    r.hi = r.lo + S.sd_avg;
+  } else {
+    r.lo = S.sd_switch + ((v - S.sd_switch) / S.sd_div2) * S.sd_div2;
+    r.hi = r.lo + S.sd_div2;
+  }
+  return r;
+}
+
 // CartesianSubDomain::get_index_of (cartesian_cuboid_n.rs:469-490) + plain-index lookup.
 // Returns 0 ok, 1 conversion failure, 2 index outside the voxel grid.
 //

@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
   bool a_nan = false;  // fminf/fmaxf drop NaNs, so test every offset
 #pragma unroll
   for (int k = 0; k < NC; ++k) a_nan |= !(oa[k] == oa[k]);
-  const uint32_t sub_v = subdomain_of(S, v);
+  const SubRange sub_v = subdomain_range(S, v);
   const bool physical = S.weight_mode == CRG_WEIGHTS_PHYSICAL;
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
@@ -753,7 +753,7 @@ __global__ void __launch_bounds__(B) k_rods_step(const PackArgs P) {
           const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                       : (uint32_t)j0 * S.nvox[1] + j1;
           const bool same = (w == v);
-          const bool local = physical || subdomain_of(S, w) == sub_v;
+          const bool local = physical || sub_v.same(w);
           if (local != (phase == 0)) continue;
           // b's offsets in a's voxel frame: off_b + (corner_b - corner_a) = off_b + (j-idx) dx
           float kd[D];
@@ -1182,7 +1182,7 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
       amax[k % D] = fmaxf(amax[k % D], o);
     }
   }
-  const uint32_t sub_v = subdomain_of(S, v);
+  const SubRange sub_v = subdomain_range(S, v);
   const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
   int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
 #pragma unroll
@@ -1205,7 +1205,7 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
         const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                     : (uint32_t)j0 * S.nvox[1] + j1;
         const bool same = (w == v);
-        const bool local = physical || subdomain_of(S, w) == sub_v;
+        const bool local = physical || sub_v.same(w);
         if (local != (phase == 0)) continue;
         const bool twice = phase == 0 && (same || physical);
         const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};

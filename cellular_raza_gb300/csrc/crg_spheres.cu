@@ -75,7 +75,9 @@ __device__ __forceinline__ bool morse_half_f64_batch(const double *z, const SimD
 template <int D>
 __device__ __forceinline__ bool mixed_half(const PackArgs &P, const SimDev &S, const double *pa,
                                            uint32_t b, const float *zf, float d2, float *h) {
-  const float dist = sqrtf(d2);
+  // one reciprocal square root serves the distance and the direction z / dist
+  const float rinv = rsqrtf(d2);
+  const float dist = d2 > 0.0f ? __fmul_rn(d2, rinv) : 0.0f;
   bool in;
   if (fabsf(dist - S.cutoff_f) <= S.band_f || dist <= S.band_f) {
     double n2 = 0.0;
@@ -93,8 +95,11 @@ __device__ __forceinline__ bool mixed_half(const PackArgs &P, const SimDev &S, c
   const float r = S.radius_f + S.radius_f;
   const float e = expf(-S.stiffness_f * (dist - r));
   const float force = -2.0f * S.strength_f * S.stiffness_f * e * (1.0f - e);
+  // a pair that interacts in FP64 at an FP32 distance of 0 has no FP32 direction: the NaN
+  // hands the agent to the FP64 fix-up kernel
+  const float sc = d2 > 0.0f ? __fmul_rn(__fmul_rn(force, 0.5f), rinv) : __int_as_float(0x7fc00000);
 #pragma unroll
-  for (int c = 0; c < D; ++c) h[c] = (zf[c] / dist) * force * 0.5f;
+  for (int c = 0; c < D; ++c) h[c] = __fmul_rn(zf[c], sc);
   return true;
 }
 
@@ -110,7 +115,7 @@ __device__ Vec3 agent_force_f64(const PackArgs &P, const SimDev &S, uint32_t i, 
   const int64_t cap = P.cap;
   int idx[D];
   unravel<D>(S, v, idx);
-  const uint32_t sub_v = subdomain_of(S, v);
+  const SubRange sub_v = subdomain_range(S, v);
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -124,7 +129,7 @@ __device__ Vec3 agent_force_f64(const PackArgs &P, const SimDev &S, uint32_t i, 
         const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                     : (uint32_t)j0 * S.nvox[1] + j1;
         const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
-                           subdomain_of(S, w) != sub_v;
+                           !sub_v.same(w);
         uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
         if (b0 > b1 || b1 > P.n_agents) b1 = b0;  // recorded by the caller's own scan
         for (uint32_t b = b0; b < b1; ++b) {
@@ -331,7 +336,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     va[c] = P.vel[c * cap + i];
     oa[c] = P.off[c * cap + i];
   }
-  const uint32_t sub_v = subdomain_of(S, v);
+  const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   double acc[D];
   float fs[D], fcmp[D];
@@ -368,6 +373,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
         const bool twice = (m >> 6) & 1u;
 #pragma unroll
         for (int c = 0; c < D; ++c) {
+          nan_seen |= h[c] != h[c];
           kahan_add(fs[c], fcmp[c], h[c]);
           if (twice) kahan_add(fs[c], fcmp[c], h[c]);
         }
@@ -381,7 +387,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
         const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                     : (uint32_t)j0 * S.nvox[1] + j1;
         const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
-                           subdomain_of(S, w) != sub_v;
+                           !sub_v.same(w);
         // centre(a) - centre(b) = -(j - idx) * dx
         float kd[D];
         kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
@@ -500,7 +506,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
     pa[c] = P.pos[c * cap + ii];
     oa[c] = P.off[c * cap + ii];
   }
-  const uint32_t sub_v = subdomain_of(S, v);
+  const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
 #pragma unroll
@@ -518,7 +524,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
     const uint32_t wv = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                  : (uint32_t)j0 * S.nvox[1] + j1;
     sTw[w][g][q] = ((wv == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
-                    subdomain_of(S, wv) != sub_v) ? 2 : 1;
+                    !sub_v.same(wv)) ? 2 : 1;
     const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};
 #pragma unroll
     for (int c = 0; c < D; ++c) sKd[w][g][q][c] = (float)dj[c] * S.dxf[c];
@@ -706,7 +712,7 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
     va[c] = P.vel[c * cap + ii];
     oa[c] = P.off[c * cap + ii];
   }
-  const uint32_t sub_v = subdomain_of(S, v);
+  const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
 #pragma unroll
@@ -754,7 +760,7 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
         }
         const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
                                     : (uint32_t)j0 * S.nvox[1] + j1;
-        twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL || subdomain_of(S, w) != sub_v;
+        twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL || !sub_v.same(w);
         // centre(a) - centre(b) = -(j - idx) * dx
         kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
         kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
