@@ -2,17 +2,20 @@
 """agent-steps/s of the chili mechanics/interaction step on GB300.
 
 One bench step = one complete run of the workload from its initial state: for the default
-workload (rods_2d) 100,000 bacterial rods x 6 vertices, 500 explicit-Euler steps in FP64.
+workload (rods_2d) 100,000 bacterial rods x 6 vertices, the first 400 of its 500
+explicit-Euler steps in FP64 (RODS_TIMED_STEPS below says why).
   value  device-resident throughput: the initial state is restored on the device (crg_snapshot)
-         and the 500 steps run from CUDA graphs; CUDA events on the library's stream bracket
+         and the 400 steps run from CUDA graphs; CUDA events on the library's stream bracket
          the K timed steps; L2 is flushed (256 MiB write) between timed steps.
   e2e    the same run through the public C ABI with host buffers: crg_upload from pinned
          host memory, crg_step, crg_download to host, every bench step.
   cpu_baseline  the oracle (a C++ restatement of chili, multi-threaded by subdomains like
-         chili) on this host's cores: all usable cores (one chili subdomain per thread) on
-         the whole timed run, and one thread on a bounded sample, with the core count and
-         CPU model of the host.  The GPU arm runs the same subdomain weight map.
---impl reference times that CPU implementation alone, with all usable host cores.
+         chili) on this host's cores: all usable cores (one chili subdomain per thread) and
+         one thread, each over the first steps of the same run that fit in about
+         --cpu-seconds (the count is stated in `sample`), with the core count and CPU model
+         of the host.  The GPU arm runs the same subdomain weight map.
+--impl reference times that CPU implementation alone, with all usable host cores, on the
+whole timed run when it takes at most ~20 s on the host, else on its first steps.
 
 Multi-GPU: the path is replicated, not sharded (independent simulations); each rank runs
 the workload on its own GPU and rank 0 reports the sum of agent-steps over the max time.
