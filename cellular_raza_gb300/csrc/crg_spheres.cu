@@ -312,6 +312,8 @@ template <int D, int PREC>
 __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
   extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  // lanes that walk candidates: they meet again after the walk (m_live)
+  const unsigned m_valid = __ballot_sync(0xffffffffu, i < P.n_agents);
   if (i >= P.n_agents) return;
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
   const SimDev &S = P.sims[sim];
@@ -321,7 +323,9 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
   }
-  if (sim_frozen(P, S)) {  // frozen simulation
+  const bool frozen = sim_frozen(P, S);
+  const unsigned m_live = __ballot_sync(m_valid, !frozen);
+  if (frozen) {  // frozen simulation
     frozen_copy(P, i, key, D);
     return;
   }
@@ -475,6 +479,10 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
       if (++ns == kSurv) flush();
     }
   }
+  // Lanes finish the walk at different times; the FP32 evaluation of the buffered survivors
+  // and the FP64 update run with the warp together again (an FP64 warp instruction holds the
+  // pipe whatever its active lanes)
+  __syncwarp(m_live);
   if (PREC != CRG_PREC_F64) {
     flush();
     if (nan_seen) {  // k_spheres_fix computes this agent's force and update in FP64
