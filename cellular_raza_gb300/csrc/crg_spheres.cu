@@ -312,8 +312,6 @@ template <int D, int PREC>
 __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
   extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  // lanes that walk candidates: they meet again after the walk (m_live)
-  const unsigned m_valid = __ballot_sync(0xffffffffu, i < P.n_agents);
   if (i >= P.n_agents) return;
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
   const SimDev &S = P.sims[sim];
@@ -323,9 +321,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     invariant_failed(P.status, kSiteForceKey, i);
     key = S.voxel_off;
   }
-  const bool frozen = sim_frozen(P, S);
-  const unsigned m_live = __ballot_sync(m_valid, !frozen);
-  if (frozen) {  // frozen simulation
+  if (sim_frozen(P, S)) {  // frozen simulation
     frozen_copy(P, i, key, D);
     return;
   }
@@ -385,104 +381,64 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     }
     ns = 0;
   };
-  // The candidates in chili's visiting order -- boxes j0, j1 (, j2) ascending, each box's
-  // agents in cell-list order -- walked as one flat loop: a lane moves on to its next box
-  // (boxes along the last axis are consecutive voxels) without waiting for the other lanes
-  // to finish theirs, so a warp pays the largest per-lane candidate count rather than the
-  // sum over boxes of the per-box maxima.
-  constexpr int L = D - 1;  // last axis
-  const int n1 = (D == 3) ? hi[1] - lo[1] + 1 : 1;
-  const int n_rows = (hi[0] - lo[0] + 1) * n1;
-  int row = 0, jl = lo[L];
-  uint32_t wrow = 0, w = 0, b = 0, b_end = 0, raw_end = 0;
-  float kd[D];
-  bool twice = false;
-  // box (row, jl): voxel w, candidate range [b, b_end), its offset kd and pair weight
-  auto open_box = [&](bool new_row) {
-    if (new_row) {
-      const int j0 = lo[0] + row / n1;
-      kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-      if (D == 3) {
-        const int j1 = lo[1] + row % n1;
+  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
+    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
+      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
+                           !sub_v.same(w);
+        // centre(a) - centre(b) = -(j - idx) * dx
+        float kd[D];
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
         kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
-        wrow = ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2];
-      } else {
-        wrow = (uint32_t)j0 * S.nvox[1];
-      }
-      jl = lo[L];
-      w = wrow + jl;
-      b = P.start[S.voxel_off + w];
-    } else {
-      ++jl;
-      ++w;
-      b = raw_end;  // start[w], loaded as the previous box's end
-    }
-    kd[L] = (float)(jl - idx[L]) * S.dxf[L];
-    raw_end = P.start[S.voxel_off + w + 1];
-    b_end = raw_end;
-    if (b > b_end || b_end > P.n_agents) {
-      invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-      b_end = b;
-    }
-    twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL || !sub_v.same(w);
-  };
-  open_box(true);
-  while (true) {
-    if (b >= b_end) {
-      if (jl < hi[L]) {
-        open_box(false);
-      } else if (++row < n_rows) {
-        open_box(true);
-      } else {
-        break;
-      }
-      continue;
-    }
-    const uint32_t bb = b++;
-    if (bb == i) continue;
-    float zf[D];
-    float d2 = 0.0f;
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
+        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
+        if (b0 > b1 || b1 > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b1 = b0;
+        }
+        for (uint32_t b = b0; b < b1; ++b) {
+          if (b == i) continue;
+          float zf[D];
+          float d2 = 0.0f;
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-      zf[c] = (oa[c] - P.off[c * cap + bb]) - kd[c];
-      d2 = fmaf(zf[c], zf[c], d2);
-    }
-    if (d2 > thr2) continue;  // NaN falls through to the exact path
-    if (PREC == CRG_PREC_F64) {
-      double z[D], h[D];
+          for (int c = 0; c < D; ++c) {
+            zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
+            d2 = fmaf(zf[c], zf[c], d2);
+          }
+          if (d2 > thr2) continue;  // NaN falls through to the exact path
+          if (PREC == CRG_PREC_F64) {
+            double z[D], h[D];
 #pragma unroll
-      for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + bb]);
-      if (morse_half_f64<D>(z, S, h)) {
+            for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
+            if (morse_half_f64<D>(z, S, h)) {
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-          acc[c] = dadd(acc[c], h[c]);
-          if (twice) acc[c] = dadd(acc[c], h[c]);
+              for (int c = 0; c < D; ++c) {
+                acc[c] = dadd(acc[c], h[c]);
+                if (twice) acc[c] = dadd(acc[c], h[c]);
+              }
+            }
+          } else {
+            // FP32 Morse on the FP32 displacement (offsets from the voxel centres, accurate
+            // to 2^-25 dx).  Whether the pair interacts is decided exactly as on the FP64
+            // path: pairs whose FP32 distance lies within the prefilter margin of the cutoff
+            // or of zero are decided from the FP64 distance, so no pair switches on or off
+            // relative to FP64.  A NaN displacement (an offset marked NaN because its agent
+            // is far outside its voxel, or NaN positions) hands the whole agent to the FP64
+            // fix-up kernel.
+            if (d2 != d2) {
+              nan_seen = true;
+              continue;
+            }
+            const int dj2 = (D == 3) ? j2 - idx[D - 1] : 0;
+            sB[ns * bd + tid] = b;
+            sM[ns * bd + tid] = (uint8_t)((j0 - idx[0] + 1) | ((j1 - idx[1] + 1) << 2) |
+                                          ((dj2 + 1) << 4) | (twice ? 0x40 : 0));
+            if (++ns == kSurv) flush();
+          }
         }
       }
-    } else {
-      // FP32 Morse on the FP32 displacement (offsets from the voxel centres, accurate to
-      // 2^-25 dx).  Whether the pair interacts is decided exactly as on the FP64 path: pairs
-      // whose FP32 distance lies within the prefilter margin of the cutoff or of zero are
-      // decided from the FP64 distance, so no pair switches on or off relative to FP64.  A
-      // NaN displacement (an offset marked NaN because its agent is far outside its voxel,
-      // or NaN positions) hands the whole agent to the FP64 fix-up kernel.
-      if (d2 != d2) {
-        nan_seen = true;
-        continue;
-      }
-      const int d0 = lo[0] + row / n1 - idx[0];
-      const int d1 = (D == 3) ? lo[1] + row % n1 - idx[1] : jl - idx[1];
-      const int d2b = (D == 3) ? jl - idx[L] : 0;
-      sB[ns * bd + tid] = bb;
-      sM[ns * bd + tid] =
-          (uint8_t)((d0 + 1) | ((d1 + 1) << 2) | ((d2b + 1) << 4) | (twice ? 0x40 : 0));
-      if (++ns == kSurv) flush();
-    }
-  }
-  // Lanes finish the walk at different times; the FP32 evaluation of the buffered survivors
-  // and the FP64 update run with the warp together again (an FP64 warp instruction holds the
-  // pipe whatever its active lanes)
-  __syncwarp(m_live);
   if (PREC != CRG_PREC_F64) {
     flush();
     if (nan_seen) {  // k_spheres_fix computes this agent's force and update in FP64
