@@ -381,64 +381,95 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     }
     ns = 0;
   };
-  for (int j0 = lo[0]; j0 <= hi[0]; ++j0)
-    for (int j1 = lo[1]; j1 <= hi[1]; ++j1)
-      for (int j2 = lo[2]; j2 <= hi[2]; ++j2) {
-        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
-                                    : (uint32_t)j0 * S.nvox[1] + j1;
-        const bool twice = (w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL ||
-                           !sub_v.same(w);
-        // centre(a) - centre(b) = -(j - idx) * dx
-        float kd[D];
-        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
-        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
-        uint32_t b0 = P.start[S.voxel_off + w], b1 = P.start[S.voxel_off + w + 1];
-        if (b0 > b1 || b1 > P.n_agents) {
-          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
-          b1 = b0;
+  // Candidates in chili's visiting order: boxes j0, j1 (, j2) ascending, each box's agents
+  // in cell-list order.  The up to three boxes along the last axis are consecutive voxels,
+  // so each row of them is one contiguous candidate range; a candidate's box (its offset kd
+  // on the last axis and its pair weight) follows from two compares with the box bounds.
+  constexpr int L = D - 1;  // last axis
+  const int nb = hi[L] - lo[L] + 1;  // boxes per row (1..3)
+  float kdl[3];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) kdl[q] = (float)(lo[L] + q - idx[L]) * S.dxf[L];
+  const int n1 = (D == 3) ? hi[1] - lo[1] + 1 : 1;
+  const int n_rows = (hi[0] - lo[0] + 1) * n1;
+  for (int row = 0; row < n_rows; ++row) {
+    const int j0 = lo[0] + row / n1;
+    const int j1 = (D == 3) ? lo[1] + row % n1 : 0;
+    float kd[D];
+    kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+    if (D == 3) kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+    const uint32_t w0 = ((D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2]
+                                  : (uint32_t)j0 * S.nvox[1]) + lo[L];
+    // box bounds s[0..nb]; a box whose range is not valid is reported and left empty
+    uint32_t sb[4];
+    sb[0] = P.start[S.voxel_off + w0];
+    uint32_t tw_bits = 0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      if (q < nb) {
+        uint32_t e = P.start[S.voxel_off + w0 + q + 1];
+        if (sb[q] > e || e > P.n_agents) {
+          invariant_failed(P.status, kSiteForceRange, S.voxel_off + w0 + q);
+          e = sb[q];
         }
-        for (uint32_t b = b0; b < b1; ++b) {
-          if (b == i) continue;
-          float zf[D];
-          float d2 = 0.0f;
+        sb[q + 1] = e;
+        const uint32_t w = w0 + q;
+        if ((w == v) || S.weight_mode == CRG_WEIGHTS_PHYSICAL || !sub_v.same(w))
+          tw_bits |= 1u << q;
+      } else {
+        sb[q + 1] = sb[q];
+      }
+    }
+    // the bounds are non-decreasing (an invalid box was left empty), so [sb[0], sb[nb]) is
+    // the row's candidates box after box (in a cell list that failed its checks, a box left
+    // empty may hand its range to the next one: the step reports CRG_EINTERNAL and rolls back)
+    {
+      for (uint32_t b = sb[0]; b < sb[nb]; ++b) {
+        const int q = (int)(b >= sb[1]) + (int)(b >= sb[2]);
+        if (b == i) continue;
+        kd[L] = (q == 0) ? kdl[0] : (q == 1) ? kdl[1] : kdl[2];
+        const bool twice = (tw_bits >> q) & 1u;
+        float zf[D];
+        float d2 = 0.0f;
 #pragma unroll
-          for (int c = 0; c < D; ++c) {
-            zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
-            d2 = fmaf(zf[c], zf[c], d2);
-          }
-          if (d2 > thr2) continue;  // NaN falls through to the exact path
-          if (PREC == CRG_PREC_F64) {
-            double z[D], h[D];
+        for (int c = 0; c < D; ++c) {
+          zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
+          d2 = fmaf(zf[c], zf[c], d2);
+        }
+        if (d2 > thr2) continue;  // NaN falls through to the exact path
+        if (PREC == CRG_PREC_F64) {
+          double z[D], h[D];
 #pragma unroll
-            for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
-            if (morse_half_f64<D>(z, S, h)) {
+          for (int c = 0; c < D; ++c) z[c] = dsub(pa[c], P.pos[c * cap + b]);
+          if (morse_half_f64<D>(z, S, h)) {
 #pragma unroll
-              for (int c = 0; c < D; ++c) {
-                acc[c] = dadd(acc[c], h[c]);
-                if (twice) acc[c] = dadd(acc[c], h[c]);
-              }
+            for (int c = 0; c < D; ++c) {
+              acc[c] = dadd(acc[c], h[c]);
+              if (twice) acc[c] = dadd(acc[c], h[c]);
             }
-          } else {
-            // FP32 Morse on the FP32 displacement (offsets from the voxel centres, accurate
-            // to 2^-25 dx).  Whether the pair interacts is decided exactly as on the FP64
-            // path: pairs whose FP32 distance lies within the prefilter margin of the cutoff
-            // or of zero are decided from the FP64 distance, so no pair switches on or off
-            // relative to FP64.  A NaN displacement (an offset marked NaN because its agent
-            // is far outside its voxel, or NaN positions) hands the whole agent to the FP64
-            // fix-up kernel.
-            if (d2 != d2) {
-              nan_seen = true;
-              continue;
-            }
-            const int dj2 = (D == 3) ? j2 - idx[D - 1] : 0;
-            sB[ns * bd + tid] = b;
-            sM[ns * bd + tid] = (uint8_t)((j0 - idx[0] + 1) | ((j1 - idx[1] + 1) << 2) |
-                                          ((dj2 + 1) << 4) | (twice ? 0x40 : 0));
-            if (++ns == kSurv) flush();
           }
+        } else {
+          // FP32 Morse on the FP32 displacement (offsets from the voxel centres, accurate
+          // to 2^-25 dx).  Whether the pair interacts is decided exactly as on the FP64
+          // path: pairs whose FP32 distance lies within the prefilter margin of the cutoff
+          // or of zero are decided from the FP64 distance, so no pair switches on or off
+          // relative to FP64.  A NaN displacement (an offset marked NaN because its agent
+          // is far outside its voxel, or NaN positions) hands the whole agent to the FP64
+          // fix-up kernel.
+          if (d2 != d2) {
+            nan_seen = true;
+            continue;
+          }
+          const int dl = lo[L] + q - idx[L];
+          const int d1 = (D == 3) ? j1 - idx[1] : dl;
+          sB[ns * bd + tid] = b;
+          sM[ns * bd + tid] = (uint8_t)((j0 - idx[0] + 1) | ((d1 + 1) << 2) |
+                                        (((D == 3) ? dl : 0) + 1) << 4 | (twice ? 0x40 : 0));
+          if (++ns == kSurv) flush();
         }
       }
+    }
+  }
   if (PREC != CRG_PREC_F64) {
     flush();
     if (nan_seen) {  // k_spheres_fix computes this agent's force and update in FP64
