@@ -309,7 +309,7 @@ constexpr int kSurv = 16;
 constexpr size_t mixed_step_smem(int block) { return (size_t)kSurv * block * 5; }
 
 template <int D, int PREC>
-__global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
+__global__ void __launch_bounds__(256, 3) k_spheres_step(const PackArgs P) {
   extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n_agents) return;
@@ -426,7 +426,6 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     {
       for (uint32_t b = sb[0]; b < sb[nb]; ++b) {
         const int q = (int)(b >= sb[1]) + (int)(b >= sb[2]);
-        if (b == i) continue;
         kd[L] = (q == 0) ? kdl[0] : (q == 1) ? kdl[1] : kdl[2];
         const bool twice = (tw_bits >> q) & 1u;
         float zf[D];
@@ -436,7 +435,9 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
           zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
           d2 = fmaf(zf[c], zf[c], d2);
         }
-        if (d2 > thr2) continue;  // NaN falls through to the exact path
+        // the agent itself and pairs beyond the prefilter threshold are skipped (one branch;
+        // a NaN distance falls through to the exact path)
+        if (b == i || d2 > thr2) continue;
         if (PREC == CRG_PREC_F64) {
           double z[D], h[D];
 #pragma unroll
