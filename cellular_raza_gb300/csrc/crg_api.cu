@@ -64,6 +64,7 @@ struct crg_ctx {
   uint32_t *h_ndiv = nullptr;  // pinned
   double *frc = nullptr;
   float2 *hl = nullptr;  // mixed-precision rods: hi / lo split of the positions
+  double *vcen = nullptr;  // voxel centres of every simulation and axis (SimDev::cen_off)
   double *fbuf = nullptr;  // crg_forces: the interaction force of every slot
   double *staging = nullptr;
   char *snap = nullptr;  // crg_snapshot buffer
@@ -315,7 +316,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->hl, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
+                  c->step_ctr, c->dbg_force, c->frc, c->hl, c->vcen, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
                   c->staging, c->snap, c->slen, c->nslen, c->grate, c->ngrate, c->parent,
                   c->nparent, c->vctr, c->nsense, c->dflag, c->dpre, c->dbsum, c->srank};
   for (void *p : ptrs)
@@ -453,7 +454,22 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
   c->n_vox = (uint32_t)vox;
   c->cap = std::max<int64_t>(cap, 1);
   c->agent_off_h.assign(n_sims + 1, 0);
+  // voxel centres min + (idx + 1/2) dx, per simulation and axis, rounded once (fma) as the
+  // device expression voxel_centre rounds them; the sort reads them for the FP32 offsets
+  std::vector<double> cen;
+  for (int s = 0; s < n_sims; ++s)
+    for (int a = 0; a < 3; ++a) {
+      const SimDev &S = c->sims_h[s];
+      c->sims_h[s].cen_off[a] = (uint32_t)cen.size();
+      if (a < c->dim)
+        for (int32_t k = 0; k < S.nvox[a]; ++k)
+          cen.push_back(std::fma((double)k + 0.5, S.dx[a], S.min[a]));
+    }
   int32_t r = allocate(c);
+  if (r == CRG_OK) r = dalloc(&c->vcen, cen.size());
+  if (r == CRG_OK && cudaMemcpy(c->vcen, cen.data(), sizeof(double) * cen.size(),
+                                cudaMemcpyHostToDevice) != cudaSuccess)
+    r = CRG_ECUDA;
   if (r == CRG_OK && c->kind == CRG_KIND_ROD && crg::prepare_rods(c->dim, c->nv) != 0)
     r = CRG_ECUDA;
   if (r != CRG_OK) {
@@ -526,6 +542,7 @@ SortArgs sort_args(crg_ctx *c, int initial) {
   SortArgs A;
   std::memset(&A, 0, sizeof(A));
   A.sims = c->d_sims;
+  A.vcen = c->vcen;
   A.sim_agent_off = c->d_agent_off;
   A.sim_of_voxel = c->d_sim_of_voxel;
   A.n_sims = c->n_sims;

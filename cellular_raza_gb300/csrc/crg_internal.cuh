@@ -25,6 +25,7 @@ struct SimDev {
   int32_t nvox[3];
   double min[3], max[3], dx[3];
   long long min_key[3], max_key[3];  // f64_order_key of min and max (boundary compares)
+  uint32_t cen_off[3];  // first entry of each axis's voxel centres in the pack's table
   float dxf[3];
   float inv_dxf[3];  // (float)(1 / dx): the FP32 voxel-index estimate (voxel_of)
   uint32_t voxel_off, n_vox;
@@ -293,7 +294,8 @@ __device__ __forceinline__ void unravel(const SimDev &S, uint32_t v, int *idx) {
   }
 }
 
-// Centre of voxel idx in FP64: min + (idx + 1/2) dx.  The FP32 offsets are taken from it
+// Centre of voxel idx in FP64: min + (idx + 1/2) dx (one rounding, as an FMA; the sort reads
+// the same values from the pack's table, built on the host with std::fma).  The FP32 offsets are taken from it
 // (|offset| <= dx / 2 inside the voxel, so their rounding is half that of corner offsets);
 // only differences of offsets and of centres, (j - idx) dx, enter the kernels.
 __device__ __forceinline__ double voxel_centre(const SimDev &S, int axis, int idx) {

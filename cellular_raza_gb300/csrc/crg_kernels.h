@@ -24,6 +24,7 @@ struct SortArgs {
   uint64_t *id;
   uint32_t *key;
   float *off;
+  const double *vcen;  // voxel centres per simulation and axis (SimDev::cen_off)
   double *hist;
   uint8_t *hmeta;
   // updated state in the previous order (read by the gather)

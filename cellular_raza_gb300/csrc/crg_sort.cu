@@ -333,7 +333,7 @@ __global__ void k_gather(const SortArgs A) {
     A.pos[c * cap + s] = p;
     A.vel[c * cap + s] = A.nvel[c * cap + src];
     const int axis = c % dim;
-    const double centre = voxel_centre(S, axis, idx[axis]);
+    const double centre = A.vcen[S.cen_off[axis] + idx[axis]];  // voxel_centre, tabled
     float o = (float)(p - centre);
     // Offsets far outside the voxel (an agent kept in its old voxel because its new index
     // fell outside the grid) would weaken the prefilter's error bound: mark them NaN so

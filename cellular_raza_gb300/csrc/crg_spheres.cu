@@ -309,7 +309,7 @@ constexpr int kSurv = 16;
 constexpr size_t mixed_step_smem(int block) { return (size_t)kSurv * block * 5; }
 
 template <int D, int PREC>
-__global__ void __launch_bounds__(256, 3) k_spheres_step(const PackArgs P) {
+__global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
   extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.n_agents) return;
