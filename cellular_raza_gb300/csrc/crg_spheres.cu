@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
       return;
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) acc[c] = (double)fs[c] - (double)fcmp[c];
+    for (int c = 0; c < D; ++c) acc[c] = (double)__fsub_rn(fs[c], fcmp[c]);  // the compensated sum, rounded once
   }
   sphere_update<D>(P, S, i, key, pa, va, acc);
 }
@@ -926,7 +926,7 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
       return;
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) acc[c] = (double)fs[c] - (double)fcmp[c];
+    for (int c = 0; c < D; ++c) acc[c] = (double)__fsub_rn(fs[c], fcmp[c]);  // the compensated sum, rounded once
   }
   sphere_update<D>(P, S, i, key, pa, va, acc);
 }
