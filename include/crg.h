@@ -347,13 +347,14 @@ int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
  *              ascending, input order inside a voxel) -- the order crg_upload produces
  *   start_out  device [n_voxels + 1]: first slot of every voxel, start_out[n_voxels] = n
  *   stream     cudaStream_t to run on (NULL: the default stream); the call synchronizes
- *              it before returning (it reads the status word back)
+ *              it before returning (it reads the status word back), so it cannot be
+ *              called while that stream is being captured
  *
  * Limits: n <= CRG_NOALLOC_MAX_POINTS and n_voxels <= CRG_NOALLOC_MAX_VOXELS, otherwise
  * CRG_EINVAL before anything runs.  All calls share the scratch array: calls that overlap
  * on the GPU (different streams or threads at the same time) race and must be serialised
  * by the caller.  The first call on a device looks up the scratch address on that device
- * (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * (cudaGetSymbolAddress). */
 #define CRG_NOALLOC_MAX_POINTS (1 << 20)
 #define CRG_NOALLOC_MAX_VOXELS (1 << 20)
 int32_t crg_cell_list_noalloc(const crg_domain *domain, int64_t n, const double *pos_dev,
