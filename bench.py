@@ -458,6 +458,18 @@ def extra_rods_mixed(torch, n_sub):
     out["force_per_rod_rel_err_p9999"] = float(np.percentile(per_rod, 99.99))
     for k in (1, 10, w.n_steps):
         out[f"pos_normwise_rel_err_{k}_steps"] = normwise(res[("mixed", k)], res[("f64", k)])
+        a, b = res[("mixed", k)], res[("f64", k)]
+        per_rod = (np.linalg.norm((a - b).reshape(w.n, -1), axis=1) /
+                   np.linalg.norm(b.reshape(w.n, -1), axis=1))
+        out[f"pos_max_rel_err_per_rod_{k}_steps"] = float(per_rod.max())
+    # the same comparison under physical pair weights (every pair weight 1)
+    for k in (10, w.n_steps):
+        ph = {}
+        for prec in ("mixed", "f64"):
+            m = w.model.replace(precision=prec, weight_mode=1)
+            ph[prec] = E.run(w.__class__(w.name, m, w.pos, w.vel, k), k)["pos"]
+        out[f"physical_weights_pos_normwise_rel_err_{k}_steps"] = normwise(ph["mixed"],
+                                                                           ph["f64"])
     out["speedup_mixed_over_f64"] = out["mixed_agent_steps_per_s"] / out["f64_agent_steps_per_s"]
     return out
 
