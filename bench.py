@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--case-precision", default=None, choices=[None, "f64", "mixed"])
     p.add_argument("--case-variant", type=int, default=0, help="CRG_OPT_KERNEL_VARIANT")
     p.add_argument("--case-workload", default=None,
-                   choices=[None, "rods_2d", "spheres_3d", "spheres_3d_large"])
+                   choices=[None, "rods_2d", "spheres_3d", "spheres_3d_large", "rod_colony"])
     # the served form over several arrival rates (minutes of GPU time: not in the default run)
     p.add_argument("--served-sweep", action="store_true",
                    help="run the request stream at --sweep-rates and print one JSON line")
@@ -558,10 +558,27 @@ def extra_cycle(n_rods=2000, steps=600):
             sim.step(1)
         dt = time.perf_counter() - t0
         n_end = sim.n_agents
-    return {"workload": "rod_colony", "agents_start": w.n, "agents_end": n_end,
-            "steps": steps, "dim": w.model.dim, "vertices_per_agent": w.model.n_vertices,
-            "agent_steps_per_s": agent_steps / dt, "ms_per_step": dt * 1e3 / steps,
-            "timing": "wall clock around the crg_step calls"}
+    out = {"workload": "rod_colony", "agents_start": w.n, "agents_end": n_end,
+           "steps": steps, "dim": w.model.dim, "vertices_per_agent": w.model.n_vertices,
+           "agent_steps_per_s": agent_steps / dt, "ms_per_step": dt * 1e3 / steps,
+           "timing": "wall clock around the crg_step calls"}
+    # the oracle's colony on the host's cores (one chili subdomain per thread), the same run
+    try:
+        import pyoracle
+
+        pyoracle.build()
+        t0 = time.perf_counter()
+        res = pyoracle.run_cycle(w.model, w.pos, w.vel, steps, spring_length=w.spring_length)
+        cpu_s = time.perf_counter() - t0
+        # agent-steps of the oracle's run: its count grows like the GPU's (same final count)
+        out["cpu_oracle"] = {"agents_end": int(len(res["ids"])), "seconds": cpu_s,
+                             "agent_steps_per_s": agent_steps / cpu_s,
+                             "threads": n_subdomains(), **host_cpu(),
+                             "note": "wall clock of the oracle's whole run, agent-steps "
+                                     "counted on the GPU run"}
+    except Exception as e:  # reported, not fatal
+        out["cpu_oracle"] = {"error": f"{type(e).__name__}: {e}"}
+    return out
 
 
 def served_stream(n_requests, rate_hz, seed=2024):
@@ -860,10 +877,13 @@ def profile_case(args):
     if args.case_precision:
         kw["precision"] = args.case_precision
     w = getattr(W, args.case_workload or args.workload)(seed=2024, **kw)
-    with E.Simulation.single(w.model, w.n) as sim:
+    cycle = getattr(w.model, "cycle", False)
+    with E.Simulation.single(w.model, 16 * w.n if cycle else w.n) as sim:
         sim.set_option(N.OPT_GRAPH_CHUNK, 0)
         sim.set_option(N.OPT_KERNEL_VARIANT, args.case_variant)
         sim.upload(w.pos, w.vel)
+        if cycle:
+            sim.set_spring_lengths(w.spring_length)
         t = time.perf_counter()
         sim.step(args.case_steps)
         sim.download()
