@@ -239,6 +239,21 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   double thr = std::fabs(m.cutoff) + margin;
   S.off_lim = (float)off_lim;
   S.band_f = (float)margin;
+  if (m.kind == CRG_KIND_ROD) {
+    // mixed rods take their distances from hi / lo coordinates (relative error ~1e-6,
+    // absolute ~2^-47 of the largest coordinate): 1e-5 of the cutoff, and 64 x 2^-47 of the
+    // largest coordinate near zero
+    double xmax = 0.0;
+    for (int i = 0; i < d.dim; ++i)
+      xmax = std::max(xmax, std::max(std::fabs(d.min[i]), std::fabs(d.max[i])));
+    const double zero = 64.0 * std::ldexp(xmax + ext, -47) + 1e-30;
+    S.mix_zero_f = (float)zero;
+    S.mix_band_f = (float)(1e-5 * std::fabs(m.cutoff) + zero);
+  } else {
+    // mixed spheres take their displacements from the FP32 offsets, within err per axis
+    S.mix_zero_f = (float)(4.0 * err);
+    S.mix_band_f = (float)(4.0 * err + std::ldexp(std::fabs(m.cutoff), -20));
+  }
   S.filt_thr2 = (float)(thr * thr);
   if (!std::isfinite(S.filt_thr2)) S.filt_thr2 = __builtin_inff();
   return CRG_OK;

@@ -527,8 +527,8 @@ __device__ __forceinline__ void diff_hl(float2 a, float2 b, float &hi, float &lo
 // carried as hi + lo pairs, z = (x - l0) - t (l1 - l0) is formed from them, and for an
 // interior nearest point one projection step removes the along-segment error that the
 // FP32 t leaves in z.  Then the direction of the force is accurate to a few FP32 ulps and
-// its magnitude to the FP32 distance.  A pair whose FP32 distance lies within the
-// prefilter margin of the cutoff or of zero is decided from the FP64 distance; a NaN
+// its magnitude to the FP32 distance.  A pair whose FP32 distance lies within mix_band_f of
+// the cutoff or mix_zero_f of zero is decided from the FP64 distance; a NaN
 // distance (NaN or infinite coordinates, a degenerate segment) or a force beyond the FP32
 // range takes the FP64 item.
 template <int D>
@@ -569,7 +569,7 @@ __device__ __forceinline__ bool mixed_item(int vx, int sy, const float2 *hp, con
   for (int c = 0; c < D; ++c) d2 = __fmaf_rn(z[c], z[c], d2);
   if (d2 == d2) {
     const float dist = __fsqrt_rn(d2);
-    if (fabsf(__fsub_rn(dist, S.cutoff_f)) <= S.band_f || dist <= S.band_f) {
+    if (fabsf(__fsub_rn(dist, S.cutoff_f)) <= S.mix_band_f || dist <= S.mix_zero_f) {
       if (!interacts_f64<D>(vx, sy, pp, ps, cap, S)) return false;
     } else if (dist > S.cutoff_f) {
       return false;

@@ -69,9 +69,9 @@ __device__ __forceinline__ bool morse_half_f64_batch(const double *z, const SimD
 
 // Mixed path: FP32 Morse half force of agent a (FP64 position pa) from partner b at FP32
 // displacement zf, |zf|^2 = d2 (not NaN).  Whether the pair interacts is decided exactly as
-// on the FP64 path: a pair whose FP32 distance lies within the prefilter margin of the
-// cutoff or of zero is decided from the FP64 distance, so no pair switches on or off
-// relative to FP64.  Shared by the mixed kernels so they produce the same bits.
+// on the FP64 path: a pair whose FP32 distance lies within a few times its error bound of
+// the cutoff (mix_band_f) or of zero (mix_zero_f) is decided from the FP64 distance, so no
+// pair switches on or off relative to FP64.  Shared by the mixed kernels so they produce the same bits.
 template <int D>
 __device__ __forceinline__ bool mixed_half(const PackArgs &P, const SimDev &S, const double *pa,
                                            uint32_t b, const float *zf, float d2, float *h) {
@@ -79,7 +79,7 @@ __device__ __forceinline__ bool mixed_half(const PackArgs &P, const SimDev &S, c
   const float rinv = rsqrtf(d2);
   const float dist = d2 > 0.0f ? __fmul_rn(d2, rinv) : 0.0f;
   bool in;
-  if (fabsf(dist - S.cutoff_f) <= S.band_f || dist <= S.band_f) {
+  if (fabsf(dist - S.cutoff_f) <= S.mix_band_f || dist <= S.mix_zero_f) {
     double n2 = 0.0;
 #pragma unroll
     for (int c = 0; c < D; ++c) {
