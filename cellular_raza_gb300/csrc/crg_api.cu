@@ -9,6 +9,7 @@
 // and runs on the handle's stream; steps are captured into CUDA graphs in chunks.
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -134,6 +135,28 @@ bool decomp_res(uint64_t n_voxel, uint64_t n_regions, uint64_t &n_out, uint64_t 
 }
 
 // Fills the geometry and parameters of one simulation descriptor.
+// Bits of the largest x >= 0 with sqrt(x) < r in round-to-nearest (-1 when there is none):
+// sqrt is correctly rounded on host and device alike and monotone, so sqrt(x) < r holds
+// exactly for the x at or below this one.
+long long sense_threshold_bits(double r) {
+  if (!(r > 0.0)) return -1;  // sqrt(x) >= 0 is never below r <= 0 (or NaN)
+  if (std::isinf(r)) {
+    const double big = std::numeric_limits<double>::max();
+    long long b;
+    std::memcpy(&b, &big, sizeof(b));
+    return b;
+  }
+  double x = r * r;
+  while (x > 0.0 && !(std::sqrt(x) < r)) x = std::nextafter(x, 0.0);
+  while (std::isfinite(std::nextafter(x, INFINITY)) &&
+         std::sqrt(std::nextafter(x, INFINITY)) < r)
+    x = std::nextafter(x, INFINITY);
+  if (!(std::sqrt(x) < r)) return -1;
+  long long b;
+  std::memcpy(&b, &x, sizeof(b));
+  return b;
+}
+
 int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   std::memset(&S, 0, sizeof(S));
   if (d.dim != 2 && d.dim != 3) return CRG_EINVAL;
@@ -198,6 +221,7 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   S.cyc_growth = m.growth_rate;
   S.cyc_div_len = m.division_length;
   S.cyc_sense = m.sense_range;
+  S.cyc_sense_x2 = sense_threshold_bits(m.sense_range);
   S.cyc_sat = m.sense_saturation;
   S.mrs_r = m.radius + m.radius;
   S.mrs_k = (-2.0 * m.strength) * m.stiffness;

@@ -67,6 +67,9 @@ struct SimDev {
   // cell cycle (rods): base growth rate, division length, sensing range and saturation
   int32_t cycle;
   double cyc_growth, cyc_div_len, cyc_sense, cyc_sat;
+  // bits of the largest squared distance x with RN(sqrt(x)) < cyc_sense (RN o sqrt is
+  // monotone, so the sensing test is one integer compare of the bits of x >= 0), -1 if none
+  long long cyc_sense_x2;
 };
 
 // Arguments shared by the per-step kernels of a pack.
