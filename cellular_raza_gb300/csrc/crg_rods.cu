@@ -1351,164 +1351,32 @@ __global__ void __launch_bounds__(32, 24) k_rods_passq(const PackArgs P) {
   }
 }
 
-// Mixed precision: the passes of the list, 32 consecutive ones per warp and round (one per
-// lane).  Each lane runs the FP32 prefilter of its pass (the survivor mask of mixed_pass);
-// the survivors of the warp go to a list in shared memory and are evaluated by all lanes
-// (mixed_item), 128 at a time; then each lane adds its own pass's items in mask order into
-// its rows and stores them -- the operations and the order of mixed_pass, so the result is
-// bit for bit that of the rod-level fallback, with the FP32 evaluation on full lanes
-// instead of on the lanes whose pass still has survivors left.
-constexpr int kMixChunk = 128;
-
+// Mixed precision: the passes of the list, one per thread (grid-stride), each pass's M / 2
+// as FP32 to its slot of the pass buffer for k_rods_update's mixed fold.
 template <int D, int NV>
 __global__ void __launch_bounds__(128) k_rods_passmix(const PackArgs P) {
-  constexpr int NC = NV * D, NE = NV - 1;
-  __shared__ float sF[4][D][kMixChunk];   // item force on the vertex
-  __shared__ float sTt[4][kMixChunk];     // item t
-  __shared__ uint16_t sItem[4][kMixChunk];  // owner lane << 8 | mask bit; bit 15: in range
-  __shared__ uint32_t sA[4][32], sB[4][32], sSim[4][32];
-  __shared__ uint8_t sExt[4][32];
+  constexpr int NC = NV * D;
   if (P.rctl[3]) return;  // overflow: the rod-level kernel computes this step
-  const int lane = threadIdx.x & 31, wb = threadIdx.x >> 5;
   const uint32_t total = P.rctl[0];
   const int64_t cap = P.cap;
   float *mb = reinterpret_cast<float *>(P.mbuf);
   const float inf = __int_as_float(0x7f800000);
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t base = (blockIdx.x * (blockDim.x >> 5) + wb) * 32u; base < total;
-       base += warps * 32u) {
-    const uint32_t t = base + lane;
-    const bool have = t < total;
-    uint32_t a = 0, b = 0, sim = 0;
-    bool is_ext = false;
-    uint64_t mask = 0;
-    if (have) {
-      a = P.pass_a[t];
-      b = P.pass_b[t];
-      const uint32_t meta = P.pass_meta[t];
-      is_ext = (meta & 1u) != 0u;
-      sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, a);
-      const SimDev &S = P.sims[sim];
-      const float thr2 = P.prefilter ? S.filt_thr2 : inf;
-      float kd[D];
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += gridDim.x * blockDim.x) {
+    const uint32_t a = P.pass_a[t], b = P.pass_b[t], meta = P.pass_meta[t];
+    const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, a);
+    const SimDev &S = P.sims[sim];
+    float kd[D];
 #pragma unroll
-      for (int c = 0; c < D; ++c) kd[c] = (float)((int)((meta >> (1 + 2 * c)) & 3u) - 1) * S.dxf[c];
-      float oa[NC], ob[NC];
+    for (int c = 0; c < D; ++c) kd[c] = (float)((int)((meta >> (1 + 2 * c)) & 3u) - 1) * S.dxf[c];
+    float oa[NC], ob[NC];
 #pragma unroll
-      for (int k = 0; k < NC; ++k) {
-        oa[k] = P.off[k * cap + a];
-        ob[k] = P.off[k * cap + b] + kd[k % D];
-      }
-#pragma unroll
-      for (int vx = 0; vx < NV; ++vx)
-#pragma unroll
-        for (int sy = 0; sy < NE; ++sy) {
-          float p32[D], l0[D], l1[D];
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            p32[c] = is_ext ? ob[vx * D + c] : oa[vx * D + c];
-            l0[c] = is_ext ? oa[sy * D + c] : ob[sy * D + c];
-            l1[c] = is_ext ? oa[(sy + 1) * D + c] : ob[(sy + 1) * D + c];
-          }
-          if (!(seg_dist2_f32<D>(p32, l0, l1) > thr2))
-            mask |= 1ull << (is_ext ? sy * NV + vx : vx * NE + sy);
-        }
+    for (int k = 0; k < NC; ++k) {
+      oa[k] = P.off[k * cap + a];
+      ob[k] = P.off[k * cap + b] + kd[k % D];
     }
-    sA[wb][lane] = a;
-    sB[wb][lane] = b;
-    sSim[wb][lane] = sim;
-    sExt[wb][lane] = is_ext ? 1 : 0;
-    // this lane's items are [first, first + cnt) of the warp's list
-    const uint32_t cnt = (uint32_t)__popcll(mask);
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const uint32_t n_items = __shfl_sync(0xffffffffu, incl, 31);
-    const uint32_t first = incl - cnt;
-    // the fold of mixed_pass as a stream over this lane's items in mask order
-    const int n_grp = is_ext ? NE : NV, g_size = is_ext ? NV : NE;
-    int g = 0;  // the open group (its row not stored yet)
-    float cs[D], cc[D], ns[D], nc[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) cs[k] = cc[k] = ns[k] = nc[k] = 0.f;
-    float *out = mb + t;
-    const int64_t stride = P.pass_cap;
-    auto close_group = [&]() {
-#pragma unroll
-      for (int k = 0; k < D; ++k) {
-        out[(g * D + k) * stride] = __fmul_rn(__fsub_rn(cs[k], cc[k]), 0.5f);
-        cs[k] = ns[k];
-        cc[k] = nc[k];
-        ns[k] = nc[k] = 0.f;
-      }
-      ++g;
-    };
-    uint64_t rest = mask;  // this lane's items not yet listed
-    for (uint32_t c0 = 0; c0 < n_items; c0 += kMixChunk) {
-      const uint32_t c1 = min(c0 + (uint32_t)kMixChunk, n_items);
-      // list the items of [c0, c1) that are this lane's, in mask order
-      for (uint32_t k = max(first, c0); k < min(first + cnt, c1); ++k) {
-        const int bit = __ffsll((long long)rest) - 1;
-        rest &= rest - 1ull;
-        sItem[wb][k - c0] = (uint16_t)((lane << 8) | bit);
-      }
-      __syncwarp();
-      // evaluate the chunk with every lane
-      for (uint32_t k = c0 + lane; k < c1; k += 32) {
-        const uint32_t it = sItem[wb][k - c0];
-        const int owner = (int)(it >> 8), bit = (int)(it & 0xffu);
-        const bool ext = sExt[wb][owner] != 0;
-        const uint32_t oa_i = sA[wb][owner], ob_i = sB[wb][owner];
-        const SimDev &So = P.sims[sSim[wb][owner]];
-        const int vx = ext ? bit % NV : bit / NE;
-        const int sy = ext ? bit / NV : bit % NE;
-        const uint32_t ip = ext ? ob_i : oa_i, is = ext ? oa_i : ob_i;
-        float f[D], tt = 0.f;
-        const bool ok = mixed_item<D>(vx, sy, P.hl + ip, P.hl + is, P.pos + ip, P.pos + is,
-                                      cap, So, f, tt);
-#pragma unroll
-        for (int c = 0; c < D; ++c) sF[wb][c][k - c0] = f[c];
-        // a pair that does not interact is marked by t = NaN with the flag bit
-        sTt[wb][k - c0] = tt;
-        sItem[wb][k - c0] = (uint16_t)(it | (ok ? 0x8000u : 0u));
-      }
-      __syncwarp();
-      // each lane adds its own items of the chunk in mask order
-      for (uint32_t k = max(first, c0); k < min(first + cnt, c1); ++k) {
-        const uint32_t it = sItem[wb][k - c0];
-        if (!(it & 0x8000u)) {
-          // the item still opens its group (mixed_pass visits the groups in order)
-          const int gi = (int)(it & 0xffu) / g_size;
-          while (g < gi) close_group();
-          continue;
-        }
-        const int gi = (int)(it & 0xffu) / g_size;
-        while (g < gi) close_group();
-        float f[D];
-#pragma unroll
-        for (int c = 0; c < D; ++c) f[c] = sF[wb][c][k - c0];
-        const float tt = sTt[wb][k - c0];
-        const float w0 = is_ext ? -__fsub_rn(1.f, tt) : 1.f;
-#pragma unroll
-        for (int c = 0; c < D; ++c) kahan_add_f(cs[c], cc[c], __fmul_rn(f[c], w0));
-        if (is_ext) {
-#pragma unroll
-          for (int c = 0; c < D; ++c) kahan_add_f(ns[c], nc[c], __fmul_rn(f[c], -tt));
-        }
-      }
-      __syncwarp();
-    }
-    if (have) {
-      while (g < n_grp) close_group();
-      if (is_ext) {
-#pragma unroll
-        for (int k = 0; k < D; ++k)
-          out[(NE * D + k) * stride] = __fmul_rn(__fsub_rn(cs[k], cc[k]), 0.5f);
-      }
-    }
+    mixed_pass<D, NV>((meta & 1u) != 0u, oa, ob, P.hl + a, P.hl + b, P.pos + a, P.pos + b, cap,
+                      S, P.prefilter ? S.filt_thr2 : inf, mb + t, P.pass_cap);
   }
 }
 
