@@ -57,7 +57,9 @@ extern "C" {
  * subdomain or its batch neighbours. */
 
 #define CRG_PREC_F64 0    /* every operation in FP64, in the reference's order */
-#define CRG_PREC_MIXED 1  /* FP32 pair forces with Kahan sums; FP64 state and update */
+#define CRG_PREC_MIXED 1  /* FP32 pair forces with Kahan sums; FP64 state and update
+                           * (spheres, Brownian, Langevin and rods; not with the cell cycle,
+                           * CRG_ENOTSUP) */
 
 #define CRG_WEIGHTS_CHILI 0    /* chili's subdomain-dependent pair weights (default) */
 #define CRG_WEIGHTS_PHYSICAL 1 /* every pair with weight 1 (not reference behaviour) */
@@ -291,8 +293,9 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * with crg_set_option(ctx, CRG_OPT_DEBUG_FORCES, 1) before that step. */
 #define CRG_OPT_DEBUG_FORCES 5
 /* Force kernel: 0 (default) automatic; 1 one thread per agent (the simple reference
- * formulation).  Rods: 0 = pass list (walk, pass kernel, bend, update), 1 thread per rod
- * (also the pass list's overflow fallback).  FP64 spheres: 0 = agent groups up to 38,912
+ * formulation).  FP64 rods: 0 = pass list (walk, pass kernel, bend, update), 1 thread per
+ * rod (also the pass list's overflow fallback); mixed rods always run the pass list.  FP64
+ * spheres: 0 = agent groups up to 38,912
  * agents, lane per agent above; 2 agent groups; 3 lane per agent (warp-packed survivors;
  * CRG_OPT_BLOCK 64 scans 64 candidates per lane and round instead of 32).  Mixed spheres:
  * 3 lane per agent (warp-packed survivors), else one thread per agent.  All variants of one
