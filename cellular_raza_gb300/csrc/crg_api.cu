@@ -993,7 +993,7 @@ int32_t crg_step(crg_ctx *c, int64_t n_steps) {
         c->prof_ms[1] += b;
         c->prof_ms[3] += d;
         c->prof_ms[4] += u;
-        c->prof_ms[2] += force_kernel_count(c) + crg::sort_kernel_count(c->n_vox, c->n_agents);
+        c->prof_ms[2] += force_kernel_count(c) + crg::sort_kernel_count(c->n_vox);
       }
       left -= k;
     } else if (chunk > 0 && left >= chunk) {

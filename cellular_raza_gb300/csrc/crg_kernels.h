@@ -75,7 +75,7 @@ void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st);
 // bsum: n / 4096 + 2 entries.
 void launch_scan(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
                  cudaStream_t st);
-int sort_kernel_count(uint32_t n_vox, uint32_t n_agents);  // kernels one launch_sort issues
+int sort_kernel_count(uint32_t n_vox);  // kernels one launch_sort issues
 void launch_init_keys(const SortArgs &A, int nv, cudaStream_t st);
 void launch_transpose_in(const double *src, double *dst, uint32_t n, int nc, int64_t cap,
                          cudaStream_t st);

@@ -135,9 +135,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(uint32_t *__restric
 // prefix, count[j] = 0, start[n] = total.
 // The voxel sizes of a failed simulation are read from `start` before the first barrier of
 // the scan, and start is written after it.
-__device__ __forceinline__ void scan_single_body(uint32_t *__restrict__ count, uint32_t n,
-                                                 uint32_t *start, const int32_t *status,
-                                                 const SimDev *sims) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_single(uint32_t *__restrict__ count,
+                                                              uint32_t n, uint32_t *start,
+                                                              const int32_t *status,
+                                                              const SimDev *sims) {
   const FailedRange fr(status, sims);
   const uint32_t base = threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
@@ -161,19 +162,14 @@ __device__ __forceinline__ void scan_single_body(uint32_t *__restrict__ count, u
   if (threadIdx.x == 0) start[n] = tot;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_single(uint32_t *__restrict__ count,
-                                                              uint32_t n, uint32_t *start,
-                                                              const int32_t *status,
-                                                              const SimDev *sims) {
-  scan_single_body(count, n, start, status, sims);
-}
-
 // Slot assignment.  Sort key = class << 62 | rank << 31 | index, where the rank is the
 // agent's previous position (with divisions: its position in chili's pre-sort order, the
 // daughters of a voxel following its other agents) and the index locates its state.
 // The agents of a simulation whose step failed keep their voxel and their place (class 0,
 // rank = current position), so their slots are their current positions.
-__device__ __forceinline__ void scatter_one(const SortArgs &A, uint32_t i) {
+__global__ void k_scatter(const SortArgs A) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= A.n_agents) return;
   const int32_t f = A.initial ? -1 : failed_sim(A.status);
   const bool keep = f >= 0 && i - A.sims[f].agent_off < A.sims[f].n_agents;
   uint32_t k = A.nkey[i];
@@ -201,11 +197,6 @@ __device__ __forceinline__ void scatter_one(const SortArgs &A, uint32_t i) {
   }
   const uint32_t rank = (A.srank && !keep) ? A.srank[i] : i;
   A.tmp[slot] = ((uint64_t)cls << 62) | ((uint64_t)rank << 31) | (uint64_t)i;
-}
-
-__global__ void k_scatter(const SortArgs A) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < A.n_agents) scatter_one(A, i);
 }
 
 constexpr int kSegThreads = 256;  // voxels per block of k_segsort
@@ -254,44 +245,6 @@ __device__ void block_bitonic(uint64_t *t, uint32_t m) {
 // memory and is sorted by the whole block afterwards, in shared memory up to kSegSmem
 // entries and in place in global memory beyond, so a voxel with 2^20 agents costs
 // O(m log^2 m) rather than O(m^2).
-// Voxel v: reset its histogram counter and insertion-sort a short segment; returns true
-// for a long one, left to segsort_long.
-__device__ __forceinline__ bool segsort_voxel(const SortArgs &A, uint32_t v) {
-  const uint32_t s0 = A.start[v], s1 = A.start[v + 1];
-  A.count[v] = 0u;
-  if (s0 > s1 || s1 > A.n_agents) {
-    invariant_failed(A.status, kSiteSegRange, v);
-  } else if (s1 - s0 > kSegShort) {
-    return true;
-  } else if (s1 - s0 >= 2) {
-    uint64_t *t = A.tmp;
-    for (uint32_t a = s0 + 1; a < s1; ++a) {
-      uint64_t x = t[a];
-      uint32_t b = a;
-      while (b > s0 && t[b - 1] > x) {
-        t[b] = t[b - 1];
-        --b;
-      }
-      t[b] = x;
-    }
-  }
-  return false;
-}
-
-// A long segment of voxel w, sorted by the whole block (every thread calls it).
-__device__ __forceinline__ void segsort_long(const SortArgs &A, uint32_t w, uint64_t *sBuf) {
-  const uint32_t s0 = A.start[w], m = A.start[w + 1] - s0;  // checked by segsort_voxel
-  if (m <= kSegSmem) {
-    for (uint32_t x = threadIdx.x; x < m; x += blockDim.x) sBuf[x] = A.tmp[s0 + x];
-    __syncthreads();
-    block_bitonic(sBuf, m);
-    for (uint32_t x = threadIdx.x; x < m; x += blockDim.x) A.tmp[s0 + x] = sBuf[x];
-    __syncthreads();
-  } else {
-    block_bitonic(A.tmp + s0, m);
-  }
-}
-
 __global__ void __launch_bounds__(kSegThreads) k_segsort(const SortArgs A) {
   __shared__ uint32_t sLong[kSegThreads];
   __shared__ uint32_t nLong;
@@ -299,15 +252,47 @@ __global__ void __launch_bounds__(kSegThreads) k_segsort(const SortArgs A) {
   if (threadIdx.x == 0) nLong = 0;
   __syncthreads();
   const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v < A.n_vox && segsort_voxel(A, v)) sLong[atomicAdd(&nLong, 1u)] = v;
+  if (v < A.n_vox) {
+    const uint32_t s0 = A.start[v], s1 = A.start[v + 1];
+    A.count[v] = 0u;
+    if (s0 > s1 || s1 > A.n_agents) {
+      invariant_failed(A.status, kSiteSegRange, v);
+    } else if (s1 - s0 > kSegShort) {
+      sLong[atomicAdd(&nLong, 1u)] = v;
+    } else if (s1 - s0 >= 2) {
+      uint64_t *t = A.tmp;
+      for (uint32_t a = s0 + 1; a < s1; ++a) {
+        uint64_t x = t[a];
+        uint32_t b = a;
+        while (b > s0 && t[b - 1] > x) {
+          t[b] = t[b - 1];
+          --b;
+        }
+        t[b] = x;
+      }
+    }
+  }
   __syncthreads();
   const uint32_t n_long = nLong;
-  for (uint32_t q = 0; q < n_long; ++q) segsort_long(A, sLong[q], sBuf);
+  for (uint32_t q = 0; q < n_long; ++q) {
+    const uint32_t w = sLong[q];
+    const uint32_t s0 = A.start[w], m = A.start[w + 1] - s0;  // checked above
+    if (m <= kSegSmem) {
+      for (uint32_t x = threadIdx.x; x < m; x += blockDim.x) sBuf[x] = A.tmp[s0 + x];
+      __syncthreads();
+      block_bitonic(sBuf, m);
+      for (uint32_t x = threadIdx.x; x < m; x += blockDim.x) A.tmp[s0 + x] = sBuf[x];
+      __syncthreads();
+    } else {
+      block_bitonic(A.tmp + s0, m);
+    }
+  }
 }
 
 // One thread per slot: move the updated state into cell-list order and refresh the FP32
 // offsets from the voxel corner.
-__device__ __forceinline__ void gather_one(const SortArgs &A, uint32_t s) {
+__global__ void k_gather(const SortArgs A) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0 && A.step_ctr) {
     *A.step_ctr += 1;
     // the failed simulation as the next step's force kernels see it (sim_frozen)
@@ -365,35 +350,6 @@ __device__ __forceinline__ void gather_one(const SortArgs &A, uint32_t s) {
     A.grate[s] = A.ngrate[src];
     A.parent[s] = A.nparent[src];
   }
-}
-
-__global__ void k_gather(const SortArgs A) {
-  gather_one(A, blockIdx.x * blockDim.x + threadIdx.x);
-}
-
-// The whole sort of a small pack in one block: the phases of scan, scatter, per-voxel
-// order and gather, separated by block barriers instead of kernel boundaries (the launches
-// and their gaps are most of a small pack's sort).  The same operations as the kernels.
-constexpr uint32_t kSmallSortAgents = 16384;  // with at most kScanTile voxels
-constexpr uint32_t kSmallLong = kSmallSortAgents / (kSegShort + 1) + 1;
-
-__global__ void __launch_bounds__(kScanThreads) k_sort_small(const SortArgs A) {
-  __shared__ uint32_t sLong[kSmallLong];
-  __shared__ uint32_t nLong;
-  __shared__ uint64_t sBuf[kSegSmem];
-  scan_single_body(A.count, A.n_vox, A.start, A.initial ? nullptr : A.status, A.sims);
-  if (threadIdx.x == 0) nLong = 0;
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < A.n_agents; i += blockDim.x) scatter_one(A, i);
-  __syncthreads();
-  for (uint32_t v = threadIdx.x; v < A.n_vox; v += blockDim.x)
-    if (segsort_voxel(A, v)) sLong[atomicAdd(&nLong, 1u)] = v;  // <= n_agents / 33 of them
-  __syncthreads();
-  const uint32_t n_long = nLong;
-  for (uint32_t q = 0; q < n_long; ++q) segsort_long(A, sLong[q], sBuf);
-  __syncthreads();
-  // gather_one(A, 0) also advances the step counter (as k_gather, run when there are agents)
-  for (uint32_t s = threadIdx.x; s < A.n_agents; s += blockDim.x) gather_one(A, s);
 }
 
 // Initial voxel keys from the caller's agents (input order), as Domain::decompose does it
@@ -526,25 +482,14 @@ void launch_scan(uint32_t *count, uint32_t n, uint32_t *start, uint32_t *bsum,
   scan_impl(count, n, start, bsum, nullptr, nullptr, st);
 }
 
-bool small_sort(uint32_t n_vox, uint32_t n_agents) {
-  return n_vox <= (uint32_t)kScanTile && n_agents <= kSmallSortAgents;
-}
-
 void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
-  if (small_sort(A.n_vox, A.n_agents)) {
-    k_sort_small<<<1, kScanThreads, 0, st>>>(A);
-    return;
-  }
   scan_impl(A.count, A.n_vox, A.start, bsum, A.initial ? nullptr : A.status, A.sims, st);
   if (A.n_agents) k_scatter<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
   k_segsort<<<grid_for(A.n_vox, kSegThreads), kSegThreads, 0, st>>>(A);
   if (A.n_agents) k_gather<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
 }
 
-int sort_kernel_count(uint32_t n_vox, uint32_t n_agents) {
-  if (small_sort(n_vox, n_agents)) return 1;
-  return n_vox <= (uint32_t)kScanTile ? 4 : 6;
-}
+int sort_kernel_count(uint32_t n_vox) { return n_vox <= (uint32_t)kScanTile ? 4 : 6; }
 
 void launch_repack(const RepackArgs &A, cudaStream_t st) {
   if (A.last > A.first) k_repack<<<grid_for(A.last - A.first, 256), 256, 0, st>>>(A);
