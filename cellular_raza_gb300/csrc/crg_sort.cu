@@ -289,34 +289,30 @@ __global__ void __launch_bounds__(kSegThreads) k_segsort(const SortArgs A) {
   }
 }
 
-// The state moves of one slot: its source index and key, with the invariant checks.
-struct GatherSrc {
-  uint32_t src, k;
-  bool live;  // false: a slot of a failed simulation (keeps its state) or past the end
-};
-__device__ __forceinline__ GatherSrc gather_src(const SortArgs &A, uint32_t s, int32_t f) {
-  GatherSrc g = {0u, 0u, false};
-  if (s >= A.n_agents) return g;
+// One thread per slot: move the updated state into cell-list order and refresh the FP32
+// offsets from the voxel corner.
+__global__ void k_gather(const SortArgs A) {
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0 && A.step_ctr) {
+    *A.step_ctr += 1;
+    // the failed simulation as the next step's force kernels see it (sim_frozen)
+    const int32_t code = A.status[0];
+    A.status[6] = code == 0 ? 0 : code == CRG_EINTERNAL ? -1 : A.status[4] + 1;
+  }
+  if (s >= A.n_agents) return;
   // a simulation whose step failed keeps its current state (its slots are its positions)
-  if (f >= 0 && s - A.sims[f].agent_off < A.sims[f].n_agents) return g;
-  g.live = true;
-  g.src = (uint32_t)(A.tmp[s] & 0x7fffffffull);
-  if (g.src >= A.n_agents) {
+  const int32_t f = A.initial ? -1 : failed_sim(A.status);
+  if (f >= 0 && s - A.sims[f].agent_off < A.sims[f].n_agents) return;
+  uint32_t src = (uint32_t)(A.tmp[s] & 0x7fffffffull);
+  if (src >= A.n_agents) {
     invariant_failed(A.status, kSiteGatherSrc, s);
-    g.src = s;
+    src = s;
   }
-  g.k = A.nkey[g.src];
-  if (g.k >= A.n_vox) {
+  uint32_t k = A.nkey[src];
+  if (k >= A.n_vox) {
     invariant_failed(A.status, kSiteGatherKey, s);
-    g.k = 0;
+    k = 0;
   }
-  return g;
-}
-
-// Slot s's state from its source: key, id, positions, velocities, the FP32 offsets from
-// the voxel centre, solver history and cycle state.
-__device__ __forceinline__ void gather_move(const SortArgs &A, uint32_t s, const GatherSrc &g) {
-  const uint32_t src = g.src, k = g.k;
   A.key[s] = k;
   A.id[s] = A.nid[src];
   const int64_t cap = A.cap;
@@ -332,15 +328,10 @@ __device__ __forceinline__ void gather_move(const SortArgs &A, uint32_t s, const
   }
   const int nc = A.nc;
   const int dim = S.dim;
-  const double *__restrict__ npos = A.npos;
-  const double *__restrict__ nvel = A.nvel;
-  double *__restrict__ pos = A.pos;
-  double *__restrict__ vel = A.vel;
-  float *__restrict__ off = A.off;
   for (int c = 0; c < nc; ++c) {
-    const double p = npos[c * cap + src];
-    pos[c * cap + s] = p;
-    vel[c * cap + s] = nvel[c * cap + src];
+    const double p = A.npos[c * cap + src];
+    A.pos[c * cap + s] = p;
+    A.vel[c * cap + s] = A.nvel[c * cap + src];
     const int axis = c % dim;
     const double centre = A.vcen[S.cen_off[axis] + idx[axis]];  // voxel_centre, tabled
     float o = (float)(p - centre);
@@ -348,7 +339,7 @@ __device__ __forceinline__ void gather_move(const SortArgs &A, uint32_t s, const
     // fell outside the grid) would weaken the prefilter's error bound: mark them NaN so
     // every comparison involving them falls through to the exact FP64 path.
     if (!(fabsf(o) <= S.off_lim)) o = __int_as_float(0x7fc00000);
-    off[c * cap + s] = o;
+    A.off[c * cap + s] = o;
   }
   if (A.hist) {
     for (int c = 0; c < 2 * nc; ++c) A.hist[c * cap + s] = A.nhist[c * cap + src];
@@ -359,26 +350,6 @@ __device__ __forceinline__ void gather_move(const SortArgs &A, uint32_t s, const
     A.grate[s] = A.ngrate[src];
     A.parent[s] = A.nparent[src];
   }
-}
-
-// Two slots per thread, s and s + half (each half coalesced): both source indices and keys
-// are read before either slot's state moves, so twice the loads are in flight while the
-// permuted reads wait on memory.
-__global__ void k_gather(const SortArgs A) {
-  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t == 0 && A.step_ctr) {
-    *A.step_ctr += 1;
-    // the failed simulation as the next step's force kernels see it (sim_frozen)
-    const int32_t code = A.status[0];
-    A.status[6] = code == 0 ? 0 : code == CRG_EINTERNAL ? -1 : A.status[4] + 1;
-  }
-  const uint32_t half = (A.n_agents + 1) / 2;
-  if (t >= half) return;
-  const int32_t f = A.initial ? -1 : failed_sim(A.status);
-  const GatherSrc g0 = gather_src(A, t, f);
-  const GatherSrc g1 = gather_src(A, t + half, f);
-  if (g0.live) gather_move(A, t, g0);
-  if (g1.live) gather_move(A, t + half, g1);
 }
 
 // Initial voxel keys from the caller's agents (input order), as Domain::decompose does it
@@ -515,7 +486,7 @@ void launch_sort(const SortArgs &A, uint32_t *bsum, cudaStream_t st) {
   scan_impl(A.count, A.n_vox, A.start, bsum, A.initial ? nullptr : A.status, A.sims, st);
   if (A.n_agents) k_scatter<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
   k_segsort<<<grid_for(A.n_vox, kSegThreads), kSegThreads, 0, st>>>(A);
-  if (A.n_agents) k_gather<<<grid_for((A.n_agents + 1) / 2, 256), 256, 0, st>>>(A);
+  if (A.n_agents) k_gather<<<grid_for(A.n_agents, 256), 256, 0, st>>>(A);
 }
 
 int sort_kernel_count(uint32_t n_vox) { return n_vox <= (uint32_t)kScanTile ? 4 : 6; }
