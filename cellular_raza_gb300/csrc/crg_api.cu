@@ -366,6 +366,10 @@ void free_all(crg_ctx *c) {
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
+// Floats per agent of the interleaved sphere offsets (one 16- or 8-byte load per agent);
+// 0 for the component-major rod offsets.
+int off_aos(const crg_ctx *c) { return c->kind == CRG_KIND_ROD ? 0 : (c->dim == 3 ? 4 : 2); }
+
 int32_t allocate(crg_ctx *c) {
   const int64_t cap = c->cap;
   const int nc = c->nc;
@@ -382,7 +386,7 @@ int32_t allocate(crg_ctx *c) {
   A(nid, cap);
   A(key, cap);
   A(nkey, cap);
-  A(off, cap * nc);
+  A(off, cap * (off_aos(c) ? off_aos(c) : nc));
   A(tmp, cap);
   A(count, (size_t)c->n_vox + 1);
   A(start, (size_t)c->n_vox + 1);
@@ -595,6 +599,7 @@ SortArgs sort_args(crg_ctx *c, int initial) {
   A.id = c->id;
   A.key = c->key;
   A.off = c->off;
+  A.off_aos = off_aos(c);
   A.hist = c->hist;
   A.hmeta = c->hmeta;
   A.npos = c->npos;
@@ -1102,7 +1107,8 @@ int32_t crg_snapshot(crg_ctx *c, int32_t op) {
   std::vector<Part> parts = {
       {c->pos, sizeof(double) * cap * nc}, {c->vel, sizeof(double) * cap * nc},
       {c->id, sizeof(uint64_t) * cap},     {c->key, sizeof(uint32_t) * cap},
-      {c->off, sizeof(float) * cap * nc},  {c->start, sizeof(uint32_t) * ((size_t)c->n_vox + 1)},
+      {c->off, sizeof(float) * cap * (off_aos(c) ? off_aos(c) : nc)},
+      {c->start, sizeof(uint32_t) * ((size_t)c->n_vox + 1)},
       {c->step_ctr, sizeof(int64_t)}};
   if (c->order > 1) {
     parts.push_back({c->hist, sizeof(double) * cap * nc * 2});
@@ -1188,8 +1194,11 @@ std::vector<CkptSlice> ckpt_slices(crg_ctx *c) {
   std::vector<CkptSlice> v = {{(char *)c->pos, sizeof(double), nc},
                               {(char *)c->vel, sizeof(double), nc},
                               {(char *)c->id, sizeof(uint64_t), 1},
-                              {(char *)c->key, sizeof(uint32_t), 1},
-                              {(char *)c->off, sizeof(float), nc}};
+                              {(char *)c->key, sizeof(uint32_t), 1}};
+  if (off_aos(c))  // interleaved sphere offsets: one record of off_aos floats per agent
+    v.push_back({(char *)c->off, sizeof(float) * (size_t)off_aos(c), 1});
+  else
+    v.push_back({(char *)c->off, sizeof(float), nc});
   if (c->order > 1) {
     v.push_back({(char *)c->hist, sizeof(double), 2 * nc});
     v.push_back({(char *)c->hmeta, 1, 1});

@@ -85,7 +85,9 @@ struct PackArgs {
   const double *vel;
   const uint64_t *id;
   const uint32_t *key;
-  const float *off;  // FP32 offsets from the voxel corner (prefilter / mixed precision)
+  const float *off;  // FP32 offsets from the voxel centre (prefilter / mixed precision):
+                     // spheres one float4 (3D) or float2 (2D) per agent (sphere_off), rods
+                     // component-major [nc][cap]
   const double *hist;     // AB history [2 slots][2 (dx,dv)][nc][cap] or null
   const uint8_t *hmeta;   // ring buffer (first | size << 4) or null
   const uint32_t *start;  // [n_vox + 1]

@@ -24,6 +24,8 @@ struct SortArgs {
   uint64_t *id;
   uint32_t *key;
   float *off;
+  int32_t off_aos;     // spheres: floats per agent of the interleaved offsets (4 in 3D, 2 in
+                       // 2D); 0: component-major [nc][cap] (rods)
   const double *vcen;  // voxel centres per simulation and axis (SimDev::cen_off)
   double *hist;
   uint8_t *hmeta;

@@ -328,6 +328,7 @@ __global__ void k_gather(const SortArgs A) {
   }
   const int nc = A.nc;
   const int dim = S.dim;
+  float ov[3] = {0.f, 0.f, 0.f};  // spheres: written together, interleaved
   for (int c = 0; c < nc; ++c) {
     const double p = A.npos[c * cap + src];
     A.pos[c * cap + s] = p;
@@ -339,8 +340,18 @@ __global__ void k_gather(const SortArgs A) {
     // fell outside the grid) would weaken the prefilter's error bound: mark them NaN so
     // every comparison involving them falls through to the exact FP64 path.
     if (!(fabsf(o) <= S.off_lim)) o = __int_as_float(0x7fc00000);
-    A.off[c * cap + s] = o;
+    if (A.off_aos) {
+      if (c == 0) ov[0] = o;
+      else if (c == 1) ov[1] = o;
+      else ov[2] = o;
+    } else {
+      A.off[c * cap + s] = o;
+    }
   }
+  if (A.off_aos == 4)
+    reinterpret_cast<float4 *>(A.off)[s] = make_float4(ov[0], ov[1], ov[2], 0.f);
+  else if (A.off_aos == 2)
+    reinterpret_cast<float2 *>(A.off)[s] = make_float2(ov[0], ov[1]);
   if (A.hist) {
     for (int c = 0; c < 2 * nc; ++c) A.hist[c * cap + s] = A.nhist[c * cap + src];
     A.hmeta[s] = A.nhmeta[src];

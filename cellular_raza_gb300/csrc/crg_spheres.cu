@@ -26,6 +26,22 @@ namespace crg {
 
 namespace {
 
+// The FP32 offsets of sphere agent i: one float4 (3D) or float2 (2D) per agent.
+template <int D>
+__device__ __forceinline__ void sphere_off(const float *off, uint32_t i, float *o) {
+  if (D == 3) {
+    const float4 v = reinterpret_cast<const float4 *>(off)[i];
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+  } else {
+    const float2 v = reinterpret_cast<const float2 *>(off)[i];
+    o[0] = v.x;
+    o[1] = v.y;
+  }
+}
+
+
 template <int D>
 struct Neigh {
   int lo[D], hi[D];
@@ -334,8 +350,8 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
   for (int c = 0; c < D; ++c) {
     pa[c] = P.pos[c * cap + i];
     va[c] = P.vel[c * cap + i];
-    oa[c] = P.off[c * cap + i];
   }
+  sphere_off<D>(P.off, i, oa);
   const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   double acc[D];
@@ -361,11 +377,12 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
   auto flush = [&]() {
     for (int q = 0; q < ns; ++q) {
       const uint32_t b = sB[q * bd + tid], m = sM[q * bd + tid];
-      float kd[D], zf[D], d2 = 0.0f;
+      float kd[D], zf[D], ob[D], d2 = 0.0f;
+      sphere_off<D>(P.off, b, ob);
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         kd[c] = (float)((int)((m >> (2 * c)) & 3u) - 1) * S.dxf[c];
-        zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
+        zf[c] = (oa[c] - ob[c]) - kd[c];
         d2 = fmaf(zf[c], zf[c], d2);
       }
       float h[D];
@@ -428,11 +445,12 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
         const int q = (int)(b >= sb[1]) + (int)(b >= sb[2]);
         kd[L] = (q == 0) ? kdl[0] : (q == 1) ? kdl[1] : kdl[2];
         const bool twice = (tw_bits >> q) & 1u;
-        float zf[D];
+        float zf[D], ob[D];
         float d2 = 0.0f;
+        sphere_off<D>(P.off, b, ob);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-          zf[c] = (oa[c] - P.off[c * cap + b]) - kd[c];
+          zf[c] = (oa[c] - ob[c]) - kd[c];
           d2 = fmaf(zf[c], zf[c], d2);
         }
         // the agent itself and pairs beyond the prefilter threshold are skipped (one branch;
@@ -536,8 +554,8 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
 #pragma unroll
   for (int c = 0; c < D; ++c) {
     pa[c] = P.pos[c * cap + ii];
-    oa[c] = P.off[c * cap + ii];
   }
+  sphere_off<D>(P.off, ii, oa);
   const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
@@ -599,10 +617,11 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
         }
         b = sB0[w][g][q] + (j - sPre[w][g][q]);
         if (b != i) {
-          float d2 = 0.0f;
+          float d2 = 0.0f, ob[D];
+          sphere_off<D>(P.off, b, ob);
 #pragma unroll
           for (int c = 0; c < D; ++c) {
-            const float z = (oa[c] - P.off[c * cap + b]) - sKd[w][g][q][c];
+            const float z = (oa[c] - ob[c]) - sKd[w][g][q][c];
             d2 = fmaf(z, z, d2);
           }
           surv = !(d2 > thr2);  // NaN falls through to the exact path
@@ -742,8 +761,8 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
   for (int c = 0; c < D; ++c) {
     pa[c] = P.pos[c * cap + ii];
     va[c] = P.vel[c * cap + ii];
-    oa[c] = P.off[c * cap + ii];
   }
+  sphere_off<D>(P.off, ii, oa);
   const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
   int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
@@ -810,10 +829,11 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
       const uint32_t b = b_next++;
       ++g;
       if (b == i) continue;
-      float d2 = 0.0f;
+      float d2 = 0.0f, ob[D];
+      sphere_off<D>(P.off, b, ob);
 #pragma unroll
       for (int c = 0; c < D; ++c) {
-        const float z = (oa[c] - P.off[c * cap + b]) - kd[c];
+        const float z = (oa[c] - ob[c]) - kd[c];
         d2 = fmaf(z, z, d2);
       }
       if (d2 > thr2) continue;  // NaN falls through to the exact path
@@ -866,10 +886,13 @@ __global__ void __launch_bounds__(32) k_spheres_pass(const PackArgs P) {
             const uint32_t code = sK[k][l];
             float zf[D], hf[D];
             float d2 = 0.0f;
+            float oa_l[D], ob_l[D];
+            sphere_off<D>(P.off, a, oa_l);
+            sphere_off<D>(P.off, b, ob_l);
 #pragma unroll
             for (int c = 0; c < D; ++c) {
               const float kdc = (float)((int)((code >> (2 * c)) & 3u) - 1) * So.dxf[c];
-              zf[c] = (P.off[c * cap + a] - P.off[c * cap + b]) - kdc;
+              zf[c] = (oa_l[c] - ob_l[c]) - kdc;
               d2 = fmaf(zf[c], zf[c], d2);
             }
             double pa_l[D];
