@@ -262,7 +262,6 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   double margin = 128.0 * err + 1e-4 * std::fabs(m.cutoff) + 1e-6;
   double thr = std::fabs(m.cutoff) + margin;
   S.off_lim = (float)off_lim;
-  S.band_f = (float)margin;
   if (m.kind == CRG_KIND_ROD) {
     // mixed rods take their distances from hi / lo coordinates (relative error ~1e-6,
     // absolute ~2^-47 of the largest coordinate): 1e-5 of the cutoff, and 64 x 2^-47 of the

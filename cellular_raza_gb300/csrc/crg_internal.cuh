@@ -54,7 +54,6 @@ struct SimDev {
   float radius_f, stiffness_f, cutoff_f, strength_f;
   float filt_thr2;  // squared FP32 prefilter threshold (cutoff + conservative margin)^2
   float off_lim;    // |FP32 offset| bound the prefilter margin was derived for
-  float band_f;     // the prefilter margin
   // mixed precision: FP32 distances closer than mix_band_f to the cutoff, or than
   // mix_zero_f to 0, are decided from the FP64 distance (each a few times the FP32
   // distance's error bound, far below the prefilter margin)

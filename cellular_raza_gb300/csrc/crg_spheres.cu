@@ -441,7 +441,6 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     // the row's candidates box after box (in a cell list that failed its checks, a box left
     // empty may hand its range to the next one: the step reports CRG_EINTERNAL and rolls back)
     {
-#pragma unroll 2
       for (uint32_t b = sb[0]; b < sb[nb]; ++b) {
         const int q = (int)(b >= sb[1]) + (int)(b >= sb[2]);
         kd[L] = (q == 0) ? kdl[0] : (q == 1) ? kdl[1] : kdl[2];
