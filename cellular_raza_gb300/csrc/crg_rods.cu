@@ -224,6 +224,50 @@ __device__ __forceinline__ void bend_force(const SimDev &S, const double *c1, co
   }
 }
 
+// Mixed precision: the same curvature force with tan(angle / 2) from the half-angle
+// identity tan(theta / 2) = |c1 x c2| / (|c1| |c2| + c1 . c2), still in FP64 but without
+// acos and tan (about 40 % of the FP64 work of bend_force).  It agrees with the reference's
+// acos / tan to a few FP64 ulps away from folded rods; a rod folded back exactly (zero
+// denominator) takes tan(pi / 2) as the reference's FP64 evaluates it.
+template <int D>
+__device__ __forceinline__ void bend_force_halfangle(const SimDev &S, const double *c1,
+                                                     const double *c2, double *f) {
+  double prod = dmul(c1[0], c2[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) prod = dadd(prod, dmul(c1[c], c2[c]));
+  const double n1 = norm_f64<D>(c1), n2 = norm_f64<D>(c2);
+  double cr;
+  if (D == 2) {
+    cr = fabs(dsub(dmul(c1[0], c2[1]), dmul(c1[1], c2[0])));
+  } else {
+    const double x = dsub(dmul(c1[1], c2[2]), dmul(c1[2], c2[1]));
+    const double y = dsub(dmul(c1[2], c2[0]), dmul(c1[0], c2[2]));
+    const double z = dsub(dmul(c1[0], c2[1]), dmul(c1[1], c2[0]));
+    cr = __dsqrt_rn(dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)));
+  }
+  auto is_zero = [](double v) { return (__double_as_longlong(v) & 0x7fffffffffffffffll) == 0; };
+  double tn = 0.0;  // zero-length segments: angle 0
+  if (!(is_zero(n1) || is_zero(n2))) {
+    const double den = dadd(dmul(n1, n2), prod);
+    if (den != den)
+      tn = den;  // NaN coordinates stay NaN
+    else if (f64_gt_key(den, 0))
+      tn = ddiv(cr, den);
+    else
+      tn = 1.633123935319537e16;  // tan(0.5 * acos(-1.0)) in FP64
+  }
+  double fd[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) fd[c] = dsub(c1[c], c2[c]);
+  const double fdn = norm_f64<D>(fd);
+  const bool fd_zero = is_zero(fdn);
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const double fdir = !fd_zero ? ddiv(fd[c], fdn) : fd[c];
+    f[c] = dmul(dmul(dmul(fdir, 2.0), S.rigidity), tn);
+  }
+}
+
 // CartesianSubDomainRods::apply_boundary (bacterial_rods.rs:489-534) on a rod's updated
 // vertices, then its next voxel key from the centroid row_sum / nrows (:550-554); writes
 // the next state at `slot` and counts the key.  `key`: the voxel the rod stays in when the
@@ -1382,7 +1426,7 @@ __global__ void __launch_bounds__(128) k_rods_passmix(const PackArgs P) {
 
 // Curvature forces of every angle of every live rod, one thread per (angle, rod), into
 // P.bend [NV - 2][D][cap] for k_rods_update (the acos / tan work, spread over more threads
-// than the per-rod update can keep resident).
+// than the per-rod update can keep resident; mixed precision: the half-angle identity).
 template <int D, int NV>
 __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
   const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1404,7 +1448,10 @@ __global__ void __launch_bounds__(128) k_rods_bend(const PackArgs P) {
     c1[c] = dsub(x[0][c], x[1][c]);
     c2[c] = dsub(x[1][c], x[2][c]);
   }
-  bend_force<D>(S, c1, c2, f);
+  if (P.hl)  // mixed precision
+    bend_force_halfangle<D>(S, c1, c2, f);
+  else
+    bend_force<D>(S, c1, c2, f);
 #pragma unroll
   for (int c = 0; c < D; ++c) P.bend[(s * D + c) * cap + i] = f[c];
 }
