@@ -59,6 +59,8 @@ def parse():
                         "graphs), print the wall time and exit")
     p.add_argument("--case-steps", type=int, default=10)
     p.add_argument("--case-n", type=int, default=0, help="agents (0: the workload's size)")
+    p.add_argument("--case-side", type=float, default=0.0,
+                   help="box side (rod_colony; 0: the workload's default)")
     p.add_argument("--case-subdomains", type=int, default=16)
     p.add_argument("--case-precision", default=None, choices=[None, "f64", "mixed"])
     p.add_argument("--case-variant", type=int, default=0, help="CRG_OPT_KERNEL_VARIANT")
@@ -876,6 +878,8 @@ def profile_case(args):
         kw["n"] = args.case_n
     if args.case_precision:
         kw["precision"] = args.case_precision
+    if args.case_side:
+        kw["side"] = args.case_side
     w = getattr(W, args.case_workload or args.workload)(seed=2024, **kw)
     cycle = getattr(w.model, "cycle", False)
     with E.Simulation.single(w.model, 16 * w.n if cycle else w.n) as sim:
