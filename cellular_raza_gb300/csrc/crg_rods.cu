@@ -469,8 +469,9 @@ __device__ __forceinline__ void rod_update(const PackArgs &P, const SimDev &S, u
 
 // ---------------------------------------------------------------------------------------
 // Mixed precision (CRG_PREC_MIXED).  The pair arithmetic of RodInteraction -- nearest point
-// on the segment and the Morse force -- runs in FP32; springs, curvature, damping, the
-// solver, the boundary and the state stay FP64 (k_rods_bend, k_rods_update).  FP32 loses
+// on the segment and the Morse force -- runs in FP32; springs, curvature (through the
+// half-angle identity, bend_force_halfangle), damping, the solver, the boundary and the
+// state stay FP64 (k_rods_bend, k_rods_update).  FP32 loses
 // nothing in the coordinate differences: every coordinate x is carried as hi = (float)x
 // and lo = (float)(x - hi), and differences are formed as hi + lo pairs (diff_hl), exact
 // to ~2^-48 |x| however far from the origin the rods are.  Whether a
