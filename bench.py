@@ -71,6 +71,10 @@ def parse():
                    help="run the request stream at --sweep-rates and print one JSON line")
     p.add_argument("--sweep-rates", default="15,25,40,80")
     p.add_argument("--sweep-requests", type=int, default=1000)
+    # every force-kernel shape the autotuner tries, timed on the ensemble and at 2^23
+    p.add_argument("--tile-sweep", action="store_true",
+                   help="time every mixed sphere force-kernel shape (block x tile) on the "
+                        "1,024-simulation ensemble and on 2^23 spheres; one JSON line")
     return p.parse_args()
 
 
@@ -666,6 +670,44 @@ def served_sweep(args):
                       "steps_per_tick": 32}), flush=True)
 
 
+TILE_SHAPES = [(1, 64, 0), (1, 128, 0), (1, 256, 0), (1, 64, 2), (1, 128, 1), (1, 128, 2),
+               (1, 128, 4), (1, 256, 1), (1, 256, 2), (3, 0, 0)]
+
+
+def tile_sweep(args):
+    """Wall time per step of each (variant, block, tile) shape of the mixed sphere force
+    kernel: one-shot thread-per-agent grids, the persistent tile kernel and the warp-packed
+    kernel (32 graph-captured steps after 32 warm-up steps per shape; the state runs on
+    from shape to shape), then what crg_autotune picks."""
+    import numpy as np
+
+    from cellular_raza_gb300 import _native as N
+    from cellular_raza_gb300 import engine as E
+    from cellular_raza_gb300 import workloads as W
+
+    def shapes_on(ws, shapes, steps):
+        sim = E.Simulation([w.model for w in ws], [w.n for w in ws])
+        sim.upload(np.concatenate([w.pos for w in ws]), np.concatenate([w.vel for w in ws]),
+                   counts=[w.n for w in ws])
+        out = {}
+        for v, b, t in shapes:
+            sim.set_option(N.OPT_KERNEL_VARIANT, v)
+            sim.set_option(N.OPT_BLOCK, b)
+            sim.set_option(N.OPT_TILE, t)
+            sim.step(steps)
+            t0 = time.perf_counter()
+            sim.step(steps)
+            out[f"variant {v} block {b} tile {t}"] = 1e3 * (time.perf_counter() - t0) / steps
+        tune = sim.autotune(5)
+        sim.close()
+        return {"ms_per_step": out, "autotune": tune}
+
+    ens = W.ensemble(seed=0, precision="mixed", n_steps=500)
+    res = {"ensemble_1024_mixed": shapes_on(ens, TILE_SHAPES, 32),
+           "spheres_2^23_mixed": shapes_on([W.spheres_3d_large()], TILE_SHAPES, 32)}
+    print(json.dumps({"workload": "tile_sweep", **res}), flush=True)
+
+
 def crg_arm(args):
     rank, world, local = dist_env()
     if world > 1:
@@ -901,6 +943,8 @@ def main():
         profile_case(args)
     elif args.served_sweep:
         served_sweep(args)
+    elif args.tile_sweep:
+        tile_sweep(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

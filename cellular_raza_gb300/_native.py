@@ -20,6 +20,7 @@ WEIGHTS_CHILI, WEIGHTS_PHYSICAL = 0, 1
 OPT_PREFILTER, OPT_GRAPH_CHUNK, OPT_BLOCK, OPT_PROFILE, OPT_DEBUG_FORCES = 1, 2, 3, 4, 5
 OPT_KERNEL_VARIANT = 6
 OPT_PASS_LIST = 7
+OPT_TILE = 8
 # CellIdentifier::Division(voxel, counter) = ID_DIVISION | voxel << 32 | counter
 ID_DIVISION = 1 << 63
 NO_PARENT = (1 << 64) - 1
@@ -28,6 +29,7 @@ NO_PARENT = (1 << 64) - 1
 EXPORTED = [
     "crg_create", "crg_create_batch", "crg_upload", "crg_step", "crg_forces", "crg_download",
     "crg_agent_count", "crg_last_error", "crg_destroy", "crg_strerror", "crg_set_option",
+    "crg_get_option",
     "crg_debug_forces", "crg_debug_neighbor_stats", "crg_profile", "crg_measure_fma_peaks",
     "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc", "crg_autotune",
     "crg_set_sim_stop", "crg_sim_download", "crg_clear_error", "crg_repack", "crg_step_count",
@@ -127,6 +129,7 @@ def load(build_if_missing: bool = True):
     L.crg_strerror.argtypes = [C.c_int32]
     L.crg_strerror.restype = C.c_char_p
     L.crg_set_option.argtypes = [vp, C.c_int32, C.c_int64]
+    L.crg_get_option.argtypes = [vp, C.c_int32, i64p]
     L.crg_debug_forces.argtypes = [vp, dp, u64p]
     L.crg_debug_neighbor_stats.argtypes = [vp, u32p, u32p, u64p, u64p]
     L.crg_profile.argtypes = [vp, dp]

@@ -78,6 +78,7 @@ struct crg_ctx {
   int graph_chunk = 32;
   int prefilter = 1;
   int variant = 0;
+  int tile = 0;  // CRG_OPT_TILE
   int block = 0;
   int profile = 0;
   double prof_ms[5] = {0, 0, 0, 0, 0};
@@ -262,6 +263,15 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
   double margin = 128.0 * err + 1e-4 * std::fabs(m.cutoff) + 1e-6;
   double thr = std::fabs(m.cutoff) + margin;
   S.off_lim = (float)off_lim;
+  {
+    // sensing (cell cycle): FP32 offset distances are within err per axis of the FP64
+    // ones, so pairs farther than 4 err * sqrt(dim) from the range are decided in FP32
+    const double r = m.sense_range, band = 4.0 * err;
+    const double lo = (r > band) ? r - band : 0.0, hi = r + band;
+    S.sense_in2 = (r > band) ? (float)(lo * lo) * (1.0f - 1e-6f) : -1.0f;
+    S.sense_out2 = std::isfinite(hi) ? (float)(hi * hi) * (1.0f + 1e-6f) : __builtin_inff();
+    if (!(r > 0.0)) S.sense_in2 = -1.0f;
+  }
   if (m.kind == CRG_KIND_ROD) {
     // mixed rods take their distances from hi / lo coordinates (relative error ~1e-6,
     // absolute ~2^-47 of the largest coordinate): 1e-5 of the cutoff, and 64 x 2^-47 of the
@@ -393,10 +403,8 @@ int32_t allocate(crg_ctx *c) {
   A(status, 8);
   A(step_ctr, 1);
   A(staging, cap * nc);
-  if (c->kind == CRG_KIND_SPHERE && c->precision != CRG_PREC_F64) {
-    A(rctl, 4);
-    A(fix_list, cap);
-  }
+  if (c->kind != CRG_KIND_ROD) A(rctl, 4);  // [0] mixed fix-up count, [2] tile counter
+  if (c->kind == CRG_KIND_SPHERE && c->precision != CRG_PREC_F64) A(fix_list, cap);
   if (c->kind == CRG_KIND_ROD) {
     A(frc, cap * nc);
     A(bend, cap * (c->nv > 2 ? c->nv - 2 : 1) * c->dim);
@@ -514,6 +522,8 @@ int32_t create_impl(int32_t n_sims, const crg_domain *domains, const crg_model *
     r = CRG_ECUDA;
   if (r == CRG_OK && c->kind == CRG_KIND_ROD && crg::prepare_rods(c->dim, c->nv) != 0)
     r = CRG_ECUDA;
+  if (r == CRG_OK && c->kind != CRG_KIND_ROD && crg::prepare_spheres(c->dim, c->precision) != 0)
+    r = CRG_ECUDA;
   if (r != CRG_OK) {
     free_all(c);
     delete c;
@@ -564,6 +574,7 @@ PackArgs pack_args(crg_ctx *c) {
   P.pass_cap = c->pass_cap;
   P.prefilter = c->prefilter;
   P.variant = c->variant;
+  P.tile = c->tile;
   if (c->cycle) {
     P.slen = c->slen;
     P.grate = c->grate;
@@ -1337,30 +1348,36 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   if (c->cycle) return CRG_ENOTSUP;  // trials restore snapshots, which hold no cycle state
   if (c->err_code != CRG_OK) return c->err_code;
   struct Shape {
-    int variant, block;
+    int variant, block, tile;
   };
   std::vector<Shape> shapes;
   if (c->kind == CRG_KIND_ROD && c->precision != CRG_PREC_F64) {
-    shapes = {{0, 0}};  // mixed-precision rods have one path
+    shapes = {{0, 0, 0}};  // mixed-precision rods have one path
   } else if (c->kind == CRG_KIND_ROD) {
-    shapes = {{0, 0}, {1, 64}};
+    shapes = {{0, 0, 0}, {1, 64, 0}};
   } else if (c->precision == CRG_PREC_F64) {
-    shapes = {{0, 0}, {2, 0}, {3, 0}, {3, 64}, {1, 64}, {1, 128}, {1, 256}};
+    shapes = {{0, 0, 0}, {2, 0, 0},   {3, 0, 0},   {3, 64, 0},  {1, 64, 0},
+              {1, 128, 0}, {1, 256, 0}, {1, 128, 1}, {1, 128, 4}, {1, 256, 2}};
   } else {
-    shapes = {{1, 64}, {1, 128}, {1, 256}, {3, 0}};
+    // thread per agent: one-shot grids, and the persistent tile kernel with tiles of
+    // block x 1, 2, 4 agents; the warp-packed kernel
+    shapes = {{1, 64, 0},  {1, 128, 0}, {1, 256, 0}, {1, 64, 2},  {1, 128, 1},
+              {1, 128, 2}, {1, 128, 4}, {1, 256, 1}, {1, 256, 2}, {3, 0, 0}};
   }
   int32_t r = crg_snapshot(c, CRG_SNAPSHOT_SAVE);
   if (r != CRG_OK) return r;
   const int saved_variant = c->variant, saved_block = c->block, saved_profile = c->profile;
+  const int saved_tile = c->tile;
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0));
   CUDA_TRY(cudaEventCreate(&e1));
   double best_ms = 1e300;
-  Shape best = {saved_variant, saved_block};
+  Shape best = {saved_variant, saved_block, saved_tile};
   c->profile = 0;
   for (const Shape &s : shapes) {
     c->variant = s.variant;
     c->block = s.block;
+    c->tile = s.tile;
     if ((r = crg_snapshot(c, CRG_SNAPSHOT_RESTORE)) != CRG_OK) break;
     launch_one_step(c);  // warm-up (first launch of this shape)
     if ((r = crg_snapshot(c, CRG_SNAPSHOT_RESTORE)) != CRG_OK) break;
@@ -1379,6 +1396,7 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   cudaEventDestroy(e1);
   c->variant = best.variant;
   c->block = best.block;
+  c->tile = best.tile;
   c->profile = saved_profile;
   invalidate_graph(c);
   int32_t r2 = crg_snapshot(c, CRG_SNAPSHOT_RESTORE);
@@ -1492,6 +1510,7 @@ int32_t crg_repack(crg_ctx *src, int32_t n_keep, const int32_t *keep, int32_t n_
   if (r != CRG_OK) return r;
   if (src) {
     c->variant = src->variant;
+    c->tile = src->tile;
     c->block = src->block;
     c->prefilter = src->prefilter;
     c->graph_chunk = src->graph_chunk;
@@ -1652,6 +1671,22 @@ int32_t crg_last_error(crg_ctx *c, int64_t *agent, int64_t *step) {
   return c->err_code;
 }
 
+int32_t crg_get_option(crg_ctx *c, int32_t option, int64_t *value) {
+  if (!c || !value) return CRG_EINVAL;
+  switch (option) {
+    case CRG_OPT_PREFILTER: *value = c->prefilter; break;
+    case CRG_OPT_GRAPH_CHUNK: *value = c->graph_chunk; break;
+    case CRG_OPT_BLOCK: *value = c->block; break;
+    case CRG_OPT_PROFILE: *value = c->profile; break;
+    case CRG_OPT_DEBUG_FORCES: *value = c->dbg_force ? 1 : 0; break;
+    case CRG_OPT_KERNEL_VARIANT: *value = c->variant; break;
+    case CRG_OPT_PASS_LIST: *value = c->pass_cap; break;
+    case CRG_OPT_TILE: *value = c->tile; break;
+    default: return CRG_EINVAL;
+  }
+  return CRG_OK;
+}
+
 int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
   if (!c) return CRG_EINVAL;
   switch (option) {
@@ -1675,6 +1710,10 @@ int32_t crg_set_option(crg_ctx *c, int32_t option, int64_t value) {
     case CRG_OPT_KERNEL_VARIANT:
       if (value < 0 || value > 3) return CRG_EINVAL;
       c->variant = (int)value;
+      break;
+    case CRG_OPT_TILE:
+      if (value < 0 || value > 16) return CRG_EINVAL;
+      c->tile = (int)value;
       break;
     case CRG_OPT_PASS_LIST: {
       if (c->kind != CRG_KIND_ROD || value < 0) return CRG_EINVAL;

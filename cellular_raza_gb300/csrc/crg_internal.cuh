@@ -69,6 +69,9 @@ struct SimDev {
   // bits of the largest squared distance x with RN(sqrt(x)) < cyc_sense (RN o sqrt is
   // monotone, so the sensing test is one integer compare of the bits of x >= 0), -1 if none
   long long cyc_sense_x2;
+  // FP32 squared-distance bounds from the offsets: below sense_in2 a vertex pair is surely
+  // closer than cyc_sense, above sense_out2 surely not; in between the FP64 test decides
+  float sense_in2, sense_out2;
 };
 
 // Arguments shared by the per-step kernels of a pack.
@@ -120,6 +123,8 @@ struct PackArgs {
                        // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
   int32_t variant;    // force kernel: 0 default, 1 thread per agent (CRG_OPT_KERNEL_VARIANT)
+  int32_t tile;       // spheres, thread per agent: 0 one thread per agent in a grid over all
+                      // agents; k > 0 the persistent tile kernel, blockDim * k agents a tile
   // cell cycle (rods; all null when off)
   const double *slen;       // [cap] spring length of each rod (current order)
   const double *grate;      // [cap] growth rate of each rod (current order)

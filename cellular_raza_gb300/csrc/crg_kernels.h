@@ -96,6 +96,7 @@ void launch_rods_step(int dim, int nv, int precision, const PackArgs &P, int blo
                       cudaStream_t st, cudaEvent_t k0 = nullptr, cudaEvent_t k1 = nullptr,
                       cudaEvent_t k2 = nullptr, cudaEvent_t k3 = nullptr);
 int prepare_rods(int dim, int nv);  // 0 on success
+int prepare_spheres(int dim, int precision);  // 0 on success
 // Cell cycle of rods: neighbour counts of this step (before the update kernel), and after
 // the update and the scan of its division flags, the divisions (n_div > 0), then the voxel
 // counters (launched once the divisions are known to have succeeded).

@@ -1650,6 +1650,9 @@ __global__ void __launch_bounds__(128) k_rods_sense(const PackArgs P) {
   const double r = S.cyc_sense;
   const double thr = dadd(r, dmul(fabs(r), 1e-9));
   const long long x2 = S.cyc_sense_x2;  // sqrt(n2) < r exactly when bits(n2) <= x2
+  float oa[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) oa[k] = P.off[k * cap + i];
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -1667,6 +1670,10 @@ __global__ void __launch_bounds__(128) k_rods_sense(const PackArgs P) {
           if (lane == 0) invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
           b1 = b0;
         }
+        float kd[D];  // b's offsets in a's voxel frame: off_b + (j - idx) dx
+        kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
+        kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+        if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
         for (uint32_t b = b0 + lane; b < b1; b += 32) {
           if (b == i) continue;
           double pb[NC];
@@ -1684,10 +1691,25 @@ __global__ void __launch_bounds__(128) k_rods_sense(const PackArgs P) {
             far |= dsub(lb, hi_a[c]) > thr || dsub(lo_a[c], hb) > thr;
           }
           if (far) continue;
+          float ob[NC];
+#pragma unroll
+          for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
 #pragma unroll
           for (int u = 0; u < NV; ++u)
 #pragma unroll
             for (int q = 0; q < NV; ++q) {
+              // FP32 first: clearly inside or outside the range (NaN offsets fall through)
+              float d2f = 0.f;
+#pragma unroll
+              for (int c = 0; c < D; ++c) {
+                const float e = oa[u * D + c] - ob[q * D + c];
+                d2f = fmaf(e, e, d2f);
+              }
+              if (d2f < S.sense_in2) {
+                ++cnt;
+                continue;
+              }
+              if (d2f > S.sense_out2) continue;
               double n2 = 0.0;
 #pragma unroll
               for (int c = 0; c < D; ++c) {

@@ -324,11 +324,10 @@ __device__ __forceinline__ void sphere_update(const PackArgs &P, const SimDev &S
 constexpr int kSurv = 16;
 constexpr size_t mixed_step_smem(int block) { return (size_t)kSurv * block * 5; }
 
+// The force and update of agent i (thread per agent; sSurv: the block's survivor buffer).
 template <int D, int PREC>
-__global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
-  extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P.n_agents) return;
+__device__ __forceinline__ void sphere_agent(const PackArgs &P, const uint32_t i,
+                                             uint32_t *sSurv) {
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
   const SimDev &S = P.sims[sim];
   const int64_t cap = P.cap;
@@ -499,6 +498,70 @@ __global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres
     for (int c = 0; c < D; ++c) acc[c] = (double)__fsub_rn(fs[c], fcmp[c]);  // the compensated sum, rounded once
   }
   sphere_update<D>(P, S, i, key, pa, va, acc);
+}
+
+template <int D, int PREC>
+__global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_step(const PackArgs P) {
+  extern __shared__ uint32_t sSurv[];  // MIXED: [kSurv][blockDim] candidates, then box codes
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n_agents) return;
+  sphere_agent<D, PREC>(P, i, sSurv);
+}
+
+// Persistent form of k_spheres_step (P.tile > 0): a grid of as many blocks as the SMs hold
+// at once, each claiming tiles of blockDim * P.tile consecutive agents of the cell list (a
+// run of voxels along the last axis and their neighbours' rows) from the counter rctl[2]
+// (zeroed before the launch) until none is left.  Thread t of a block takes agents
+// base + t, base + t + blockDim, ... of its tile: the same per-agent work as k_spheres_step,
+// so the results are identical whatever the tile size and claim order.
+template <int D, int PREC>
+__global__ void __launch_bounds__(256, (PREC == CRG_PREC_F64) ? 3 : 4) k_spheres_tiles(const PackArgs P) {
+  extern __shared__ uint32_t sSurv[];
+  __shared__ uint32_t sTile;
+  const uint32_t per = (uint32_t)P.tile, tile_agents = blockDim.x * per;
+  const uint32_t n_tiles = (P.n_agents + tile_agents - 1) / tile_agents;
+  for (;;) {
+    if (threadIdx.x == 0) sTile = atomicAdd(&P.rctl[2], 1u);
+    __syncthreads();
+    const uint32_t t = sTile;
+    __syncthreads();  // every thread has read sTile before thread 0 claims again
+    if (t >= n_tiles) break;
+    const uint32_t base = t * tile_agents;
+    for (uint32_t j = 0; j < per; ++j) {
+      const uint32_t i = base + j * blockDim.x + threadIdx.x;
+      if (i < P.n_agents) sphere_agent<D, PREC>(P, i, sSurv);
+    }
+  }
+}
+
+// Resident blocks of k_spheres_tiles on the whole device for [dim - 2][precision == MIXED]
+// [block / 64 - 1], set by prepare_spheres when a handle is created (an occupancy query
+// inside a stream capture could load the module, which a capture does not allow); 0: unknown.
+unsigned g_tile_grid[2][2][4] = {};
+
+template <int D, int PREC>
+cudaError_t prepare_tiles() {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  for (int q = 0; q < 4 && e == cudaSuccess; ++q) {
+    const int block = 64 * (q + 1);
+    const size_t smem = (PREC == CRG_PREC_F64) ? 0 : mixed_step_smem(block);
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_spheres_tiles<D, PREC>, block, smem);
+    if (e == cudaSuccess) g_tile_grid[D - 2][PREC == CRG_PREC_F64 ? 0 : 1][q] = (unsigned)(sms * n);
+  }
+  return e;
+}
+
+template <int D, int PREC>
+void launch_tiles(const PackArgs &P, int block, cudaStream_t st) {
+  const uint32_t tile_agents = (uint32_t)block * (uint32_t)P.tile;
+  const unsigned n_tiles = (P.n_agents + tile_agents - 1) / tile_agents;
+  unsigned grid = g_tile_grid[D - 2][PREC == CRG_PREC_F64 ? 0 : 1][block / 64 - 1];
+  if (!grid || grid > n_tiles) grid = n_tiles;
+  const size_t smem = (PREC == CRG_PREC_F64) ? 0 : mixed_step_smem(block);
+  k_spheres_tiles<D, PREC><<<grid, block, smem, st>>>(P);
 }
 
 // Largest system the FP64 default runs with agent groups (k_spheres_groups); above it the
@@ -1027,7 +1090,11 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
     }
     return;
   }
-  if (precision != CRG_PREC_F64) cudaMemsetAsync(P.rctl, 0, sizeof(uint32_t), st);
+  if (block <= 0 || block > 256) block = 128;
+  // persistent form (thread per agent); its tile counter is rctl[2]
+  const bool tiles = P.tile > 0 && block % 64 == 0 && P.rctl != nullptr;
+  if (precision != CRG_PREC_F64 || tiles)  // fix-up count; tile counter
+    cudaMemsetAsync(P.rctl, 0, 3 * sizeof(uint32_t), st);
   if (precision != CRG_PREC_F64 && P.variant == 3) {  // warp-packed mixed kernel
     const unsigned grid = (P.n_agents + 31) / 32;
     if (dim == 3) {
@@ -1039,7 +1106,24 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
     }
     return;
   }
-  if (block <= 0 || block > 256) block = 128;
+  if (tiles) {
+    if (dim == 3) {
+      if (precision == CRG_PREC_F64) {
+        launch_tiles<3, CRG_PREC_F64>(P, block, st);
+      } else {
+        launch_tiles<3, CRG_PREC_MIXED>(P, block, st);
+        k_spheres_fix<3><<<32, 128, 0, st>>>(P);
+      }
+    } else {
+      if (precision == CRG_PREC_F64) {
+        launch_tiles<2, CRG_PREC_F64>(P, block, st);
+      } else {
+        launch_tiles<2, CRG_PREC_MIXED>(P, block, st);
+        k_spheres_fix<2><<<32, 128, 0, st>>>(P);
+      }
+    }
+    return;
+  }
   const unsigned grid = (P.n_agents + block - 1) / block;
   if (dim == 3) {
     if (precision == CRG_PREC_F64) {
@@ -1056,6 +1140,15 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
       k_spheres_fix<2><<<32, 128, 0, st>>>(P);
     }
   }
+}
+
+int prepare_spheres(int dim, int precision) {
+  cudaError_t e;
+  if (dim == 3)
+    e = precision == CRG_PREC_F64 ? prepare_tiles<3, CRG_PREC_F64>() : prepare_tiles<3, CRG_PREC_MIXED>();
+  else
+    e = precision == CRG_PREC_F64 ? prepare_tiles<2, CRG_PREC_F64>() : prepare_tiles<2, CRG_PREC_MIXED>();
+  return e == cudaSuccess ? 0 : 1;
 }
 
 void launch_sphere_stats(int dim, const PackArgs &P, uint32_t *n_cand, uint32_t *n_inter,

@@ -207,6 +207,11 @@ class Simulation:
     def set_option(self, opt: int, value: int):
         N.check(self._L.crg_set_option(self._h, int(opt), int(value)), "crg_set_option")
 
+    def get_option(self, opt: int) -> int:
+        v = C.c_int64()
+        N.check(self._L.crg_get_option(self._h, int(opt), C.byref(v)), "crg_get_option")
+        return v.value
+
     def debug_forces(self) -> Dict[str, np.ndarray]:
         n = self.n_agents
         f = np.empty((n, self.nv, self.dim))
@@ -260,7 +265,8 @@ class Simulation:
         v, b, ms = C.c_int64(), C.c_int64(), C.c_double()
         rc = self._L.crg_autotune(self._h, int(steps), C.byref(v), C.byref(b), C.byref(ms))
         N.check(rc, "crg_autotune", self._h)
-        return {"variant": v.value, "block": b.value, "ms_per_step": ms.value}
+        return {"variant": v.value, "block": b.value, "tile": self.get_option(N.OPT_TILE),
+                "ms_per_step": ms.value}
 
     def profile(self):
         out = (C.c_double * 5)()

@@ -269,10 +269,11 @@ int32_t crg_checkpoint_load(crg_ctx *ctx, const void *buf, int64_t bytes);
 int32_t crg_get_stream(crg_ctx *ctx, void **stream);
 
 /* Autotuner: times `steps` steps of every force-kernel shape this handle can use (kernel
- * variant x block size) on the handle's current state, restoring that state after each
- * trial (crg_snapshot), and keeps the fastest: *variant and *block receive the chosen
- * CRG_OPT_KERNEL_VARIANT / CRG_OPT_BLOCK values, *ms_per_step its time.  The simulation
- * state is unchanged on return. */
+ * variant x block size x tile, the tile for the persistent sphere kernel) on the handle's
+ * current state, restoring that state after each trial (crg_snapshot), and keeps the
+ * fastest: *variant and *block receive the chosen CRG_OPT_KERNEL_VARIANT / CRG_OPT_BLOCK
+ * values, *ms_per_step its time; the chosen CRG_OPT_TILE is read with crg_get_option.  The
+ * simulation state is unchanged on return. */
 int32_t crg_autotune(crg_ctx *ctx, int64_t steps, int64_t *variant, int64_t *block,
                      double *ms_per_step);
 
@@ -287,6 +288,9 @@ const char *crg_strerror(int32_t code);
 #define CRG_OPT_GRAPH_CHUNK 2 /* steps per captured CUDA graph (0 disables graphs) */
 #define CRG_OPT_BLOCK 3       /* threads per block of the force kernel (autotuner) */
 int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
+/* The current value of an option (CRG_OPT_PASS_LIST: the pass list's capacity in passes;
+ * CRG_OPT_DEBUG_FORCES: 1 while forces are captured).  CRG_EINVAL for an unknown option. */
+int32_t crg_get_option(crg_ctx *ctx, int32_t option, int64_t *value);
 
 /* Interaction force accumulated during the most recent step, [n][nv][dim] in the order
  * of the ids array (same layout as crg_download's ids).  Capture must have been enabled
@@ -306,6 +310,12 @@ int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
  * forces with the rod-level kernel instead (same results) and the list is grown to fit at
  * the end of crg_step.  Created with 12 passes per rod of capacity. */
 #define CRG_OPT_PASS_LIST 7
+/* Spheres, thread-per-agent kernel (CRG_OPT_KERNEL_VARIANT 1, or the mixed default): 0
+ * (default) one thread per agent in a grid over all agents; k in 1..16 the persistent form,
+ * as many blocks as the SMs hold at once (CRG_OPT_BLOCK threads, a multiple of 64; 128 when
+ * 0), each claiming tiles of CRG_OPT_BLOCK x k consecutive agents of the cell list until
+ * none is left.  The results do not depend on it. */
+#define CRG_OPT_TILE 8
 int32_t crg_debug_forces(crg_ctx *ctx, double *force, uint64_t *ids);
 
 /* Neighbour statistics of the CURRENT cell list (what the next step will visit): per agent

@@ -47,3 +47,19 @@ def test_status_strings_without_gpu():
     lib = _native.load()
     assert lib.crg_strerror(_native.CRG_EBOUNDARY).decode().startswith("agent outside")
     assert lib.crg_strerror(12345).decode() == "unknown status"
+
+
+def test_option_numbers_match_header():
+    text = open(os.path.join(ROOT, "include", "crg.h")).read()
+    declared = {m.group(1): int(m.group(2))
+                for m in re.finditer(r"#define CRG_OPT_([A-Z_]+)\s+(\d+)", text)}
+    bound = {k[4:]: v for k, v in vars(_native).items() if k.startswith("OPT_")}
+    assert declared == bound
+
+
+def test_options_need_a_handle():
+    lib = _native.load()
+    v = ctypes.c_int64(-1)
+    assert lib.crg_get_option(None, _native.OPT_TILE, ctypes.byref(v)) == _native.CRG_EINVAL
+    assert lib.crg_set_option(None, _native.OPT_TILE, 1) == _native.CRG_EINVAL
+    assert v.value == -1

@@ -67,3 +67,56 @@ def test_rod_batch_members_equal_single_runs(gpu):
         off += w.n
         alone = E.run(w, 30 if s == 1 else 60)
         assert np.array_equal(g["pos"], alone["pos"]) and np.array_equal(g["vel"], alone["vel"])
+
+
+def run_pack_shape(ws, steps, variant, block, tile):
+    sim = E.Simulation([w.model for w in ws], [w.n for w in ws])
+    sim.set_option(N.OPT_KERNEL_VARIANT, variant)
+    sim.set_option(N.OPT_BLOCK, block)
+    sim.set_option(N.OPT_TILE, tile)
+    assert sim.get_option(N.OPT_TILE) == tile
+    sim.upload(np.concatenate([w.pos for w in ws]), np.concatenate([w.vel for w in ws]),
+               counts=[w.n for w in ws])
+    sim.step(steps)
+    out = sim.download(order="id")
+    sim.close()
+    return out
+
+
+@pytest.mark.parametrize("precision", ["f64", "mixed"])
+def test_persistent_tiles_equal_one_shot_grid(gpu, precision):
+    """The persistent tile kernel (blocks claiming tiles of block x k agents until none is
+    left) does each agent's work exactly as the one-thread-per-agent grid does: bitwise equal
+    for every block and tile size, on a pack of uneven simulations (3D and 2D)."""
+    for dim in (3, 2):
+        rng = np.random.Generator(np.random.PCG64(83 + dim))
+        ns = np.exp(rng.uniform(np.log(150), np.log(9000), size=9)).astype(int)
+        # 3D at the ensemble's density; 2D at one agent per 250 unit^2
+        ws = [W.spheres(int(n), (n / 5.12e-4) ** (1 / 3) if dim == 3 else (n * 250.0) ** 0.5,
+                        seed=900 + s, dim=dim, strength=float(rng.uniform(0.1, 1.0)),
+                        damping=float(rng.uniform(0.5, 2.0)), precision=precision)
+              for s, n in enumerate(ns)]
+        ref = run_pack_shape(ws, 40, 1, 128, 0)
+        for block, tile in [(64, 1), (128, 1), (128, 3), (256, 2), (256, 16)]:
+            got = run_pack_shape(ws, 40, 1, block, tile)
+            for k in ("pos", "vel", "voxel"):
+                assert np.array_equal(got[k], ref[k]), (dim, block, tile, k)
+
+
+def test_autotune_reports_tile_and_keeps_state(gpu):
+    ws = W.ensemble(seed=86, n_sims=5, n_lo=300, n_hi=5000, precision="mixed", n_steps=20)
+    sim = E.Simulation([w.model for w in ws], [w.n for w in ws])
+    sim.upload(np.concatenate([w.pos for w in ws]), np.concatenate([w.vel for w in ws]),
+               counts=[w.n for w in ws])
+    sim.step(5)
+    before = sim.download(order="id")
+    tune = sim.autotune(2)
+    assert tune["tile"] == sim.get_option(N.OPT_TILE)
+    assert tune["block"] == sim.get_option(N.OPT_BLOCK)
+    after = sim.download(order="id")
+    assert np.array_equal(before["pos"], after["pos"])
+    sim.step(10)
+    got = sim.download(order="id")
+    sim.close()
+    ref = run_pack_shape(ws, 15, 1, 128, 0)
+    assert np.array_equal(got["pos"], ref["pos"]) and np.array_equal(got["vel"], ref["vel"])
