@@ -31,6 +31,7 @@ EXPORTED = [
     "crg_agent_count", "crg_last_error", "crg_destroy", "crg_strerror", "crg_set_option",
     "crg_get_option",
     "crg_debug_forces", "crg_debug_neighbor_stats", "crg_profile", "crg_measure_fma_peaks",
+    "crg_check_division",
     "crg_snapshot", "crg_get_stream", "crg_cell_list_noalloc", "crg_autotune",
     "crg_set_sim_stop", "crg_sim_download", "crg_clear_error", "crg_repack", "crg_step_count",
     "crg_checkpoint_size", "crg_checkpoint_save", "crg_checkpoint_load",
@@ -134,6 +135,7 @@ def load(build_if_missing: bool = True):
     L.crg_debug_neighbor_stats.argtypes = [vp, u32p, u32p, u64p, u64p]
     L.crg_profile.argtypes = [vp, dp]
     L.crg_measure_fma_peaks.argtypes = [dp, dp]
+    L.crg_check_division.argtypes = [C.c_int64, C.c_uint64, i64p, i64p]
     L.crg_snapshot.argtypes = [vp, C.c_int32]
     L.crg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.crg_cell_list_noalloc.argtypes = [C.POINTER(CrgDomain), C.c_int64, vp, vp, vp, vp, vp]

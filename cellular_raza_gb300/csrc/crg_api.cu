@@ -53,6 +53,7 @@ struct crg_ctx {
   double *mbuf = nullptr;
   int64_t pass_cap = 0;
   uint32_t *rctl = nullptr;
+  double *seg = nullptr;  // FP64 rods: per-segment l1 - l0, squared norm, reciprocal
   uint32_t *fix_list = nullptr;  // mixed spheres: agents for the FP64 fix-up kernel
   double *bend = nullptr;        // rods: curvature forces between the bend and update kernels
   // cell cycle (rods, single simulation): per-agent state (current / next), neighbour
@@ -364,7 +365,7 @@ void free_all(crg_ctx *c) {
   void *ptrs[] = {c->d_sims, c->d_agent_off, c->d_sim_of_voxel, c->pos, c->vel, c->npos,
                   c->nvel, c->id, c->nid, c->key, c->nkey, c->off, c->hist, c->nhist,
                   c->hmeta, c->nhmeta, c->count, c->start, c->bsum, c->tmp, c->status,
-                  c->step_ctr, c->dbg_force, c->frc, c->hl, c->vcen, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off,
+                  c->step_ctr, c->dbg_force, c->frc, c->hl, c->vcen, c->fbuf, c->bend, c->rctl, c->fix_list, c->npass, c->pass_off, c->seg,
                   c->staging, c->snap, c->slen, c->nslen, c->grate, c->ngrate, c->parent,
                   c->nparent, c->vctr, c->nsense, c->dflag, c->dpre, c->dbsum, c->srank};
   for (void *p : ptrs)
@@ -383,8 +384,10 @@ int32_t allocate(crg_ctx *c) {
   const int64_t cap = c->cap;
   const int nc = c->nc;
   int32_t r;
-#define A(ptr, n) \
-  if ((r = dalloc(&c->ptr, (size_t)(n))) != CRG_OK) return r
+#define A(ptr, n)                                              \
+  do {                                                         \
+    if ((r = dalloc(&c->ptr, (size_t)(n))) != CRG_OK) return r; \
+  } while (0)
   A(d_sims, c->n_sims);
   A(d_agent_off, c->n_sims + 1);
   A(pos, cap * nc);
@@ -408,7 +411,11 @@ int32_t allocate(crg_ctx *c) {
   if (c->kind == CRG_KIND_ROD) {
     A(frc, cap * nc);
     A(bend, cap * (c->nv > 2 ? c->nv - 2 : 1) * c->dim);
-    if (c->precision != CRG_PREC_F64) A(hl, cap * nc);
+    if (c->precision != CRG_PREC_F64) {
+      A(hl, cap * nc);
+    } else {
+      A(seg, cap * (size_t)(c->nv - 1) * (c->dim + 2));
+    }
     A(rctl, 4);
     A(npass, cap);
     A(pass_off, cap);
@@ -565,6 +572,7 @@ PackArgs pack_args(crg_ctx *c) {
   P.fix_list = c->fix_list;
   P.bend = c->bend;
   P.hl = c->hl;
+  P.seg = c->seg;
   P.npass = c->npass;
   P.pass_off = c->pass_off;
   P.pass_a = c->pass_a;
@@ -1791,6 +1799,11 @@ int32_t crg_debug_neighbor_stats(crg_ctx *c, uint32_t *n_cand, uint32_t *n_inter
 int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
   if (!fp64_tflops || !fp32_tflops) return CRG_EINVAL;
   return crg::measure_fma_peaks(fp64_tflops, fp32_tflops);
+}
+
+int32_t crg_check_division(int64_t n, uint64_t seed, int64_t *mismatches, int64_t *fast) {
+  if (n < 0 || !mismatches || !fast) return CRG_EINVAL;
+  return crg::check_division(n, seed, mismatches, fast);
 }
 
 }  // extern "C"

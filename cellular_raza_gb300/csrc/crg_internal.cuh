@@ -119,6 +119,8 @@ struct PackArgs {
   double *bend;    // rods: [nv - 2][dim][cap] curvature forces (k_rods_bend)
   float2 *hl;      // mixed-precision rods: [nc][cap] each coordinate x as FP32 hi = (float)x
                    // and lo = (float)(x - hi), written by k_rods_walk (null on FP64)
+  double *seg;     // FP64 rods: [nv - 1][dim + 2][cap] per segment l1 - l0 (dim), its squared
+                   // norm n and RN(1 / n), written by k_rods_walk (null on mixed)
   uint32_t *fix_list;  // mixed spheres: agents whose force the FP64 fix-up kernel computes
                        // (count in rctl[0])
   int32_t prefilter;  // 0 disables the FP32 candidate prefilter (testing)
@@ -157,6 +159,28 @@ __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a,
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// a / b rounded to nearest -- the bits of ddiv(a, b) -- from y = RN(1 / b), b's correctly
+// rounded reciprocal, with one multiply and four FMAs (no division) when a and b are finite,
+// non-zero and of binary exponent in [-400, 400]; otherwise ddiv itself.  q = RN(a y) lies
+// within 2 ulp of a / b.  One residual step, q + (a - b q) y with the residual from an FMA,
+// leaves q within 2^-51 ulp of a / b before rounding: faithful.  For a faithful q and
+// y = RN(1 / b) the residual a - b q is exact in an FMA and RN(q + (a - b q) y) = RN(a / b)
+// (Markstein's theorem: P. W. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook
+// of Floating-Point Arithmetic, division with a fused multiply-add).  The exponent range
+// keeps every intermediate (q within 2^+-801, the residual's granularity above 2^-505) in
+// the normal range, where the theorem holds.
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+  const unsigned long long ea = ((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ffull;
+  const unsigned long long eb = ((unsigned long long)__double_as_longlong(b) >> 52) & 0x7ffull;
+  if (ea - 623ull > 800ull || eb - 623ull > 800ull) return ddiv(a, b);  // biased 623..1423
+  double q = __dmul_rn(a, y);
+  double r = __fma_rn(-b, q, a);
+  q = __fma_rn(r, y, q);
+  r = __fma_rn(-b, q, a);
+  return __fma_rn(r, y, q);
+}
 
 // 0.0 + x, exactly: x itself except that -0.0 becomes +0.0 (integer instructions only).
 __device__ __forceinline__ double plus_zero(double x) {

@@ -113,5 +113,6 @@ void launch_neighbor_stats(int dim, int nv, const PackArgs &P, uint32_t *n_cand,
                            uint32_t *n_inter, uint64_t *hash, cudaStream_t st);
 
 int measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
+int check_division(int64_t n, uint64_t seed, int64_t *mismatches, int64_t *fast);
 
 }  // namespace crg

@@ -70,6 +70,30 @@ __device__ __forceinline__ void nearest_point_f64(const double *p, const double 
   for (int c = 0; c < D; ++c) q[c] = dadd(dmul(l0[c], omt), dmul(l1[c], t));
 }
 
+// nearest_point_f64 for segment sy of rod r with the segment's l1 - l0, squared norm and its
+// reciprocal taken from P.seg (k_rods_walk computes them with nearest_point_f64's operations)
+// and t = dot / nsq from div_rn_recip: the same q and t, bit for bit, with no division.
+template <int D>
+__device__ __forceinline__ void nearest_point_seg(const double *p, const double *l0,
+                                                  const double *l1, const double *seg,
+                                                  int64_t cap, double *q, double &t) {
+  double ab[D], ap[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    ab[c] = seg[c * cap];
+    ap[c] = dsub(p[c], l0[c]);
+  }
+  double dot = dmul(ab[0], ap[0]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) dot = dadd(dot, dmul(ab[c], ap[c]));
+  t = div_rn_recip(dot, seg[D * cap], seg[(D + 1) * cap]);
+  if (lt_zero(t)) t = 0.0;
+  if (gt_one(t)) t = 1.0;
+  const double omt = dsub(1.0, t);
+#pragma unroll
+  for (int c = 0; c < D; ++c) q[c] = dadd(dmul(l0[c], omt), dmul(l1[c], t));
+}
+
 // Full (unhalved) Morse force on `own` from the point `ext` (interaction.rs:151-182).
 template <int D>
 __device__ __forceinline__ bool morse_full_f64(const double *own, const double *ext,
@@ -1046,7 +1070,10 @@ __device__ __forceinline__ void eval_fold_queue(const PackArgs &P, double *sRes,
           l0[c] = P.pos[(sy * D + c) * cap + sr];
           l1[c] = P.pos[((sy + 1) * D + c) * cap + sr];
         }
-        nearest_point_f64<D>(p, l0, l1, q, tt);
+        if (P.seg)  // written by this step's k_rods_walk
+          nearest_point_seg<D>(p, l0, l1, P.seg + (int64_t)sy * (D + 2) * cap + sr, cap, q, tt);
+        else
+          nearest_point_f64<D>(p, l0, l1, q, tt);
         if (!morse_full_f64<D>(p, q, P.sims[sim_l], f)) {
 #pragma unroll
           for (int c = 0; c < D; ++c) f[c] = 0.0;  // adding +0 leaves M unchanged
@@ -1197,6 +1224,26 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
   const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, ii);
   const SimDev &S = P.sims[sim];
   const bool live = valid && !sim_frozen(P, S);  // frozen rods have no passes
+  if (P.seg && valid) {
+    // FP64: each segment's l1 - l0, squared norm and reciprocal for the pass kernel, with
+    // the operations of nearest_point_f64
+    constexpr int NE = NV - 1;
+#pragma unroll
+    for (int sy = 0; sy < NE; ++sy) {
+      double ab[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+        ab[c] = dsub(P.pos[((sy + 1) * D + c) * cap + i], P.pos[(sy * D + c) * cap + i]);
+      double nsq = dmul(ab[0], ab[0]);
+#pragma unroll
+      for (int c = 1; c < D; ++c) nsq = dadd(nsq, dmul(ab[c], ab[c]));
+      double *sg = P.seg + (int64_t)sy * (D + 2) * cap + i;
+#pragma unroll
+      for (int c = 0; c < D; ++c) sg[c * cap] = ab[c];
+      sg[D * cap] = nsq;
+      sg[(D + 1) * cap] = __drcp_rn(nsq);
+    }
+  }
   if (P.hl && live) {  // mixed precision: the hi / lo split of the rod's coordinates
 #pragma unroll
     for (int k = 0; k < NC; ++k) {

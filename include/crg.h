@@ -338,6 +338,13 @@ int32_t crg_profile(crg_ctx *ctx, double *out5);
  * dependent-chain microbenchmark (TFLOP/s, 2 flops per FMA). */
 int32_t crg_measure_fma_peaks(double *fp64_tflops, double *fp32_tflops);
 
+/* Checks the FP64 rod pass kernel's division (a quotient from b's correctly rounded
+ * reciprocal, with FMA residual corrections) against the IEEE division on n generated
+ * operand pairs: rod-like values, random exponents across the fast path's range, quotients
+ * next to rounding midpoints, all-ones and power-of-two divisors.  *mismatches receives
+ * the pairs whose bits differ (0 expected), *fast the pairs that took the fast path. */
+int32_t crg_check_division(int64_t n, uint64_t seed, int64_t *mismatches, int64_t *fast);
+
 /* ---- cell list without device allocation -------------------------------------------
  * No counterpart in the reference: chili keeps its cells in per-voxel Vecs and never
  * builds a device cell list.
