@@ -80,6 +80,7 @@ struct crg_ctx {
   int prefilter = 1;
   int variant = 0;
   int tile = 0;  // CRG_OPT_TILE
+  bool grow_target = false;  // created by grow_capacity: loads a checkpoint of any capacity
   int block = 0;
   int profile = 0;
   double prof_ms[5] = {0, 0, 0, 0, 0};
@@ -745,6 +746,45 @@ void invalidate_graph(crg_ctx *c) {
   c->gexec_steps = 0;
 }
 
+// Cell-cycle handles whose divisions would outgrow the capacity: the handle's state (the
+// state before the step, which nothing of the step has changed yet) moves to a new handle of
+// at least `need` and twice the capacity, through a checkpoint, and the new handle's
+// resources replace the old ones behind the same pointer (the stream stays the caller's).
+int32_t grow_capacity(crg_ctx *c, int64_t need) {
+  int64_t new_cap = std::max<int64_t>(need, 2 * c->cap);
+  new_cap = std::min<int64_t>(new_cap, 0x7fffffffll);
+  if (new_cap < need) return CRG_ENOMEM;
+  int64_t bytes = 0;
+  int32_t r = crg_checkpoint_size(c, &bytes);
+  if (r != CRG_OK) return r;
+  std::vector<char> blob((size_t)bytes);
+  r = crg_checkpoint_save(c, blob.data(), bytes);
+  if (r != CRG_OK) return r;
+  crg_ctx *g = nullptr;
+  r = create_impl(1, c->doms.data(), c->mods.data(), &new_cap, &g);
+  if (r != CRG_OK) return r;
+  g->grow_target = true;
+  g->graph_chunk = c->graph_chunk;
+  g->prefilter = c->prefilter;
+  g->variant = c->variant;
+  g->tile = c->tile;
+  g->block = c->block;
+  g->profile = c->profile;
+  if (c->dbg_force) r = crg_set_option(g, CRG_OPT_DEBUG_FORCES, 1);
+  if (r == CRG_OK && c->pass_cap > g->pass_cap) r = alloc_pass_list(g, c->pass_cap);
+  if (r == CRG_OK) r = crg_checkpoint_load(g, blob.data(), bytes);
+  g->grow_target = false;
+  if (r != CRG_OK) {
+    crg_destroy(g);
+    return r;
+  }
+  cudaStreamSynchronize(c->stream);
+  std::swap(*c, *g);
+  std::swap(c->stream, g->stream);  // the caller keeps its stream; g's own is destroyed
+  crg_destroy(g);
+  return CRG_OK;
+}
+
 // Cell-cycle handles run one step at a time: divisions change the agent count that every
 // launch is sized by.  Per step: neighbour counts (k_rods_sense), forces and the update
 // (growth, division flags), the scan of the flags, a read of the division count, the
@@ -769,10 +809,16 @@ int32_t step_cycle(crg_ctx *c, int64_t n_steps) {
     if (read_status(c) != CRG_OK) break;
     const uint32_t n_div = c->h_ndiv[0];
     if ((int64_t)n + (int64_t)n_div > c->cap) {
-      c->err_code = CRG_ENOMEM;
-      c->err_agent = -1;
-      c->err_step = c->steps_done + done + 1;
-      break;
+      // nothing of this step is committed yet: grow the handle and take the step again
+      const int32_t r = grow_capacity(c, (int64_t)n + (int64_t)n_div);
+      if (r != CRG_OK) {
+        c->err_code = r;
+        c->err_agent = -1;
+        c->err_step = c->steps_done + done + 1;
+        break;
+      }
+      --done;
+      continue;
     }
     if (n_div) {
       crg::launch_rods_divide(c->dim, c->nv, P, n_div, st);
@@ -1171,7 +1217,7 @@ struct CkptHeader {
   uint64_t params;  // params_hash of the handle's domains and models
 };
 constexpr char kCkptMagic[8] = {'C', 'R', 'G', 'C', 'K', 'P', 'T', '1'};
-constexpr int32_t kCkptVersion = 3;
+constexpr int32_t kCkptVersion = 4;
 
 // FNV-1a over every field of the handle's domains, models and capacities (field by field:
 // crg_model has padding bytes), so a checkpoint loads only into a handle that steps the same
@@ -1221,27 +1267,34 @@ std::vector<CkptSlice> ckpt_slices(crg_ctx *c) {
     v.push_back({(char *)c->hist, sizeof(double), 2 * nc});
     v.push_back({(char *)c->hmeta, 1, 1});
   }
+  if (c->cycle) {  // spring length, growth rate and parent of every rod
+    v.push_back({(char *)c->slen, sizeof(double), 1});
+    v.push_back({(char *)c->grate, sizeof(double), 1});
+    v.push_back({(char *)c->parent, sizeof(uint64_t), 1});
+  }
   return v;
 }
 
+// header, agent offsets, stop steps and step bases, the slices, the cell starts, the step
+// counter and (cell cycle) every voxel's id counter
 size_t ckpt_bytes(crg_ctx *c, uint32_t n_agents) {
   size_t b = sizeof(CkptHeader) + sizeof(uint32_t) * (c->n_sims + 1) +
              2 * sizeof(int64_t) * c->n_sims;
   for (const CkptSlice &s : ckpt_slices(c)) b += s.elem * s.comps * n_agents;
-  return b + sizeof(uint32_t) * ((size_t)c->n_vox + 1) + sizeof(int64_t);
+  b += sizeof(uint32_t) * ((size_t)c->n_vox + 1) + sizeof(int64_t);
+  if (c->cycle) b += sizeof(uint64_t) * (size_t)c->n_vox;
+  return b;
 }
 
 }  // namespace
 
 int32_t crg_checkpoint_size(crg_ctx *c, int64_t *bytes) {
   if (!c || !bytes) return CRG_EINVAL;
-  if (c->cycle) return CRG_ENOTSUP;  // the cycle state is not part of checkpoints
   *bytes = (int64_t)ckpt_bytes(c, c->n_agents);
   return CRG_OK;
 }
 
 int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
-  if (c && c->cycle) return CRG_ENOTSUP;
   if (!c || !buf || bytes < (int64_t)ckpt_bytes(c, c->n_agents)) return CRG_EINVAL;
   if (c->err_code != CRG_OK) return c->err_code;
   char *p = (char *)buf;
@@ -1276,19 +1329,26 @@ int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
                            cudaMemcpyDeviceToHost, st));
   p += sizeof(uint32_t) * ((size_t)c->n_vox + 1);
   CUDA_TRY(cudaMemcpyAsync(p, c->step_ctr, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  p += sizeof(int64_t);
+  if (c->cycle)
+    CUDA_TRY(cudaMemcpyAsync(p, c->vctr, sizeof(uint64_t) * (size_t)c->n_vox,
+                             cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   return CRG_OK;
 }
 
 int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
-  if (c && c->cycle) return CRG_ENOTSUP;
   if (!c || !buf || bytes < (int64_t)sizeof(CkptHeader)) return CRG_EINVAL;
+  // a handle made to grow a cell-cycle handle (from the same domains and models) takes a
+  // checkpoint of another capacity, whose parameter hash differs in that field
+  const bool check_params = !c->grow_target;
   const char *p = (const char *)buf;
   CkptHeader h;
   std::memcpy(&h, p, sizeof(h));
   if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != kCkptVersion ||
       h.n_sims != c->n_sims || h.nc != c->nc || h.dim != c->dim || h.kind != c->kind ||
-      h.order != c->order || h.n_vox != c->n_vox || h.params != params_hash(c) ||
+      h.order != c->order || h.n_vox != c->n_vox ||
+      (check_params && h.params != params_hash(c)) ||
       h.n_agents > (uint64_t)c->cap || bytes < (int64_t)ckpt_bytes(c, h.n_agents))
     return CRG_EINVAL;
   p += sizeof(h);
@@ -1344,11 +1404,16 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
                            cudaMemcpyHostToDevice, st));
   p += sizeof(uint32_t) * ((size_t)c->n_vox + 1);
   CUDA_TRY(cudaMemcpyAsync(c->step_ctr, p, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  p += sizeof(int64_t);
+  if (c->cycle)
+    CUDA_TRY(cudaMemcpyAsync(c->vctr, p, sizeof(uint64_t) * (size_t)c->n_vox,
+                             cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int32_t) * 8, st));
   CUDA_TRY(cudaMemsetAsync(c->count, 0, sizeof(uint32_t) * ((size_t)c->n_vox + 1), st));
   CUDA_TRY(cudaStreamSynchronize(st));
   return CRG_OK;
 }
+
 
 int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block,
                      double *ms_per_step) {

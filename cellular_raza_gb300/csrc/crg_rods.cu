@@ -111,8 +111,9 @@ __device__ __forceinline__ bool morse_full_f64(const double *own, const double *
   if (mag <= 0x7ff0000000000000ull && (mag == 0ull || db > S.cutoff_bits)) return false;
   const double e = exp(dmul(S.mrs_nstiff, dsub(dist, S.mrs_r)));
   const double force = dmul(dmul(S.mrs_k, e), dsub(1.0, e));
+  const double y = __drcp_rn(dist);  // z[c] / dist for every c from one reciprocal
 #pragma unroll
-  for (int c = 0; c < D; ++c) f[c] = dmul(ddiv(z[c], dist), force);
+  for (int c = 0; c < D; ++c) f[c] = dmul(div_rn_recip(z[c], dist, y), force);
   return true;
 }
 

@@ -232,7 +232,10 @@ int32_t crg_set_spring_lengths(crg_ctx *ctx, const double *spring_length);
 
 /* Cell cycle: per-agent spring length, growth rate and parent identifier, in the order
  * of crg_download.  Any pointer may be NULL.  A step whose divisions would take the agent
- * count past the handle's capacity stops with CRG_ENOMEM; a DivisionError is CRG_ECALC. */
+ * count past the handle's capacity first grows the handle (at least twice the capacity,
+ * state moved through a checkpoint, the same stream) and then takes the step, as chili's
+ * growable Vecs do; CRG_ENOMEM only when that allocation fails.  A DivisionError is
+ * CRG_ECALC. */
 int32_t crg_download_cycle(crg_ctx *ctx, double *spring_length, double *growth_rate,
                            uint64_t *parent);
 
@@ -250,7 +253,8 @@ int32_t crg_snapshot(crg_ctx *ctx, int32_t op);
 
 /* Host checkpoint of the handle's simulation state: positions, velocities, ids, the cell
  * list in its storage order, FP32 offsets, solver history, the step counter, and per
- * simulation its agent range, stop step and own step count.  crg_checkpoint_size gives the bytes needed;
+ * simulation its agent range, stop step and own step count; with the cell cycle also every
+ * rod's spring length, growth rate and parent and every voxel's division counter.  crg_checkpoint_size gives the bytes needed;
  * crg_checkpoint_save writes them to host memory; crg_checkpoint_load, on a handle created
  * with the same domains, models and capacities (a fresh one, or the same one later),
  * restores the state so that stepping continues bit for bit as if it had not stopped.

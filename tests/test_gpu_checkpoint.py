@@ -55,6 +55,38 @@ def test_mixed_batch_with_stop_steps_resume_bitwise(gpu):
     assert_same(straight, resumed)
 
 
+@pytest.mark.parametrize("dim,order", [(2, 1), (3, 2)])
+def test_cell_cycle_resume_bitwise(gpu, dim, order):
+    """Growing, dividing rods: spring lengths, growth rates, parents and the voxels'
+    division counters travel with the checkpoint, so the resumed colony names its daughters
+    and grows exactly as the uninterrupted one."""
+    w = W.rod_colony(n=150, side=300.0 if dim == 2 else 120.0, seed=74, dim=dim,
+                     n_subdomains=2, solver_order=order)
+    cap = 16 * w.n
+
+    def make():
+        return E.Simulation.single(w.model, cap)
+
+    a = make()
+    a.upload(w.pos, w.vel)
+    a.set_spring_lengths(w.spring_length)
+    a.step(90)
+    blob = a.checkpoint()
+    n_at_checkpoint = a.n_agents
+    a.step(110)
+    straight = a.download(order="list")
+    a.close()
+    b = make()
+    b.resume(blob)
+    assert b.n_agents == n_at_checkpoint and b.steps_done == 90
+    b.step(110)
+    resumed = b.download(order="list")
+    b.close()
+    assert len(straight["ids"]) > n_at_checkpoint > w.n  # divisions on both sides
+    for k in ("ids", "parent", "voxel", "pos", "vel", "spring_length", "growth_rate"):
+        assert np.array_equal(straight[k], resumed[k]), k
+
+
 def test_brownian_stream_continues_after_resume(gpu):
     w = W.spheres(2500, 140.0, 73, 3, kind="brownian", diffusion=0.4, kb_temperature=1.5,
                   rng_seed=5, solver_order=2)

@@ -71,14 +71,25 @@ def test_cycle_without_growth_equals_plain_rods(gpu):
     assert np.all(b["spring_length"] == w.model.spring_length)
 
 
-def test_capacity_exceeded_is_reported(gpu):
+@pytest.mark.parametrize("room", [0, 2])
+def test_capacity_grows_with_the_colony(gpu, room):
+    """A colony on a handle with room for `room` more rods: a step whose divisions do not
+    fit grows the handle (state moved through a checkpoint) and is taken again.  The run
+    equals one with ample room bit for bit, and the handle keeps its stream."""
     w = W.rod_colony(n=150, seed=3)
-    with E.Simulation.single(w.model, w.n + 2) as sim:
+    ref = gpu_run(w, 200)
+    assert len(ref["ids"]) > w.n + room  # the handle has to grow
+    with E.Simulation.single(w.model, w.n + room) as sim:
+        stream = sim.stream()
         sim.upload(w.pos, w.vel)
         sim.set_spring_lengths(w.spring_length)
-        with pytest.raises(N.CrgError) as e:
-            sim.step(200)
-        assert e.value.code == N.CRG_ENOMEM
+        sim.step(120)
+        sim.step(80)
+        assert sim.stream() == stream
+        assert sim.steps_done == 200
+        got = sim.download(order="list")
+    for k in ("ids", "parent", "voxel", "pos", "vel", "spring_length", "growth_rate"):
+        assert np.array_equal(got[k], ref[k]), k
 
 
 def test_spring_lengths_only_before_the_first_step(gpu):
