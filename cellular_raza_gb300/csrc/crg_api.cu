@@ -1429,8 +1429,11 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   } else if (c->kind == CRG_KIND_ROD) {
     shapes = {{0, 0, 0}, {1, 64, 0}};
   } else if (c->precision == CRG_PREC_F64) {
-    shapes = {{0, 0, 0}, {2, 0, 0},   {3, 0, 0},   {3, 64, 0},  {1, 64, 0},
-              {1, 128, 0}, {1, 256, 0}, {1, 128, 1}, {1, 128, 4}, {1, 256, 2}};
+    // agent groups with 8 (block 0), 16 or 32 lanes per agent; lane per agent; thread per
+    // agent, one-shot and persistent
+    shapes = {{0, 0, 0},   {2, 0, 0},   {2, 16, 0},  {2, 32, 0},  {3, 0, 0},
+              {3, 64, 0},  {1, 64, 0},  {1, 128, 0}, {1, 256, 0}, {1, 128, 1},
+              {1, 128, 4}, {1, 256, 2}};
   } else {
     // thread per agent: one-shot grids, and the persistent tile kernel with tiles of
     // block x 1, 2, 4 agents; the warp-packed kernel

@@ -567,25 +567,27 @@ void launch_tiles(const PackArgs &P, int block, cudaStream_t st) {
 // Largest system the FP64 default runs with agent groups (k_spheres_groups); above it the
 // lane-per-agent kernel has warps enough to fill the SMs.
 constexpr uint32_t kSphereGroupsMax = 38912;
-constexpr int kGrpL = 8;     // lanes per agent
-constexpr int kGrpA = 4;     // agents per warp
 constexpr int kGrpCap = 64;  // survivor list of an agent between evaluations
 
 // ---------------------------------------------------------------------------------------
 // Agent groups (FP64, small systems).  With a few thousand agents the lane-per-agent kernel
 // leaves most SMs without a warp, and a warp per agent wastes the FP64 lanes of the agent's
-// few survivors.  Here a warp carries four agents with eight lanes each:
+// few survivors.  Here a warp carries 32 / L agents with L lanes each (L = 8 by default;
+// 16 and 32 give small systems more warps):
 //   * each group numbers its agent's candidates consecutively -- the 3^D neighbourhood
 //     boxes in visiting order, each box's agents in cell-list order, itself skipped -- and
-//     scans eight per round through the FP32 prefilter, appending survivors in order to the
+//     scans L per round through the FP32 prefilter, appending survivors in order to the
 //     agent's list in shared memory;
-//   * the survivors of the four agents are evaluated in FP64 in full 32-lane batches;
-//   * each group's first lane adds its agent's half-forces in list (= candidate) order and,
-//     at the end, updates the agent.
+//   * the survivors of the warp's agents are evaluated in FP64 in full 32-lane batches;
+//   * lanes 0..D-1 of each group add the agent's half-forces in list (= candidate) order,
+//     one component each; at the end one thread per agent of the block updates it.
 // Same terms, same order of additions as k_spheres_step: identical bits.
 // ---------------------------------------------------------------------------------------
-template <int D>
+template <int D, int L>
 __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
+  constexpr int kGrpL = L;       // lanes per agent
+  constexpr int kGrpA = 32 / L;  // agents per warp
+  constexpr uint32_t kGrpMask = (L == 32) ? 0xffffffffu : ((1u << L) - 1u);
   __shared__ uint32_t sB0[4][kGrpA][27], sPre[4][kGrpA][28];
   __shared__ float sKd[4][kGrpA][27][D];
   __shared__ uint8_t sTw[4][kGrpA][27];
@@ -593,6 +595,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
   __shared__ uint8_t sWt[4][kGrpA][kGrpCap];
   __shared__ double sH[4][kGrpA][kGrpCap][D];
   __shared__ uint8_t sOk[4][kGrpA][kGrpCap];
+  __shared__ double sAcc[4][kGrpA][D];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int g = lane / kGrpL, k = lane % kGrpL;
   const uint32_t agent0 = (blockIdx.x * 4 + w) * kGrpA;
@@ -612,12 +615,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
   const uint32_t v = key - S.voxel_off;
   int idx[D];
   unravel<D>(S, v, idx);
-  double pa[D];
   float oa[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    pa[c] = P.pos[c * cap + ii];
-  }
   sphere_off<D>(P.off, ii, oa);
   const SubRange sub_v = subdomain_range(S, v);
   const float thr2 = P.prefilter ? S.filt_thr2 : __int_as_float(0x7f800000);
@@ -658,9 +656,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
   __syncwarp();
   const uint32_t total = sPre[w][g][n_box];
 
-  double acc[D];
-#pragma unroll
-  for (int c = 0; c < D; ++c) acc[c] = 0.0;
+  double acc[D], acc_k = 0.0;  // acc_k: component k of the force (lanes k < D)
   uint32_t j_next = 0;  // the group's next candidate
   while (__any_sync(0xffffffffu, j_next < total)) {
     // ---- scan rounds until the candidates are done or a list could overflow ----------
@@ -691,7 +687,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
           wt = sTw[w][g][q];
         }
       }
-      const uint32_t gm = (__ballot_sync(0xffffffffu, surv) >> (g * kGrpL)) & 0xffu;
+      const uint32_t gm = (__ballot_sync(0xffffffffu, surv) >> (g * kGrpL)) & kGrpMask;
       if (surv) {
         const int pos = n_list + __popc(gm & ((1u << k) - 1u));
         sPart[w][g][pos] = b;
@@ -703,7 +699,7 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
       }
     }
     __syncwarp();
-    // ---- FP64 Morse for the listed survivors of the four agents, full batches --------
+    // ---- FP64 Morse for the listed survivors of the warp's agents, full batches -------
     int st[kGrpA + 1];
     st[0] = 0;
 #pragma unroll
@@ -730,25 +726,41 @@ __global__ void __launch_bounds__(128) k_spheres_groups(const PackArgs P) {
       }
     }
     __syncwarp();
-    // ---- each agent's half-forces in candidate order --------------------------------
-    if (k == 0) {
+    // ---- each agent's half-forces in candidate order: lane k of the group folds
+    // component k (the components' sums are independent chains) ------------------------
+    if (k < D) {
       for (int m = 0; m < n_list; ++m) {
         if (!sOk[w][g][m]) continue;
-        const bool tw = sWt[w][g][m] == 2;
-#pragma unroll
-        for (int c = 0; c < D; ++c) {
-          acc[c] = dadd(acc[c], sH[w][g][m][c]);
-          if (tw) acc[c] = dadd(acc[c], sH[w][g][m][c]);
-        }
+        const double h = sH[w][g][m][k];
+        acc_k = dadd(acc_k, h);
+        if (sWt[w][g][m] == 2) acc_k = dadd(acc_k, h);
       }
     }
     __syncwarp();
   }
-  if (live && k == 0) {
-    double va[D];
+  // ---- updates: the block's 4 * kGrpA agents, one thread each (thread t: warp t / kGrpA,
+  // group t % kGrpA), so the update's instructions run on a quarter of the warps ---------
+  if (k < D) sAcc[w][g][k] = acc_k;
+  __syncthreads();
+  if (threadIdx.x < 4 * kGrpA) {
+    const int wu = threadIdx.x / kGrpA, gu = threadIdx.x % kGrpA;
+    const uint32_t iu = (blockIdx.x * 4 + wu) * kGrpA + gu;
+    if (iu < P.n_agents) {
+      const uint32_t simu = (P.n_sims == 1) ? 0u : sim_of_agent(P, iu);
+      const SimDev &Su = P.sims[simu];
+      uint32_t keyu = P.key[iu];
+      if (keyu - Su.voxel_off >= Su.n_vox) keyu = Su.voxel_off;  // reported above
+      if (!sim_frozen(P, Su)) {
+        double pu[D], vu[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) va[c] = P.vel[c * cap + i];
-    sphere_update<D>(P, S, i, key, pa, va, acc);
+        for (int c = 0; c < D; ++c) {
+          pu[c] = P.pos[c * cap + iu];
+          vu[c] = P.vel[c * cap + iu];
+          acc[c] = sAcc[wu][gu][c];
+        }
+        sphere_update<D>(P, Su, iu, keyu, pu, vu, acc);
+      }
+    }
   }
 }
 
@@ -1065,11 +1077,19 @@ void launch_spheres_step(int dim, int precision, const PackArgs &P, int block, c
   // warps of the lane-per-agent form (variant 2), the lane-per-agent kernel above that
   const bool small = P.n_agents <= kSphereGroupsMax;
   if (precision == CRG_PREC_F64 && (P.variant == 2 || (P.variant == 0 && small))) {
-    const unsigned grid = (P.n_agents + 4 * kGrpA - 1) / (4 * kGrpA);
-    if (dim == 3)
-      k_spheres_groups<3><<<grid, 128, 0, st>>>(P);
-    else
-      k_spheres_groups<2><<<grid, 128, 0, st>>>(P);
+    // lanes per agent: block 16 or 32 (autotuned shapes), else 8 (four agents per warp)
+    const int lanes = (block == 16 || block == 32) ? block : 8;
+    const unsigned per_block = 4 * (32 / lanes);  // agents per block of four warps
+    const unsigned grid = (P.n_agents + per_block - 1) / per_block;
+    if (dim == 3) {
+      if (lanes == 32) k_spheres_groups<3, 32><<<grid, 128, 0, st>>>(P);
+      else if (lanes == 16) k_spheres_groups<3, 16><<<grid, 128, 0, st>>>(P);
+      else k_spheres_groups<3, 8><<<grid, 128, 0, st>>>(P);
+    } else {
+      if (lanes == 32) k_spheres_groups<2, 32><<<grid, 128, 0, st>>>(P);
+      else if (lanes == 16) k_spheres_groups<2, 16><<<grid, 128, 0, st>>>(P);
+      else k_spheres_groups<2, 8><<<grid, 128, 0, st>>>(P);
+    }
     return;
   }
   if (precision == CRG_PREC_F64 && P.variant != 1) {

@@ -304,7 +304,8 @@ int32_t crg_get_option(crg_ctx *ctx, int32_t option, int64_t *value);
  * formulation).  FP64 rods: 0 = pass list (walk, pass kernel, bend, update), 1 thread per
  * rod (also the pass list's overflow fallback); mixed rods always run the pass list.  FP64
  * spheres: 0 = agent groups up to 38,912
- * agents, lane per agent above; 2 agent groups; 3 lane per agent (warp-packed survivors;
+ * agents, lane per agent above; 2 agent groups (CRG_OPT_BLOCK 16 or 32: lanes per agent,
+ * else 8); 3 lane per agent (warp-packed survivors;
  * CRG_OPT_BLOCK 64 scans 64 candidates per lane and round instead of 32).  Mixed spheres:
  * 3 lane per agent (warp-packed survivors), else one thread per agent.  All variants of one
  * precision produce identical results. */

@@ -279,11 +279,15 @@ def test_rod_passes_without_survivors(gpu):
 
 @pytest.mark.parametrize("n_sub", [1, 5])
 def test_sphere_kernel_variants_bitwise_identical(gpu, n_sub):
-    """FP64 sphere kernels -- warp per agent (the default at this size), thread per agent and
-    lane per agent with warp-packed survivors: identical bits."""
+    """FP64 sphere kernels -- agent groups of 8 lanes (the default at this size), of 16 and
+    of 32 lanes, thread per agent (one-shot and persistent) and lane per agent with
+    warp-packed survivors: identical bits."""
     w = W.spheres_3d(seed=62, n=20_000, n_subdomains=n_sub)
     a = E.run(w, 100)
     for opts in ({N.OPT_KERNEL_VARIANT: 1}, {N.OPT_KERNEL_VARIANT: 2},
+                 {N.OPT_KERNEL_VARIANT: 2, N.OPT_BLOCK: 16},
+                 {N.OPT_KERNEL_VARIANT: 2, N.OPT_BLOCK: 32},
+                 {N.OPT_KERNEL_VARIANT: 1, N.OPT_BLOCK: 128, N.OPT_TILE: 2},
                  {N.OPT_KERNEL_VARIANT: 3}, {N.OPT_KERNEL_VARIANT: 3, N.OPT_BLOCK: 64}):
         b = E.run(w, 100, options=opts)
         assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
