@@ -403,17 +403,21 @@ __device__ __forceinline__ void sphere_agent(const PackArgs &P, const uint32_t i
   // on the last axis and its pair weight) follows from two compares with the box bounds.
   constexpr int L = D - 1;  // last axis
   const int nb = hi[L] - lo[L] + 1;  // boxes per row (1..3)
-  float kdl[3];
+  // The scan's distance takes the box shift into the agent's own offset once per row (and
+  // per box on the last axis): (oa - kd) - ob, the same bound on its error as the survivors'
+  // (oa - ob) - kd (within the prefilter margin), so the scan keeps the same survivors up to
+  // pairs far beyond the cutoff, which the exact decision rejects anyway.
+  float oal[3];
 #pragma unroll
-  for (int q = 0; q < 3; ++q) kdl[q] = (float)(lo[L] + q - idx[L]) * S.dxf[L];
+  for (int q = 0; q < 3; ++q) oal[q] = oa[L] - (float)(lo[L] + q - idx[L]) * S.dxf[L];
   const int n1 = (D == 3) ? hi[1] - lo[1] + 1 : 1;
   const int n_rows = (hi[0] - lo[0] + 1) * n1;
   for (int row = 0; row < n_rows; ++row) {
     const int j0 = lo[0] + row / n1;
     const int j1 = (D == 3) ? lo[1] + row % n1 : 0;
-    float kd[D];
-    kd[0] = (float)(j0 - idx[0]) * S.dxf[0];
-    if (D == 3) kd[1] = (float)(j1 - idx[1]) * S.dxf[1];
+    float oak[D];  // the agent's offsets less the row's box shift (last axis: per box)
+    oak[0] = oa[0] - (float)(j0 - idx[0]) * S.dxf[0];
+    if (D == 3) oak[1] = oa[1] - (float)(j1 - idx[1]) * S.dxf[1];
     const uint32_t w0 = ((D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2]
                                   : (uint32_t)j0 * S.nvox[1]) + lo[L];
     // box bounds s[0..nb]; a box whose range is not valid is reported and left empty
@@ -442,15 +446,15 @@ __device__ __forceinline__ void sphere_agent(const PackArgs &P, const uint32_t i
     {
       for (uint32_t b = sb[0]; b < sb[nb]; ++b) {
         const int q = (int)(b >= sb[1]) + (int)(b >= sb[2]);
-        kd[L] = (q == 0) ? kdl[0] : (q == 1) ? kdl[1] : kdl[2];
+        oak[L] = (q == 0) ? oal[0] : (q == 1) ? oal[1] : oal[2];
         const bool twice = (tw_bits >> q) & 1u;
-        float zf[D], ob[D];
+        float ob[D];
         float d2 = 0.0f;
         sphere_off<D>(P.off, b, ob);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-          zf[c] = (oa[c] - ob[c]) - kd[c];
-          d2 = fmaf(zf[c], zf[c], d2);
+          const float z = oak[c] - ob[c];
+          d2 = fmaf(z, z, d2);
         }
         // the agent itself and pairs beyond the prefilter threshold are skipped (one branch;
         // a NaN distance falls through to the exact path)
