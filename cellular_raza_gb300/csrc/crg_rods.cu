@@ -1382,6 +1382,181 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
   });
 }
 
+// Warp-per-rod form of k_rods_walk for small systems, where a thread per rod leaves most
+// SMs without a warp (a 2,000-rod colony: 63 warps).  The same side outputs (segment data,
+// hi / lo split), the same boxes in the same phases, and per box the lanes test 32
+// candidates at a time; a prefix sum over the lanes' pass counts (0, 1 or 2 per candidate)
+// puts every pass where k_rods_walk puts it within the rod's range.  One reservation per
+// rod; a range's place in the list does not change any result (k_rods_update sums each
+// rod's passes in range order).
+template <int D, int NV>
+__global__ void __launch_bounds__(128) k_rods_walk_warp(const PackArgs P) {
+  constexpr int NC = NV * D, NE = NV - 1;
+  const int lane = threadIdx.x & 31;
+  const uint32_t i = (uint32_t)(((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i >= P.n_agents) return;  // whole warps
+  const int64_t cap = P.cap;
+  const uint32_t sim = (P.n_sims == 1) ? 0u : sim_of_agent(P, i);
+  const SimDev &S = P.sims[sim];
+  const bool live = !sim_frozen(P, S);
+  if (P.seg) {  // FP64: segment data, one segment per lane
+    for (int sy = lane; sy < NE; sy += 32) {
+      double ab[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+        ab[c] = dsub(P.pos[((sy + 1) * D + c) * cap + i], P.pos[(sy * D + c) * cap + i]);
+      double nsq = dmul(ab[0], ab[0]);
+#pragma unroll
+      for (int c = 1; c < D; ++c) nsq = dadd(nsq, dmul(ab[c], ab[c]));
+      double *sg = P.seg + (int64_t)sy * (D + 2) * cap + i;
+#pragma unroll
+      for (int c = 0; c < D; ++c) sg[c * cap] = ab[c];
+      sg[D * cap] = nsq;
+      sg[(D + 1) * cap] = __drcp_rn(nsq);
+    }
+  }
+  if (P.hl && live) {  // mixed precision: hi / lo split, one coordinate per lane
+    for (int k = lane; k < NC; k += 32) {
+      const double x = P.pos[k * cap + i];
+      const float hi = __double2float_rn(x);
+      P.hl[k * cap + i] = make_float2(hi, __double2float_rn(dsub(x, (double)hi)));
+    }
+  }
+  uint32_t key = P.key[i];
+  if (key - S.voxel_off >= S.n_vox) {
+    if (live && lane == 0) invariant_failed(P.status, kSiteForceKey, i);
+    key = S.voxel_off;
+  }
+  const uint32_t v = key - S.voxel_off;
+  int idx[D];
+  unravel<D>(S, v, idx);
+  float amin[D], amax[D];
+  bool a_nan = false;
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const float o = P.off[k * cap + i];
+    a_nan |= !(o == o);
+    if (k < D) {
+      amin[k] = o;
+      amax[k] = o;
+    } else {
+      amin[k % D] = fminf(amin[k % D], o);
+      amax[k % D] = fmaxf(amax[k % D], o);
+    }
+  }
+  const SubRange sub_v = subdomain_range(S, v);
+  const float thr = P.prefilter ? sqrtf(S.filt_thr2) : __int_as_float(0x7f800000);
+  int lo[3] = {0, 0, 0}, nb[3] = {1, 1, 1};
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo[c] = idx[c] > 0 ? idx[c] - 1 : 0;
+    const int hi = idx[c] + 1 < S.nvox[c] ? idx[c] + 1 : S.nvox[c] - 1;
+    nb[c] = hi - lo[c] + 1;
+  }
+  const int n_box = nb[0] * nb[1] * nb[2];
+  const bool physical = S.weight_mode == CRG_WEIGHTS_PHYSICAL;
+  // emit(k, b, meta): the rod's k-th pass (k counted from 0 in k_rods_walk's order)
+  auto walk = [&](auto &&emit) -> uint32_t {
+    uint32_t pos = 0;  // passes before this round (the same on every lane)
+    for (int phase = 0; phase < 3; ++phase)
+      for (int o = 0; o < n_box; ++o) {
+        const int j2 = lo[2] + o % nb[2];
+        const int j1 = lo[1] + (o / nb[2]) % nb[1];
+        const int j0 = lo[0] + o / (nb[1] * nb[2]);
+        const uint32_t w = (D == 3) ? ((uint32_t)j0 * S.nvox[1] + j1) * S.nvox[2] + j2
+                                    : (uint32_t)j0 * S.nvox[1] + j1;
+        const bool same = (w == v);
+        const bool local = physical || sub_v.same(w);
+        if (local != (phase == 0)) continue;
+        const bool twice = phase == 0 && (same || physical);
+        const int dj[3] = {j0 - idx[0], j1 - idx[1], D == 3 ? j2 - idx[D - 1] : 0};
+        float kd[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) kd[c] = (float)dj[c] * S.dxf[c];
+        const uint32_t box = (uint32_t)((dj[0] + 1) | ((dj[1] + 1) << 2) | ((dj[2] + 1) << 4));
+        const uint32_t b0 = P.start[S.voxel_off + w];
+        uint32_t b_end = P.start[S.voxel_off + w + 1];
+        if (b0 > b_end || b_end > P.n_agents) {
+          if (lane == 0) invariant_failed(P.status, kSiteForceRange, S.voxel_off + w);
+          b_end = b0;
+        }
+        for (uint32_t base = b0; base < b_end; base += 32) {
+          const uint32_t b = base + lane;
+          uint32_t np = 0, m0 = 0, m1 = 0;
+          if (b < b_end && b != i) {
+            float bmin[D], bmax[D];
+            bool b_nan = false;
+#pragma unroll
+            for (int k = 0; k < NC; ++k) {
+              const float o2 = P.off[k * cap + b] + kd[k % D];
+              b_nan |= !(o2 == o2);
+              if (k < D) {
+                bmin[k] = o2;
+                bmax[k] = o2;
+              } else {
+                bmin[k % D] = fminf(bmin[k % D], o2);
+                bmax[k % D] = fmaxf(bmax[k % D], o2);
+              }
+            }
+            bool far = false;
+            if (!a_nan && !b_nan) {
+#pragma unroll
+              for (int c = 0; c < D; ++c)
+                far |= (bmin[c] - amax[c] > thr) || (amin[c] - bmax[c] > thr);
+            }
+            if (!far) {
+              if (phase == 2) {
+                np = 1;
+                m0 = (box << 1) | 1u | kPassGroup;  // step 3: ext_a(b), summed per box
+              } else if (!twice) {
+                np = 1;
+                m0 = box << 1;  // own_a(b) only: a neighbour voxel, or step 2
+              } else {
+                const uint32_t ext_first = (same && b < i) ? 1u : 0u;
+                np = 2;
+                m0 = (box << 1) | ext_first;
+                m1 = (box << 1) | (ext_first ^ 1u);
+              }
+            }
+          }
+          uint32_t incl = np;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += y;
+          }
+          const uint32_t k = pos + incl - np;
+          if (np >= 1) emit(k, b, m0);
+          if (np == 2) emit(k + 1, b, m1);
+          pos += __shfl_sync(0xffffffffu, incl, 31);
+        }
+      }
+    return pos;
+  };
+  const uint32_t count = live ? walk([](uint32_t, uint32_t, uint32_t) {}) : 0u;
+  uint32_t first = 0;
+  if (lane == 0) {
+    if (count) {
+      first = atomicAdd(&P.rctl[0], count);
+      const uint64_t end = (uint64_t)first + count;
+      atomicMax(&P.status[5], (int32_t)(end < 0x7fffffffull ? end : 0x7fffffffull));
+    }
+    P.npass[i] = count;
+    P.pass_off[i] = first;
+  }
+  first = __shfl_sync(0xffffffffu, first, 0);
+  if (!count) return;
+  if ((uint64_t)first + count > (uint64_t)P.pass_cap) {
+    if (lane == 0) P.rctl[3] = 1u;
+    return;
+  }
+  walk([&](uint32_t k, uint32_t b, uint32_t meta) {
+    P.pass_a[first + k] = i;
+    P.pass_b[first + k] = b;
+    P.pass_meta[first + k] = (uint8_t)meta;
+  });
+}
+
 // The passes of the list, 32 consecutive ones per warp and round: every lane carries a pass
 // until the list drains, however the passes are spread over rods.  Per pass: the FP32 scan
 // of the vertex/segment pairs, the FP64 evaluation and row folds of eval_fold_queue, and
@@ -1922,6 +2097,10 @@ __global__ void k_cycle_counters(const PackArgs P) {
   P.vctr[v] += 2ull * (uint64_t)(P.dpre[P.start[v + 1]] - P.dpre[P.start[v]]);
 }
 
+// Largest rod count the default walk runs with a warp per rod (below it a thread per rod
+// leaves most SMs idle).
+constexpr uint32_t kWarpWalkMax = 16384;
+
 // Resident warps of k_rods_passq and resident blocks of k_rods_passmix on the current
 // device, [D - 2][NV] (set by prepare_rods).
 unsigned g_passq_warps[2][9] = {};
@@ -1930,7 +2109,6 @@ unsigned g_passmix_blocks[2][9] = {};
 template <int D, int NV>
 void launch_t(const PackArgs &P, int precision, int block, cudaStream_t st, cudaEvent_t k0,
               cudaEvent_t k1, cudaEvent_t k2, cudaEvent_t k3) {
-  (void)block;
   (void)precision;
   auto rec = [&](cudaEvent_t e) { record_event(e, st); };
   constexpr int B = 64;
@@ -1945,7 +2123,12 @@ void launch_t(const PackArgs &P, int precision, int block, cudaStream_t st, cuda
   const unsigned warps = (P.n_agents + 31) / 32;
   const unsigned rblocks = (P.n_agents + 127) / 128;
   cudaMemsetAsync(P.rctl, 0, 4 * sizeof(uint32_t), st);
-  k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
+  // walk: a warp per rod for small systems (block 32, or by default below kWarpWalkMax
+  // rods), else a thread per rod (block 128); the same pass list either way
+  if (block == 32 || (block != 128 && P.n_agents <= kWarpWalkMax))
+    k_rods_walk_warp<D, NV><<<(P.n_agents + 3) / 4, 128, 0, st>>>(P);
+  else
+    k_rods_walk<D, NV><<<rblocks, 128, 0, st>>>(P);
   rec(k0);
   if (mixed) {  // FP32 pair forces; each launch returns at once unless it is this step's
     const unsigned mgrid = g_passmix_blocks[D - 2][NV] ? g_passmix_blocks[D - 2][NV] : rblocks;

@@ -40,3 +40,25 @@ def test_pass_list_equals_rod_kernel(gpu, dim, n_sub):
             out.append(sim.download(order="id"))
     assert np.array_equal(out[0]["pos"], out[1]["pos"])
     assert np.array_equal(out[0]["vel"], out[1]["vel"])
+
+
+@pytest.mark.parametrize("precision,dim", [("f64", 2), ("mixed", 2), ("f64", 3)])
+def test_warp_walk_equals_thread_walk(gpu, precision, dim):
+    """The pass list walked with a warp per rod (CRG_OPT_BLOCK 32, the default for small
+    systems) and with a thread per rod (128): identical bits after 60 steps, 4 subdomains."""
+    w = W.rods(n=3000, side=360.0 if dim == 2 else 80.0, seed=41 + dim, dim=dim,
+               n_subdomains=4, precision=precision)
+    out = []
+    for block in (32, 128):
+        out.append(E.run(w, 60, options={N.OPT_BLOCK: block}))
+    for k in ("pos", "vel", "voxel"):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_warp_walk_colony(gpu):
+    """A dividing colony (agent count changing every few steps) walked both ways."""
+    w = W.rod_colony(n=150, seed=9, n_subdomains=2)
+    a = E.run(w, 150, order="list", options={N.OPT_BLOCK: 32})
+    b = E.run(w, 150, order="list", options={N.OPT_BLOCK: 128})
+    for k in ("ids", "parent", "pos", "vel", "spring_length"):
+        assert np.array_equal(a[k], b[k]), k
