@@ -1425,9 +1425,10 @@ int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block
   };
   std::vector<Shape> shapes;
   if (c->kind == CRG_KIND_ROD && c->precision != CRG_PREC_F64) {
-    shapes = {{0, 0, 0}};  // mixed-precision rods have one path
+    shapes = {{0, 0, 0}, {0, 32, 0}, {0, 128, 0}};  // one pass kernel, either walk
   } else if (c->kind == CRG_KIND_ROD) {
-    shapes = {{0, 0, 0}, {1, 64, 0}};
+    // pass list walked by size, with a warp or with a thread per rod; the rod-level kernel
+    shapes = {{0, 0, 0}, {0, 32, 0}, {0, 128, 0}, {1, 64, 0}};
   } else if (c->precision == CRG_PREC_F64) {
     // agent groups with 8 (block 0), 16 or 32 lanes per agent; lane per agent; thread per
     // agent, one-shot and persistent

@@ -290,7 +290,9 @@ const char *crg_strerror(int32_t code);
 /* ---- options and diagnostics ------------------------------------------------------- */
 #define CRG_OPT_PREFILTER 1  /* 1 (default): FP32 candidate prefilter on; 0: off */
 #define CRG_OPT_GRAPH_CHUNK 2 /* steps per captured CUDA graph (0 disables graphs) */
-#define CRG_OPT_BLOCK 3       /* threads per block of the force kernel (autotuner) */
+#define CRG_OPT_BLOCK 3       /* threads per block of the force kernel (autotuner); rods'
+                              * pass list: 32 walks with a warp per rod, 128 with a thread
+                              * per rod, 0 by size (a warp per rod up to 16,384 rods) */
 int32_t crg_set_option(crg_ctx *ctx, int32_t option, int64_t value);
 /* The current value of an option (CRG_OPT_PASS_LIST: the pass list's capacity in passes;
  * CRG_OPT_DEBUG_FORCES: 1 while forces are captured).  CRG_EINVAL for an unknown option. */
