@@ -273,6 +273,8 @@ int32_t fill_sim(const crg_domain &d, const crg_model &m, SimDev &S) {
     S.sense_in2 = (r > band) ? (float)(lo * lo) * (1.0f - 1e-6f) : -1.0f;
     S.sense_out2 = std::isfinite(hi) ? (float)(hi * hi) * (1.0f + 1e-6f) : __builtin_inff();
     if (!(r > 0.0)) S.sense_in2 = -1.0f;
+    // per-axis gap of the bounding boxes, rounded up (NaN stays NaN: nothing is skipped)
+    S.sense_gap_f = std::isfinite(hi) ? (float)hi + std::fabs((float)hi) * 1e-6f : (float)hi;
   }
   if (m.kind == CRG_KIND_ROD) {
     // mixed rods take their distances from hi / lo coordinates (relative error ~1e-6,

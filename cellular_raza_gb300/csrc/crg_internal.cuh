@@ -72,6 +72,8 @@ struct SimDev {
   // FP32 squared-distance bounds from the offsets: below sense_in2 a vertex pair is surely
   // closer than cyc_sense, above sense_out2 surely not; in between the FP64 test decides
   float sense_in2, sense_out2;
+  float sense_gap_f;  // bounding boxes of two rods' FP32 offsets further apart than this
+                      // along an axis hold no vertex pair closer than cyc_sense
 };
 
 // Arguments shared by the per-step kernels of a pack.

@@ -1858,24 +1858,22 @@ __global__ void __launch_bounds__(128) k_rods_sense(const PackArgs P) {
   }
   int idx[D];
   unravel<D>(S, key - S.voxel_off, idx);
-  double pa[NC], lo_a[D], hi_a[D];
+  double pa[NC];
 #pragma unroll
   for (int k = 0; k < NC; ++k) pa[k] = P.pos[k * cap + i];
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    lo_a[c] = hi_a[c] = pa[c];
-#pragma unroll
-    for (int q = 1; q < NV; ++q) {
-      lo_a[c] = fmin(lo_a[c], pa[q * D + c]);
-      hi_a[c] = fmax(hi_a[c], pa[q * D + c]);
-    }
-  }
-  const double r = S.cyc_sense;
-  const double thr = dadd(r, dmul(fabs(r), 1e-9));
   const long long x2 = S.cyc_sense_x2;  // sqrt(n2) < r exactly when bits(n2) <= x2
-  float oa[NC];
+  float oa[NC], lo_a[D], hi_a[D];  // FP32 offsets and their bounding box
 #pragma unroll
   for (int k = 0; k < NC; ++k) oa[k] = P.off[k * cap + i];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    lo_a[c] = hi_a[c] = oa[c];
+#pragma unroll
+    for (int q = 1; q < NV; ++q) {
+      lo_a[c] = fminf(lo_a[c], oa[q * D + c]);
+      hi_a[c] = fmaxf(hi_a[c], oa[q * D + c]);
+    }
+  }
   int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -1899,24 +1897,23 @@ __global__ void __launch_bounds__(128) k_rods_sense(const PackArgs P) {
         if (D == 3) kd[D - 1] = (float)(j2 - idx[D - 1]) * S.dxf[D - 1];
         for (uint32_t b = b0 + lane; b < b1; b += 32) {
           if (b == i) continue;
-          double pb[NC];
-#pragma unroll
-          for (int k = 0; k < NC; ++k) pb[k] = P.pos[k * cap + b];
-          bool far = false;
-#pragma unroll
-          for (int c = 0; c < D; ++c) {
-            double lb = pb[c], hb = pb[c];
-#pragma unroll
-            for (int q = 1; q < NV; ++q) {
-              lb = fmin(lb, pb[q * D + c]);
-              hb = fmax(hb, pb[q * D + c]);
-            }
-            far |= dsub(lb, hi_a[c]) > thr || dsub(lo_a[c], hb) > thr;
-          }
-          if (far) continue;
           float ob[NC];
 #pragma unroll
           for (int k = 0; k < NC; ++k) ob[k] = P.off[k * cap + b] + kd[k % D];
+          // bounding boxes further apart along an axis than the range plus the offsets'
+          // error band: no vertex pair can count (NaN offsets compare false: not skipped)
+          bool far = false;
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            float lb = ob[c], hb = ob[c];
+#pragma unroll
+            for (int q = 1; q < NV; ++q) {
+              lb = fminf(lb, ob[q * D + c]);
+              hb = fmaxf(hb, ob[q * D + c]);
+            }
+            far |= (lb - hi_a[c] > S.sense_gap_f) || (lo_a[c] - hb > S.sense_gap_f);
+          }
+          if (far) continue;
 #pragma unroll
           for (int u = 0; u < NV; ++u)
 #pragma unroll
@@ -1936,7 +1933,7 @@ __global__ void __launch_bounds__(128) k_rods_sense(const PackArgs P) {
               double n2 = 0.0;
 #pragma unroll
               for (int c = 0; c < D; ++c) {
-                const double d = dsub(pa[u * D + c], pb[q * D + c]);
+                const double d = dsub(pa[u * D + c], P.pos[(q * D + c) * cap + b]);
                 n2 = (c == 0) ? dmul(d, d) : dadd(n2, dmul(d, d));
               }
               // (own_point - ext_point).norm() < r (bacterial_rods/src/main.rs:49-64)
