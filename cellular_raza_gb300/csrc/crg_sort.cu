@@ -308,14 +308,27 @@ __global__ void k_gather(const SortArgs A) {
     invariant_failed(A.status, kSiteGatherSrc, s);
     src = s;
   }
+  // Loads before stores: the state arrays never overlap, but nothing tells the compiler,
+  // so a load written after a store waits for the store's order.  The key, id and the first
+  // four components are read together (one memory round trip for a sphere, not one per
+  // component), the rest four at a time below.
+  const int nc = A.nc;
+  const int64_t cap = A.cap;
   uint32_t k = A.nkey[src];
+  const uint64_t idv = A.nid[src];
+  double gp[4], gv[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (q < nc) {
+      gp[q] = A.npos[q * cap + src];
+      gv[q] = A.nvel[q * cap + src];
+    }
   if (k >= A.n_vox) {
     invariant_failed(A.status, kSiteGatherKey, s);
     k = 0;
   }
   A.key[s] = k;
-  A.id[s] = A.nid[src];
-  const int64_t cap = A.cap;
+  A.id[s] = idv;
   const uint32_t sim = (A.n_sims == 1) ? 0u : A.sim_of_voxel[k];
   const SimDev &S = A.sims[sim];
   int idx[3] = {0, 0, 0};
@@ -326,26 +339,41 @@ __global__ void k_gather(const SortArgs A) {
       v /= (uint32_t)S.nvox[i];
     }
   }
-  const int nc = A.nc;
   const int dim = S.dim;
+  // voxel_centre of the agent's voxel per axis, tabled (named, not an array: the axis of a
+  // component is only known at run time)
+  const double cen0 = A.vcen[S.cen_off[0] + idx[0]];
+  const double cen1 = A.vcen[S.cen_off[1] + idx[1]];
+  const double cen2 = dim == 3 ? A.vcen[S.cen_off[2] + idx[2]] : 0.0;
   float ov[3] = {0.f, 0.f, 0.f};  // spheres: written together, interleaved
-  for (int c = 0; c < nc; ++c) {
-    const double p = A.npos[c * cap + src];
-    A.pos[c * cap + s] = p;
-    A.vel[c * cap + s] = A.nvel[c * cap + src];
-    const int axis = c % dim;
-    const double centre = A.vcen[S.cen_off[axis] + idx[axis]];  // voxel_centre, tabled
-    float o = (float)(p - centre);
-    // Offsets far outside the voxel (an agent kept in its old voxel because its new index
-    // fell outside the grid) would weaken the prefilter's error bound: mark them NaN so
-    // every comparison involving them falls through to the exact FP64 path.
-    if (!(fabsf(o) <= S.off_lim)) o = __int_as_float(0x7fc00000);
-    if (A.off_aos) {
-      if (c == 0) ov[0] = o;
-      else if (c == 1) ov[1] = o;
-      else ov[2] = o;
-    } else {
-      A.off[c * cap + s] = o;
+  for (int c0 = 0; c0 < nc; c0 += 4) {
+    if (c0 > 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (c0 + q < nc) {
+          gp[q] = A.npos[(c0 + q) * cap + src];
+          gv[q] = A.nvel[(c0 + q) * cap + src];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + q;
+      if (c >= nc) break;
+      A.pos[c * cap + s] = gp[q];
+      A.vel[c * cap + s] = gv[q];
+      const int axis = c % dim;
+      float o = (float)(gp[q] - (axis == 0 ? cen0 : axis == 1 ? cen1 : cen2));
+      // Offsets far outside the voxel (an agent kept in its old voxel because its new
+      // index fell outside the grid) would weaken the prefilter's error bound: mark them
+      // NaN so every comparison involving them falls through to the exact FP64 path.
+      if (!(fabsf(o) <= S.off_lim)) o = __int_as_float(0x7fc00000);
+      if (A.off_aos) {
+        if (c == 0) ov[0] = o;
+        else if (c == 1) ov[1] = o;
+        else ov[2] = o;
+      } else {
+        A.off[c * cap + s] = o;
+      }
     }
   }
   if (A.off_aos == 4)
