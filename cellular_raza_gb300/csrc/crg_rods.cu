@@ -1227,14 +1227,17 @@ __global__ void __launch_bounds__(128) k_rods_walk(const PackArgs P) {
   const bool live = valid && !sim_frozen(P, S);  // frozen rods have no passes
   if (P.seg && valid) {
     // FP64: each segment's l1 - l0, squared norm and reciprocal for the pass kernel, with
-    // the operations of nearest_point_f64
+    // the operations of nearest_point_f64 (the coordinates are read first: a load written
+    // after a store would wait for it)
     constexpr int NE = NV - 1;
+    double x[NC];
+#pragma unroll
+    for (int k = 0; k < NC; ++k) x[k] = P.pos[k * cap + i];
 #pragma unroll
     for (int sy = 0; sy < NE; ++sy) {
       double ab[D];
 #pragma unroll
-      for (int c = 0; c < D; ++c)
-        ab[c] = dsub(P.pos[((sy + 1) * D + c) * cap + i], P.pos[(sy * D + c) * cap + i]);
+      for (int c = 0; c < D; ++c) ab[c] = dsub(x[(sy + 1) * D + c], x[sy * D + c]);
       double nsq = dmul(ab[0], ab[0]);
 #pragma unroll
       for (int c = 1; c < D; ++c) nsq = dadd(nsq, dmul(ab[c], ab[c]));
