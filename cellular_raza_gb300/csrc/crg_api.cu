@@ -8,6 +8,7 @@
 //   sort                 (crg_sort.cu: scan, scatter, per-voxel order, gather)
 // and runs on the handle's stream; steps are captured into CUDA graphs in chunks.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <limits>
 #include <cstdio>
@@ -1417,11 +1418,64 @@ int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
 }
 
 
+namespace {
+
+// Cell-cycle handles: every shape's trial starts from a host checkpoint (device snapshots
+// hold no cycle state) and is timed on the host clock (the cycle step reads its division
+// count every step).  The checkpoint loads with any capacity, so a trial that grew the
+// handle does not keep the next one from starting where the first did.
+int32_t autotune_cycle(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block,
+                       double *ms_per_step) {
+  const int shapes[4][2] = {{0, 0}, {0, 32}, {0, 128}, {1, 64}};
+  int64_t bytes = 0;
+  int32_t r = crg_checkpoint_size(c, &bytes);
+  if (r != CRG_OK) return r;
+  std::vector<char> blob((size_t)bytes);
+  if ((r = crg_checkpoint_save(c, blob.data(), bytes)) != CRG_OK) return r;
+  const int saved_variant = c->variant, saved_block = c->block;
+  int best_v = saved_variant, best_b = saved_block;
+  double best_ms = 1e300;
+  auto restore = [&]() {
+    c->grow_target = true;
+    const int32_t rr = crg_checkpoint_load(c, blob.data(), bytes);
+    c->grow_target = false;
+    return rr;
+  };
+  for (const auto &sh : shapes) {
+    c->variant = sh[0];
+    c->block = sh[1];
+    if ((r = restore()) != CRG_OK) break;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int32_t rs = crg_step(c, steps);
+    const auto t1 = std::chrono::steady_clock::now();
+    if (rs != CRG_OK) {  // a failing trial (the state's own error): keep the others
+      c->err_code = CRG_OK;
+      continue;
+    }
+    const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count() / steps;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_v = sh[0];
+      best_b = sh[1];
+    }
+  }
+  c->variant = best_v;
+  c->block = best_b;
+  const int32_t r2 = restore();
+  if (r != CRG_OK) return r;
+  if (variant) *variant = best_v;
+  if (block) *block = best_b;
+  if (ms_per_step) *ms_per_step = best_ms;
+  return r2;
+}
+
+}  // namespace
+
 int32_t crg_autotune(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *block,
                      double *ms_per_step) {
   if (!c || steps <= 0) return CRG_EINVAL;
-  if (c->cycle) return CRG_ENOTSUP;  // trials restore snapshots, which hold no cycle state
   if (c->err_code != CRG_OK) return c->err_code;
+  if (c->cycle) return autotune_cycle(c, steps, variant, block, ms_per_step);
   struct Shape {
     int variant, block, tile;
   };

@@ -277,7 +277,8 @@ int32_t crg_get_stream(crg_ctx *ctx, void **stream);
  * current state, restoring that state after each trial (crg_snapshot), and keeps the
  * fastest: *variant and *block receive the chosen CRG_OPT_KERNEL_VARIANT / CRG_OPT_BLOCK
  * values, *ms_per_step its time; the chosen CRG_OPT_TILE is read with crg_get_option.  The
- * simulation state is unchanged on return. */
+ * simulation state is unchanged on return.  Cell-cycle handles: the rod walk and kernel
+ * shapes, each trial started from a host checkpoint and timed on the host clock. */
 int32_t crg_autotune(crg_ctx *ctx, int64_t steps, int64_t *variant, int64_t *block,
                      double *ms_per_step);
 

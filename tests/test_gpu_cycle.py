@@ -103,3 +103,25 @@ def test_spring_lengths_only_before_the_first_step(gpu):
         assert e.value.code == N.CRG_EINVAL
         with pytest.raises(N.CrgError):
             sim.snapshot()
+
+
+def test_autotune_on_a_colony(gpu):
+    """The autotuner on a dividing colony: its trials start from a host checkpoint, the
+    state is unchanged afterwards, and the run goes on exactly as an untuned one."""
+    w = W.rod_colony(n=150, seed=8, n_subdomains=2)
+    ref = gpu_run(w, 60)
+    with E.Simulation.single(w.model, 16 * w.n) as sim:
+        sim.upload(w.pos, w.vel)
+        sim.set_spring_lengths(w.spring_length)
+        sim.step(30)
+        before = sim.download(order="list")
+        tune = sim.autotune(5)
+        assert tune["ms_per_step"] > 0
+        after = sim.download(order="list")
+        for k in ("ids", "pos", "vel", "spring_length"):
+            assert np.array_equal(before[k], after[k]), k
+        assert sim.steps_done == 30
+        sim.step(30)
+        got = sim.download(order="list")
+    for k in ("ids", "parent", "pos", "vel", "spring_length", "growth_rate"):
+        assert np.array_equal(got[k], ref[k]), k
