@@ -81,7 +81,9 @@ struct crg_ctx {
   int prefilter = 1;
   int variant = 0;
   int tile = 0;  // CRG_OPT_TILE
-  bool grow_target = false;  // created by grow_capacity: loads a checkpoint of any capacity
+  // set while the library itself loads a checkpoint of this handle taken at another
+  // capacity (growth of a cell-cycle handle, the autotuner's trials after a growth)
+  bool ckpt_any_capacity = false;
   int block = 0;
   int profile = 0;
   double prof_ms[5] = {0, 0, 0, 0, 0};
@@ -766,7 +768,7 @@ int32_t grow_capacity(crg_ctx *c, int64_t need) {
   crg_ctx *g = nullptr;
   r = create_impl(1, c->doms.data(), c->mods.data(), &new_cap, &g);
   if (r != CRG_OK) return r;
-  g->grow_target = true;
+  g->ckpt_any_capacity = true;
   g->graph_chunk = c->graph_chunk;
   g->prefilter = c->prefilter;
   g->variant = c->variant;
@@ -776,7 +778,7 @@ int32_t grow_capacity(crg_ctx *c, int64_t need) {
   if (c->dbg_force) r = crg_set_option(g, CRG_OPT_DEBUG_FORCES, 1);
   if (r == CRG_OK && c->pass_cap > g->pass_cap) r = alloc_pass_list(g, c->pass_cap);
   if (r == CRG_OK) r = crg_checkpoint_load(g, blob.data(), bytes);
-  g->grow_target = false;
+  g->ckpt_any_capacity = false;
   if (r != CRG_OK) {
     crg_destroy(g);
     return r;
@@ -1342,9 +1344,9 @@ int32_t crg_checkpoint_save(crg_ctx *c, void *buf, int64_t bytes) {
 
 int32_t crg_checkpoint_load(crg_ctx *c, const void *buf, int64_t bytes) {
   if (!c || !buf || bytes < (int64_t)sizeof(CkptHeader)) return CRG_EINVAL;
-  // a handle made to grow a cell-cycle handle (from the same domains and models) takes a
-  // checkpoint of another capacity, whose parameter hash differs in that field
-  const bool check_params = !c->grow_target;
+  // the library's own loads of a checkpoint of this simulation at another capacity, whose
+  // parameter hash differs in that field (the domains and models are the same)
+  const bool check_params = !c->ckpt_any_capacity;
   const char *p = (const char *)buf;
   CkptHeader h;
   std::memcpy(&h, p, sizeof(h));
@@ -1436,9 +1438,9 @@ int32_t autotune_cycle(crg_ctx *c, int64_t steps, int64_t *variant, int64_t *blo
   int best_v = saved_variant, best_b = saved_block;
   double best_ms = 1e300;
   auto restore = [&]() {
-    c->grow_target = true;
+    c->ckpt_any_capacity = true;
     const int32_t rr = crg_checkpoint_load(c, blob.data(), bytes);
-    c->grow_target = false;
+    c->ckpt_any_capacity = false;
     return rr;
   };
   for (const auto &sh : shapes) {
