@@ -252,8 +252,10 @@ __device__ __forceinline__ void bend_force(const SimDev &S, const double *c1, co
 // Mixed precision: the same curvature force with tan(angle / 2) from the half-angle
 // identity tan(theta / 2) = |c1 x c2| / (|c1| |c2| + c1 . c2), still in FP64 but without
 // acos and tan (about 40 % of the FP64 work of bend_force).  It agrees with the reference's
-// acos / tan to a few FP64 ulps away from folded rods; a rod folded back exactly (zero
-// denominator) takes tan(pi / 2) as the reference's FP64 evaluates it.
+// acos / tan to a few FP64 ulps for angles away from 0 and pi; near a straight rod the
+// reference's acos of a rounded cosine carries an absolute error up to ~1.5e-8 rad that the
+// cross product does not share (far inside the mixed path's error).  A rod folded back
+// exactly (zero denominator) takes tan(pi / 2) as the reference's FP64 evaluates it.
 template <int D>
 __device__ __forceinline__ void bend_force_halfangle(const SimDev &S, const double *c1,
                                                      const double *c2, double *f) {
