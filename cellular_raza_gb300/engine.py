@@ -283,6 +283,34 @@ def measure_fma_peaks():
     return {"fp64_tflops": a.value, "fp32_tflops": b.value}
 
 
+def resume_save_point(location: str, iteration: int, model: Model,
+                      capacity: Optional[int] = None) -> "Simulation":
+    """A handle holding the agents of a SerdeJson save point (written by
+    ``storage.export_cells``, or by chili's own ``save_cells`` for agents in the same
+    layout): positions, velocities and identifiers uploaded in the save point's storage
+    order, which makes the handle's cell list the saved one; with the cell cycle also the
+    spring lengths.  Solver history and the step counter are not part of a save point: an
+    AB2 / AB3 solver restarts with its first step and a stochastic stream from step 0.
+    ``capacity`` defaults to the agent count (16 times it with the cell cycle)."""
+    from . import storage as ST
+
+    recs = ST.load_cells(location, iteration)
+    st = ST.state_from_records(recs, model.kind, model.dim)
+    n = len(recs)
+    cycle = getattr(model, "cycle", False)
+    if capacity is None:
+        capacity = 16 * n if cycle else n
+    sim = Simulation.single(model, max(int(capacity), 1))
+    try:
+        sim.upload(st["pos"], st["vel"], ids=st["ids"])
+        if cycle:
+            sim.set_spring_lengths(st["spring_length"])
+    except Exception:
+        sim.close()
+        raise
+    return sim
+
+
 def run(workload, n_steps: Optional[int] = None, options: Optional[Dict[int, int]] = None,
         order: str = "id", capacity: Optional[int] = None) -> Dict[str, np.ndarray]:
     """Upload a workload, run it and return the final state (ordered by id by default).

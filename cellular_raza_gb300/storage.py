@@ -292,6 +292,48 @@ def load_cells(location: str, iteration: int) -> List[Dict]:
     return out
 
 
+def crg_id(identifier: Dict) -> int:
+    """The crg id of a CellIdentifier record (the inverse of `cell_identifier`)."""
+    if "Initial" in identifier:
+        return int(identifier["Initial"])
+    voxel, counter = identifier["Division"]
+    return ID_DIVISION | (int(voxel) << 32) | int(counter)
+
+
+def _floats(x) -> np.ndarray:
+    """Numbers of a record; serde_json writes non-finite numbers as null, read as NaN."""
+    return np.asarray([math.nan if v is None else v for v in x], dtype=np.float64)
+
+
+def state_from_records(records: List[Dict], kind: str, dim: int) -> Dict[str, np.ndarray]:
+    """The arrays of loaded records, in their storage order, as `Simulation.upload` and
+    `set_spring_lengths` take them: ``pos`` and ``vel`` (n, vertices, dim; zeros for
+    Brownian agents, which have no velocity), ``ids`` and ``parent`` (uint64, NO_PARENT for
+    none), and for rods ``spring_length``; with the cell cycle also ``growth_rate``."""
+    n = len(records)
+    pos, vel = [], []
+    for rec in records:
+        mech = rec["cell"]["mechanics"]
+        if kind == "rod":
+            p = _floats(mech["pos"][0]).reshape(dim, -1).T
+            v = _floats(mech["vel"][0]).reshape(dim, -1).T
+        else:
+            p = _floats(mech["pos"]).reshape(1, dim)
+            v = _floats(mech["vel"]).reshape(1, dim) if "vel" in mech else np.zeros((1, dim))
+        pos.append(p)
+        vel.append(v)
+    out = {"pos": np.asarray(pos).reshape(n, -1, dim), "vel": np.asarray(vel).reshape(n, -1, dim),
+           "ids": np.array([crg_id(r["identifier"]) for r in records], dtype=np.uint64),
+           "parent": np.array([NO_PARENT if r["parent"] is None else crg_id(r["parent"])
+                               for r in records], dtype=np.uint64)}
+    if kind == "rod":
+        out["spring_length"] = _floats([r["cell"]["mechanics"]["spring_length"]
+                                        for r in records])
+    if records and all("growth_rate" in r["cell"] for r in records):
+        out["growth_rate"] = _floats([r["cell"]["growth_rate"] for r in records])
+    return out
+
+
 def positions_of(records: List[Dict], kind: str, dim: int) -> np.ndarray:
     """Positions of loaded records, (n, vertices, dim), as the reference's plotting scripts
     read them (`cell.mechanics.pos`, rods: `pos[0]` reshaped to (dim, vertices))."""

@@ -118,3 +118,24 @@ def test_rod_colony_save_point_from_oracle(oracle, tmp_path):
         float(x) for x in res["spring_length"]]
     assert recs[0]["cell"]["spring_length_threshold"] == w.model.division_length
     assert recs[0]["cell"]["mechanics"]["pos"][1] == w.model.n_vertices
+
+
+def test_records_read_back_as_upload_arrays(oracle, tmp_path):
+    """state_from_records inverts the export: positions, velocities, identifiers, parents,
+    spring lengths and growth rates of oracle states come back bit for bit, in storage
+    order (spheres over four subdomains; a dividing rod colony)."""
+    w = W.spheres(500, 140.0, seed=6, dim=3, n_subdomains=4)
+    st = list_order(oracle.run(w.model, w.pos, w.vel, 8, debug=True))
+    S.export_cells(str(tmp_path / "s"), 8, w.model, st)
+    got = S.state_from_records(S.load_cells(str(tmp_path / "s"), 8), "sphere", 3)
+    assert np.array_equal(got["pos"], st["pos"]) and np.array_equal(got["vel"], st["vel"])
+    assert np.array_equal(got["ids"], st["ids"].astype(np.uint64))
+    assert np.all(got["parent"] == np.uint64(S.NO_PARENT))
+
+    c = W.rod_colony(n=60, side=200.0, seed=7, dim=2, n_subdomains=2)
+    res = oracle.run_cycle(c.model, c.pos, c.vel, 80, spring_length=c.spring_length)
+    S.export_cells(str(tmp_path / "r"), 80, c.model, res)
+    got = S.state_from_records(S.load_cells(str(tmp_path / "r"), 80), "rod", 2)
+    for k in ("pos", "vel", "ids", "parent", "spring_length", "growth_rate"):
+        assert np.array_equal(got[k], np.asarray(res[k]).astype(got[k].dtype)), k
+    assert S.crg_id({"Division": [12, 5]}) == S.ID_DIVISION | (12 << 32) | 5
