@@ -63,3 +63,9 @@ def test_options_need_a_handle():
     assert lib.crg_get_option(None, _native.OPT_TILE, ctypes.byref(v)) == _native.CRG_EINVAL
     assert lib.crg_set_option(None, _native.OPT_TILE, 1) == _native.CRG_EINVAL
     assert v.value == -1
+
+
+def test_integration_guide_binds_every_symbol():
+    """INTEGRATION.md (the Rust host's binding guide) names every function the ABI declares."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    assert [s for s in declared_symbols() if s not in text] == []
