@@ -255,6 +255,17 @@ class Simulation:
         off = struct.unpack_from(f"<{n + 1}I", blob, 56)
         self.counts = [off[s + 1] - off[s] for s in range(n)]
 
+    def save_point(self, location: str, iteration: int, aux=None) -> List[str]:
+        """Write the handle's state as a save point in chili's SerdeJson layout
+        (``storage.export_cells``; single-simulation handles); returns the files written.
+        ``engine.resume_save_point`` reads it back."""
+        from . import storage as ST
+
+        if len(self.models) != 1:
+            raise ValueError("save points are written per simulation: single handles only")
+        return ST.export_cells(location, iteration, self.models[0],
+                               self.download(order="list"), aux)
+
     def stream(self) -> int:
         s = C.c_void_p()
         N.check(self._L.crg_get_stream(self._h, C.byref(s)), "crg_get_stream")
